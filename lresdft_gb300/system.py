@@ -1,0 +1,228 @@
+"""Host-side system description: periodic crystal, H2 geometry generators and the
+LCAO-on-grid basis that the window solve consumes.
+
+This is one-time input preparation (the reference does it in numpy as well); the
+per-iteration work on these inputs runs on the GPU.  Arithmetic follows the
+reference operation by operation, so that the basis matrices (X, S, T) and
+therefore the window problems are the reference's to the last bit or two:
+
+* ``Crystal`` / ``h2_crystal``         lrft/three_d.py:41-87
+* ``LCAOBasis``                         lrft/lcao3d.py:49-100
+* ``cell_centres``                      lrft/lcao3d.py:287-289
+* ``fd_hamiltonian`` (FD kinetic part)  lrft/three_d.py:151-164
+* ``amorphous_h2`` (random sequential addition)  benchmarks/referee_checks.py:128-141
+
+Two generators have no reference counterpart and follow the workload definitions
+of the batched benchmark: ``cubic_h2`` (no jitter, bond along z) and
+``jittered_h2`` (uniform centre jitter, isotropic random bond axes).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+from scipy import sparse
+
+S_EXPS = (1.0, 0.3, 0.12)     # lrft/lcao3d.py:37
+P_EXPS = (0.5,)               # lrft/lcao3d.py:38
+
+
+@dataclass
+class Crystal:
+    """Periodic orthorhombic supercell sampled on a uniform grid (lrft/three_d.py:41-71)."""
+    pos: np.ndarray           # (natoms, 3) bohr
+    Z: np.ndarray             # (natoms,) ionic charges
+    cell: np.ndarray          # (3,) box lengths
+    shape: tuple              # grid points per axis
+    rc: float = 1.0           # erf softening radius of the local pseudopotential
+    rcs: np.ndarray = None
+    charge: int = 0
+
+    @property
+    def atom_rc(self):
+        return np.full(len(self.Z), self.rc) if self.rcs is None else np.asarray(self.rcs, float)
+
+    @property
+    def dx(self):
+        return self.cell[0] / self.shape[0]
+
+    @property
+    def n_elec(self):
+        return int(round(self.Z.sum())) - int(self.charge)
+
+    @property
+    def ng(self):
+        return int(np.prod(self.shape))
+
+    @property
+    def dV(self):
+        return float(np.prod(self.cell / np.array(self.shape)))
+
+
+def _crystal(pos, n, a, pts_per_cell, rc):
+    cell = a * np.array(n, float)
+    shape = tuple(int(pts_per_cell * m) for m in n)
+    return Crystal(np.array(pos), np.ones(len(pos)), cell, shape, rc)
+
+
+def h2_crystal(n=(2, 2, 2), a=4.5, bond=1.4, pts_per_cell=8, jitter=0.15, seed=0, rc=1.0):
+    """One H2 per cell, normal centre jitter, random axis (lrft/three_d.py:74-87)."""
+    rng = np.random.default_rng(seed)
+    pos = []
+    for i in range(n[0]):
+        for j in range(n[1]):
+            for k in range(n[2]):
+                c = (np.array([i, j, k]) + 0.5) * a + rng.normal(scale=jitter, size=3)
+                u = rng.normal(size=3)
+                u /= np.linalg.norm(u)
+                pos += [c - 0.5 * bond * u, c + 0.5 * bond * u]
+    return _crystal(pos, n, a, pts_per_cell, rc)
+
+
+def cubic_h2(n=(3, 3, 3), a=4.5, bond=1.4, pts_per_cell=8, rc=1.0):
+    """Simple-cubic H2 crystal: molecules at the cell centres, bonds along z, no jitter."""
+    pos = []
+    u = np.array([0.0, 0.0, 1.0])
+    for i in range(n[0]):
+        for j in range(n[1]):
+            for k in range(n[2]):
+                c = (np.array([i, j, k]) + 0.5) * a
+                pos += [c - 0.5 * bond * u, c + 0.5 * bond * u]
+    return _crystal(pos, n, a, pts_per_cell, rc)
+
+
+def jittered_h2(n=(8, 8, 8), a=4.5, bond=1.4, pts_per_cell=8, jitter=0.1, seed=0, rc=1.0):
+    """H2 crystal with centres displaced by U(-jitter, jitter) per axis and bond axes
+    uniform on the sphere (normalised N(0, I3)); same loop order and generator as
+    ``h2_crystal``."""
+    rng = np.random.default_rng(seed)
+    pos = []
+    for i in range(n[0]):
+        for j in range(n[1]):
+            for k in range(n[2]):
+                c = (np.array([i, j, k]) + 0.5) * a + rng.uniform(-jitter, jitter, size=3)
+                u = rng.normal(size=3)
+                u /= np.linalg.norm(u)
+                pos += [c - 0.5 * bond * u, c + 0.5 * bond * u]
+    return _crystal(pos, n, a, pts_per_cell, rc)
+
+
+def min_image(d, L):
+    """Minimum-image displacement (lrft/lcao3d.py:45-46)."""
+    return d - L * np.round(d / L)
+
+
+def amorphous_h2(nmol=512, box=36.0, dmin=3.0, bond=1.4, seed=7, shape=None, rc=1.0):
+    """Random sequential addition of H2 centres with a minimum centre distance, random
+    axes (benchmarks/referee_checks.py:128-141).  ``shape`` defaults to the
+    reference's 0.6 bohr spacing; returns (crystal, centres)."""
+    rng = np.random.default_rng(seed)
+    centres = []
+    L = np.full(3, box)
+    while len(centres) < nmol:
+        c = rng.uniform(0, box, 3)
+        if centres:
+            Q = np.array(centres)
+            if np.min(np.linalg.norm(min_image(c - Q, L), axis=1)) < dmin:
+                continue
+        centres.append(c)
+    pos = []
+    for c in centres:
+        u = rng.normal(size=3)
+        u /= np.linalg.norm(u)
+        pos += [c - 0.5 * bond * u, c + 0.5 * bond * u]
+    if shape is None:
+        m = int(round(box / 0.6))
+        shape = (m, m, m)
+    return Crystal(np.array(pos), np.ones(2 * nmol), np.full(3, float(box)), tuple(shape), rc), np.array(centres)
+
+
+def cell_centres(n, a):
+    """Centres of an n0 x n1 x n2 block of cubic cells (lrft/lcao3d.py:287-289)."""
+    g = np.array([[i, j, k] for i in range(n[0]) for j in range(n[1]) for k in range(n[2])], float)
+    return (g + 0.5) * a
+
+
+def fd_hamiltonian(cr: Crystal, v):
+    """Periodic 7-point finite-difference Hamiltonian -Lap/2 + v (lrft/three_d.py:151-164)."""
+    dx = cr.dx
+    idx = np.arange(cr.ng).reshape(cr.shape)
+    rows, cols = [], []
+    for ax in range(3):
+        for s in (1, -1):
+            rows.append(idx.ravel())
+            cols.append(np.roll(idx, s, axis=ax).ravel())
+    rows = np.concatenate(rows)
+    cols = np.concatenate(cols)
+    off = sparse.csr_matrix((np.full(rows.size, -0.5 / dx**2), (rows, cols)), shape=(cr.ng, cr.ng))
+    return (off + sparse.diags(v.ravel() + 3.0 / dx**2)).tocsr()
+
+
+class LCAOBasis:
+    """s/p Gaussians times the compact cutoff (1-(r/rcut)^2)^2 tabulated on the grid,
+    each normalised on the grid; S = X^T X dV and T = X^T T_FD X dV
+    (lrft/lcao3d.py:49-96).  Functions of one atom are contiguous and share one
+    support, which the GPU side uses to assemble H(v) by atom pairs."""
+
+    def __init__(self, cr: Crystal, rcut=5.5, s_exps=None, p_exps=None, atom_exps=None):
+        self.cr, self.rcut = cr, rcut
+        s_exps = S_EXPS if s_exps is None else s_exps
+        p_exps = P_EXPS if p_exps is None else p_exps
+        dx = cr.dx
+        n1, n2, n3 = cr.shape
+        rad = int(np.ceil(rcut / dx))
+        off = np.arange(-rad, rad + 1)
+        rows, cols, vals = [], [], []
+        atom_of_fn, fn_ptr = [], [0]
+        fn = 0
+        for a, R in enumerate(cr.pos):
+            if atom_exps is not None:
+                s_exps, p_exps = atom_exps[a]
+            c = np.round(R / dx).astype(int)
+            I, J, K = np.meshgrid(c[0] + off, c[1] + off, c[2] + off, indexing="ij")
+            P = np.stack([I, J, K], -1).reshape(-1, 3)
+            d = P * dx - R
+            d = min_image(d, cr.cell)
+            r = np.linalg.norm(d, axis=1)
+            m = r < rcut
+            P, d, r = P[m], d[m], r[m]
+            idx = np.ravel_multi_index((P[:, 0] % n1, P[:, 1] % n2, P[:, 2] % n3), cr.shape)
+            cut = (1 - (r / rcut) ** 2) ** 2
+            funcs = [np.exp(-al * r**2) * cut for al in s_exps]
+            for al in p_exps:
+                g = np.exp(-al * r**2) * cut
+                funcs += [d[:, 0] * g, d[:, 1] * g, d[:, 2] * g]
+            for f in funcs:
+                f = f / np.sqrt(np.sum(f**2) * cr.dV)
+                rows.append(idx)
+                cols.append(np.full(idx.size, fn))
+                vals.append(f)
+                atom_of_fn.append(a)
+                fn += 1
+            fn_ptr.append(fn)
+        self.nb = fn
+        self.atom_of_fn = np.array(atom_of_fn)
+        self.atom_fn_ptr = np.array(fn_ptr, dtype=np.int64)   # functions of atom a: [ptr[a], ptr[a+1])
+        self.X = sparse.csc_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
+                                   shape=(cr.ng, fn))
+        self.Xr = self.X.tocsr()
+        self._matrices()
+
+    def _matrices(self):
+        dV = self.cr.dV
+        self.S = (self.X.T @ self.X).tocsr() * dV
+        T = fd_hamiltonian(self.cr, np.zeros(self.cr.shape))
+        self.T = (self.X.T @ (T @ self.X)).tocsr() * dV
+
+    def H(self, v):
+        """Host reference of H(v) = T + X^T diag(v) X dV (lrft/lcao3d.py:98-100); the
+        GPU solver assembles H on the device instead."""
+        Xv = self.Xr.multiply(v.reshape(-1, 1)).tocsc()
+        return (self.T + (self.X.T @ Xv) * self.cr.dV).tocsr()
+
+
+def csr64(A):
+    """Sorted CSR with int64 indices (lrft/lcao3d.py:297-300)."""
+    A = A.tocsr()
+    A.sort_indices()
+    return (A.indptr.astype(np.int64), A.indices.astype(np.int64), np.ascontiguousarray(A.data, dtype=np.float64))
