@@ -1,0 +1,134 @@
+/*
+ * lres_gb300.h — C ABI of the GB300 (sm_103a) LRes-DFT LCAO window solve.
+ *
+ * Plain C: fixed-width integers, doubles and raw pointers; no C++ or torch types.
+ * Every function returns 0 (LRES_OK) or a negative LRES_E* code; the message of the
+ * last failure on the calling thread is available from lres_last_error().  No
+ * exception crosses the ABI.  A context is bound to the CUDA device that was current
+ * when it was created and is not thread-safe: calls on one context must not overlap.
+ * `stream` arguments are cudaStream_t values passed as void* (NULL = legacy default
+ * stream); every call is stream-ordered and returns after enqueueing its work, except
+ * calls that hand results back in host memory, which synchronise that stream.
+ *
+ * Conventions of the data (all identical to the reference's):
+ *   grid index    ravel of (i, j, k) with k fastest, shape (n1, n2, n3)
+ *   CSR arrays    int64 indptr / indices (sorted within rows), float64 values
+ *   windows       Wflat/Woff: basis functions of window w are Wflat[Woff[w]:Woff[w+1]] (ascending)
+ *   ownership     Oflat/Ooff: grid points owned by window w (disjoint, covering the grid)
+ *   density       electrons / bohr^3 with the spin factor 2 included (lrft/lcao3d.py:456)
+ *
+ * Reference interfaces replaced (albert-hzbn/LResDFT):
+ *   lres_ctx_create + lres_set_potential + lres_pass   replace one call of
+ *       _lrft_cpp.lrft_windows (src/lrft_cpp.cpp:129-233), bound at lrft/lcao3d.py:359-366,
+ *       and the host H(v) assembly LCAOBasis.H (lrft/lcao3d.py:98-100).  The eigenpair
+ *       outputs (lam, c, y2) of lrft_windows have no counterpart: the pole route yields the
+ *       window density, electron count and band energy directly (see lres_pass).
+ *   lres_set_hamiltonian_csr    the CSR H argument of lrft_windows (Hp, Hi, Hv).
+ *   lres_inertia / lres_min_eig the role of lam.min() in the warm/cold decisions of
+ *       LRFTLCAOCpp._density (lrft/lcao3d.py:420,450-451).
+ *   lres_voronoi_owner          the ownership loop of LRFTLCAO.__init__ (lrft/lcao3d.py:139-151).
+ *   lres_lda_xc                 lrft/three_d.py:132-148
+ *   lres_hartree                lrft/three_d.py:122-129
+ *   lres_ion_potential          lrft/three_d.py:102-112,119 (erf part; no GTH short-range term)
+ */
+#ifndef LRES_GB300_H
+#define LRES_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    LRES_OK = 0,
+    LRES_EINVAL = -22,     /* bad argument or inconsistent input */
+    LRES_ENOMEM = -12,     /* device allocation failed */
+    LRES_ECUDA = -5,       /* CUDA runtime error */
+    LRES_ENUMERIC = -33,   /* a zero or non-finite pivot in some window (per-window status kept) */
+    LRES_ESTATE = -71      /* call out of order (e.g. lres_pass before a Hamiltonian was set) */
+};
+
+enum { LRES_FP64 = 0, LRES_MIXED = 1 };
+
+typedef struct lres_ctx lres_ctx;
+
+/* System description, host pointers; copied to the device by lres_ctx_create. */
+typedef struct {
+    int64_t nb;            /* basis functions */
+    int64_t shape[3];      /* grid shape; ng = shape[0]*shape[1]*shape[2] */
+    double cell[3];        /* orthorhombic box lengths (bohr) */
+    double dV;             /* grid volume element */
+    /* basis values on the grid: CSR, ng rows x nb columns */
+    const int64_t* Xp; const int64_t* Xi; const double* Xv;
+    /* overlap S and kinetic T = X^T T_FD X dV: CSR, nb x nb.  T may be NULL, then the
+       Hamiltonian can only be given with lres_set_hamiltonian_csr. */
+    const int64_t* Sp; const int64_t* Si; const double* Sv;
+    const int64_t* Tp; const int64_t* Ti; const double* Tv;
+    /* functions grouped by atom: group g owns functions [gptr[g], gptr[g+1]), at most
+       8 per group, all with the same support on the grid */
+    int64_t ngroups; const int64_t* gptr;
+    /* windows and owned grid points */
+    int64_t nwin;
+    const int64_t* Wflat; const int64_t* Woff;
+    const int64_t* Oflat; const int64_t* Ooff;
+} lres_system_desc;
+
+const char* lres_version(void);
+const char* lres_last_error(void);
+
+/* Create a context: uploads the system, builds the dense window overlaps S_W and the
+ * owned-point basis blocks F_W = X[own(w), W]^T, and for LRES_MIXED the FP64 Cholesky
+ * inverses L_W^-1 and F^_W = L_W^-1 F_W.  M is the (even) number of poles. */
+int lres_ctx_create(lres_ctx** out, const lres_system_desc* desc, int precision, int M, void* stream);
+int lres_ctx_destroy(lres_ctx* ctx);
+
+/* Set the Hamiltonian H = T + X^T diag(v) X dV from the local potential v[ng]
+ * (host or device pointer as v_on_device says): assembled on the GPU by atom pairs,
+ * then gathered into the dense window blocks H_W (and H^_W = L^-1 H_W L^-T in
+ * LRES_MIXED).  Requires T in the system description. */
+int lres_set_potential(lres_ctx* ctx, const double* v, int v_on_device, void* stream);
+
+/* Set the Hamiltonian from a host CSR matrix (any sorted pattern inside the window
+ * blocks), e.g. one built on the host with extra nonlocal terms. */
+int lres_set_hamiltonian_csr(lres_ctx* ctx, const int64_t* Hp, const int64_t* Hi, const double* Hv, void* stream);
+
+/* One pole pass at chemical potential mu and filter edge e_lo (e_lo < mu): all
+ * windows x M/2 upper-half-plane poles z_j = c + R exp(i pi (2j+1)/M), c = (mu+e_lo)/2,
+ * R = (mu-e_lo)/2, weights w_j = R exp(i pi (2j+1)/M) / M.  Writes
+ *   dens[ng]  spin-summed density on the grid (host or device pointer per dens_on_device;
+ *             NULL to skip the copy-out, the device copy stays in the context)
+ *   out[0]    electron count N(mu) = dV sum dens
+ *   out[1]    band energy E_band = 2 sum_w tr(P^lambda_W O_W)
+ *   out[2]    number of windows whose factorisation met a zero / non-finite pivot
+ * and returns LRES_ENUMERIC when out[2] > 0. */
+int lres_pass(lres_ctx* ctx, double mu, double e_lo, double* dens, int dens_on_device, double* out, void* stream);
+
+/* Per-window electron counts and band energies of the last pass (host arrays of nwin). */
+int lres_window_sums(lres_ctx* ctx, double* n_w, double* e_w);
+
+/* Sylvester inertia of every window at shift sigma: below[w] = number of generalised
+ * eigenvalues of (H_W, S_W) below sigma (FP64 pivot-free LDL^T of sigma S_W - H_W).
+ * below may be NULL; *total receives the sum over windows. */
+int lres_inertia(lres_ctx* ctx, double sigma, int32_t* below, int64_t* total, void* stream);
+
+/* Smallest generalised eigenvalue over all windows by bisection on the inertia count,
+ * starting from the bracket [lo, hi] (widened if needed), to absolute width tol. */
+int lres_min_eig(lres_ctx* ctx, double lo, double hi, double tol, double* lam_min, void* stream);
+
+/* Voronoi ownership of the grid (lrft/lcao3d.py:139-151): owner[p] = index of the
+ * nearest centre in minimum-image distance, the lowest index on exact ties, with the
+ * reference's floating-point operation order.  Host arrays in and out. */
+int lres_voronoi_owner(const int64_t shape[3], const double cell[3], int64_t ncent, const double* centres,
+                       int32_t* owner);
+
+/* Grid kernels on device arrays of ng doubles (context supplies shape and cell). */
+int lres_lda_xc(lres_ctx* ctx, const double* dens, double* exc, double* vxc, void* stream);
+int lres_hartree(lres_ctx* ctx, const double* dens, double* vh, void* stream);
+int lres_ion_potential(lres_ctx* ctx, int64_t natoms, const double* pos, const double* Z, const double* rc,
+                       double* vion, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

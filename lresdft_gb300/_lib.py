@@ -1,0 +1,112 @@
+"""ctypes binding of liblres_gb300.so (include/lres_gb300.h).
+
+The library is built in-tree by ``lresdft_gb300.build``; importing this module
+loads it and raises if it is missing — there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liblres_gb300.so")
+
+LRES_FP64, LRES_MIXED = 0, 1
+ERRORS = {-22: "EINVAL", -12: "ENOMEM", -5: "ECUDA", -33: "ENUMERIC", -71: "ESTATE"}
+
+EXPORTS = ("lres_version", "lres_last_error", "lres_ctx_create", "lres_ctx_destroy", "lres_set_potential",
+           "lres_set_hamiltonian_csr", "lres_pass", "lres_window_sums", "lres_inertia", "lres_min_eig",
+           "lres_voronoi_owner", "lres_lda_xc", "lres_hartree", "lres_ion_potential")
+
+
+class LResError(RuntimeError):
+    """A failed call of the C ABI (code and message of lres_last_error)."""
+
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class NumericError(LResError):
+    """LRES_ENUMERIC: a zero / non-finite pivot in some window factorisation."""
+
+
+P64 = C.POINTER(C.c_int64)
+PD = C.POINTER(C.c_double)
+
+
+class SystemDesc(C.Structure):
+    _fields_ = [("nb", C.c_int64), ("shape", C.c_int64 * 3), ("cell", C.c_double * 3), ("dV", C.c_double),
+                ("Xp", P64), ("Xi", P64), ("Xv", PD),
+                ("Sp", P64), ("Si", P64), ("Sv", PD),
+                ("Tp", P64), ("Ti", P64), ("Tv", PD),
+                ("ngroups", C.c_int64), ("gptr", P64),
+                ("nwin", C.c_int64), ("Wflat", P64), ("Woff", P64), ("Oflat", P64), ("Ooff", P64)]
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} not built: run `python -m lresdft_gb300.build` (no CPU fallback)")
+    lib = C.CDLL(LIB_PATH)
+    vp, i32, i64, dbl = C.c_void_p, C.c_int, C.c_int64, C.c_double
+    sig = {
+        "lres_version": (C.c_char_p, []),
+        "lres_last_error": (C.c_char_p, []),
+        "lres_ctx_create": (i32, [C.POINTER(vp), C.POINTER(SystemDesc), i32, i32, vp]),
+        "lres_ctx_destroy": (i32, [vp]),
+        "lres_set_potential": (i32, [vp, vp, i32, vp]),
+        "lres_set_hamiltonian_csr": (i32, [vp, P64, P64, PD, vp]),
+        "lres_pass": (i32, [vp, dbl, dbl, vp, i32, PD, vp]),
+        "lres_window_sums": (i32, [vp, PD, PD]),
+        "lres_inertia": (i32, [vp, dbl, C.POINTER(C.c_int32), C.POINTER(i64), vp]),
+        "lres_min_eig": (i32, [vp, dbl, dbl, dbl, PD, vp]),
+        "lres_voronoi_owner": (i32, [P64, PD, i64, PD, C.POINTER(C.c_int32)]),
+        "lres_lda_xc": (i32, [vp, vp, vp, vp, vp]),
+        "lres_hartree": (i32, [vp, vp, vp, vp]),
+        "lres_ion_potential": (i32, [vp, i64, PD, PD, PD, vp, vp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype, f.argtypes = res, args
+    return lib
+
+
+lib = _load()
+
+
+def check(rc):
+    if rc:
+        msg = lib.lres_last_error().decode(errors="replace")
+        if rc == -33:
+            raise NumericError(rc, msg)
+        raise LResError(rc, msg)
+    return rc
+
+
+def ptr64(a):
+    return a.ctypes.data_as(P64)
+
+
+def ptrd(a):
+    return a.ctypes.data_as(PD)
+
+
+def i64(a):
+    return np.ascontiguousarray(a, dtype=np.int64)
+
+
+def f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def voronoi_owner(shape, cell, centres):
+    """Nearest-centre ownership of every grid point (GPU)."""
+    shape = i64(shape)
+    cell = f64(cell)
+    centres = f64(centres).reshape(-1, 3)
+    owner = np.empty(int(np.prod(shape)), np.int32)
+    check(lib.lres_voronoi_owner(ptr64(shape), ptrd(cell), centres.shape[0], ptrd(centres),
+                                 owner.ctypes.data_as(C.POINTER(C.c_int32))))
+    return owner

@@ -1,0 +1,851 @@
+// C ABI of liblres_gb300: context set-up, Hamiltonian updates, pole passes,
+// inertia counts and the grid kernels of the SCF step.  See include/lres_gb300.h.
+#include "common.cuh"
+#include "lres_internal.h"
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <memory>
+#include <cstdarg>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+static thread_local char g_err[1024] = "";
+
+extern "C" void lres_set_error(const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+extern "C" const char* lres_last_error(void) { return g_err; }
+extern "C" const char* lres_version(void) { return "lres_gb300 0.1 (sm_103a)"; }
+
+using namespace lres;
+
+namespace {
+
+template <class T>
+int dalloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * count);
+    if (e != cudaSuccess) {
+        lres_set_error("cudaMalloc of %zu bytes failed: %s", sizeof(T) * count, cudaGetErrorString(e));
+        return LRES_ENOMEM;
+    }
+    return LRES_OK;
+}
+
+template <class T>
+int upload(T** p, const std::vector<T>& v, cudaStream_t s) {
+    int rc = dalloc(p, v.size());
+    if (rc) return rc;
+    if (!v.empty()) LRES_CUDA_TRY(cudaMemcpyAsync(*p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, s));
+    return LRES_OK;
+}
+
+#define TRY(x)                 \
+    do {                       \
+        int _rc = (x);         \
+        if (_rc) return _rc;   \
+    } while (0)
+
+}  // namespace
+
+struct lres_ctx {
+    int device = 0, precision = 0, M = 0, npoles = 0;
+    int64_t nb = 0, ng = 0, shape[3] = {0, 0, 0};
+    double cell[3] = {0, 0, 0}, dV = 0;
+    int nwin = 0, ngroups = 0, nmax = 0, mmax = 0, nsm = 0;
+    long long npts = 0;
+    bool have_T = false, have_h = false;
+    size_t smem_budget = 0;
+    // host copies
+    std::vector<int> n_w, m_w, gptr_h, order;
+    std::vector<long long> offC, offF, offQ;
+    // device: windows
+    int *d_n = nullptr, *d_m = nullptr;
+    long long *d_offC = nullptr, *d_offF = nullptr, *d_offQ = nullptr, *d_Oflat = nullptr;
+    int *d_wgrp_off = nullptr, *d_wgrp = nullptr, *d_wgrp_lo = nullptr, *d_gloc = nullptr;
+    // block storage
+    BlockPattern bp;
+    Supports sp;
+    double *d_Sblk = nullptr, *d_Tblk = nullptr, *d_Hblk = nullptr;
+    std::vector<int> bptr_h, bcol_h;
+    std::vector<long long> boff_h;
+    // dense windows
+    double *d_SW = nullptr, *d_HW = nullptr, *d_F = nullptr;
+    double *d_LinvT = nullptr, *d_Y = nullptr, *d_Hhat = nullptr;
+    float *d_Hhat32 = nullptr, *d_Fhat32 = nullptr;
+    long long sizeC = 0, sizeF = 0;
+    // pole work
+    int2 *d_items = nullptr, *d_items_win = nullptr;
+    int nitems = 0;
+    int *d_counter = nullptr, *d_status = nullptr, *d_npos = nullptr;
+    void* d_ws = nullptr;
+    size_t ws_bytes = 0;
+    void* d_shifts = nullptr;
+    double2 *d_wq = nullptr, *d_wzq = nullptr;
+    void* d_q = nullptr;
+    double *d_dens = nullptr, *d_nw = nullptr, *d_ew = nullptr, *d_v = nullptr;
+    std::vector<double> nw_h, ew_h;
+    // grid
+    FFT3* fft = nullptr;
+    double2* d_fftwork = nullptr;
+    ~lres_ctx();
+};
+
+lres_ctx::~lres_ctx() {
+    void* ptrs[] = {d_n, d_m, d_offC, d_offF, d_offQ, d_Oflat, d_wgrp_off, d_wgrp, d_wgrp_lo, d_gloc,
+                    bp.gptr, bp.bptr, bp.bcol, bp.brow, bp.boff, bp.btrans, bp.pair_blk, sp.soff, sp.sgrid,
+                    sp.sval, sp.coff, sp.cslot, d_Sblk, d_Tblk, d_Hblk, d_SW, d_HW, d_F, d_LinvT, d_Y, d_Hhat,
+                    d_Hhat32, d_Fhat32, d_items, d_items_win, d_counter, d_status, d_npos, d_ws, d_shifts,
+                    d_wq, d_wzq, d_q, d_dens, d_nw, d_ew, d_v, d_fftwork};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (fft) fft3_destroy(fft);
+}
+
+namespace {
+
+// Runs the fused LDL^T kernel over `items` (device) with the given operands.
+int ldl_launch(lres_ctx* c, LdlJob::Kind kind, int nitems, const int2* items, const void* C, const void* B,
+               const void* F, const int* m_w, const long long* offF, const void* shifts, void* q, double* mult,
+               int ldp, int mmax, cudaStream_t s) {
+    LdlJob j{};
+    j.kind = kind;
+    j.nitems = nitems;
+    j.items = items;
+    j.counter = c->d_counter;
+    j.n_w = c->d_n;
+    j.m_w = m_w;
+    j.offC = c->d_offC;
+    j.offF = offF;
+    j.offQ = c->d_offQ;
+    j.C = C;
+    j.B = B;
+    j.F = F;
+    j.shifts = shifts;
+    j.q = q;
+    j.qstride = c->npts;
+    j.mult = mult;
+    j.npos = c->d_npos;
+    j.status = c->d_status;
+    j.ws = c->d_ws;
+    j.ldp = ldp;
+    j.nmax = c->nmax;
+    j.mmax = mmax;
+    const size_t el = kind == LdlJob::C128 ? 16 : 8;
+    j.ws_stride = (long long)(c->ws_bytes / el / c->nsm);
+    if ((long long)ldp * c->nmax > j.ws_stride) {
+        lres_set_error("workspace too small");
+        return LRES_EINVAL;
+    }
+    j.grid = c->nsm;
+    j.smem_budget = c->smem_budget;
+    LRES_CUDA_TRY(cudaMemsetAsync(c->d_counter, 0, sizeof(int), s));
+    return run_ldl(j, s);
+}
+
+int read_status(lres_ctx* c, cudaStream_t s, int* st) {
+    LRES_CUDA_TRY(cudaMemcpyAsync(st, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    LRES_CUDA_TRY(cudaStreamSynchronize(s));
+    return LRES_OK;
+}
+
+__global__ void identity_kernel(const int* n_w, const long long* off, double* I, int nwin) {
+    const int w = blockIdx.x;
+    if (w >= nwin) return;
+    const int n = n_w[w];
+    double* D = I + off[w];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) D[i + (long long)i * n] = 1.0;
+}
+
+int window_transform(lres_ctx* c, cudaStream_t s) {
+    // H^_W = L^-1 H_W L^-T with LinvT = L^-T stored column-major:  Y = H LinvT,  H^ = LinvT^T Y
+    TRY(batched_gemm(c->nwin, c->d_n, c->d_offC, c->nmax, false, c->d_HW, c->d_LinvT, c->d_Y, s));
+    TRY(batched_gemm(c->nwin, c->d_n, c->d_offC, c->nmax, true, c->d_LinvT, c->d_Y, c->d_Hhat, s));
+    TRY(convert_f64_f32(c->d_Hhat, c->d_Hhat32, c->sizeC, s));
+    return LRES_OK;
+}
+
+int after_h_blocks(lres_ctx* c, cudaStream_t s) {
+    LRES_CUDA_TRY(cudaMemsetAsync(c->d_HW, 0, sizeof(double) * c->sizeC, s));
+    TRY(gather_windows(c->bp, c->nwin, c->d_wgrp_off, c->d_wgrp, c->d_wgrp_lo, c->d_gloc, c->d_offC, c->d_n, c->nmax,
+                       c->d_Hblk, c->d_HW, s));
+    if (c->precision == LRES_MIXED) TRY(window_transform(c, s));
+    c->have_h = true;
+    return LRES_OK;
+}
+
+int find_block(const std::vector<int>& bptr, const std::vector<int>& bcol, int g, int h) {
+    auto b0 = bcol.begin() + bptr[g], b1 = bcol.begin() + bptr[g + 1];
+    auto it = std::lower_bound(b0, b1, h);
+    if (it == b1 || *it != h) return -1;
+    return (int)(it - bcol.begin());
+}
+
+int scatter_csr(const lres_ctx* c, const std::vector<int>& group_of_fn, const int64_t* Ap, const int64_t* Ai,
+                const double* Av, std::vector<double>& blk) {
+    blk.assign(c->bp.nval, 0.0);
+    for (int64_t a = 0; a < c->nb; ++a) {
+        const int g = group_of_fn[a];
+        const int fa = (int)(a - c->gptr_h[g]);
+        for (int64_t p = Ap[a]; p < Ap[a + 1]; ++p) {
+            const int64_t b = Ai[p];
+            if (b < 0 || b >= c->nb) {
+                lres_set_error("CSR column index %lld out of range", (long long)b);
+                return LRES_EINVAL;
+            }
+            const int h = group_of_fn[b];
+            const int blkid = find_block(c->bptr_h, c->bcol_h, g, h);
+            if (blkid < 0) {
+                lres_set_error("CSR entry (%lld,%lld) outside the atom-pair pattern", (long long)a, (long long)b);
+                return LRES_EINVAL;
+            }
+            const int nfh = c->gptr_h[h + 1] - c->gptr_h[h];
+            blk[c->boff_h[blkid] + fa * nfh + (b - c->gptr_h[h])] = Av[p];
+        }
+    }
+    return LRES_OK;
+}
+
+}  // namespace
+
+extern "C" int lres_ctx_create(lres_ctx** out, const lres_system_desc* d, int precision, int M, void* stream) {
+    if (!out || !d) {
+        lres_set_error("null argument");
+        return LRES_EINVAL;
+    }
+    *out = nullptr;
+    if (precision != LRES_FP64 && precision != LRES_MIXED) {
+        lres_set_error("precision must be LRES_FP64 or LRES_MIXED");
+        return LRES_EINVAL;
+    }
+    if (M < 2 || M % 2) {
+        lres_set_error("M must be even and >= 2 (got %d)", M);
+        return LRES_EINVAL;
+    }
+    if (!d->Xp || !d->Xi || !d->Xv || !d->Sp || !d->Si || !d->Sv || !d->gptr || !d->Wflat || !d->Woff ||
+        !d->Oflat || !d->Ooff || d->nb <= 0 || d->ngroups <= 0 || d->nwin <= 0) {
+        lres_set_error("incomplete system description");
+        return LRES_EINVAL;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    auto c = std::make_unique<lres_ctx>();
+    LRES_CUDA_TRY(cudaGetDevice(&c->device));
+    LRES_CUDA_TRY(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->device));
+    int optin = 0;
+    LRES_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
+    c->smem_budget = (size_t)optin - 1024;
+    c->precision = precision;
+    c->M = M;
+    c->npoles = M / 2;
+    c->nb = d->nb;
+    for (int i = 0; i < 3; ++i) {
+        c->shape[i] = d->shape[i];
+        c->cell[i] = d->cell[i];
+    }
+    c->ng = d->shape[0] * d->shape[1] * d->shape[2];
+    c->dV = d->dV;
+    c->nwin = (int)d->nwin;
+    c->ngroups = (int)d->ngroups;
+    c->have_T = d->Tp && d->Ti && d->Tv;
+    const int64_t nb = c->nb, ng = c->ng;
+
+    // ---- groups
+    c->gptr_h.resize(c->ngroups + 1);
+    for (int g = 0; g <= c->ngroups; ++g) c->gptr_h[g] = (int)d->gptr[g];
+    if (c->gptr_h[0] != 0 || c->gptr_h[c->ngroups] != nb) {
+        lres_set_error("gptr must start at 0 and end at nb");
+        return LRES_EINVAL;
+    }
+    std::vector<int> group_of_fn(nb);
+    int nfmax = 0;
+    for (int g = 0; g < c->ngroups; ++g) {
+        const int nf = c->gptr_h[g + 1] - c->gptr_h[g];
+        if (nf <= 0 || nf > 8) {
+            lres_set_error("group %d has %d functions (1..8 supported)", g, nf);
+            return LRES_EINVAL;
+        }
+        nfmax = std::max(nfmax, nf);
+        for (int f = c->gptr_h[g]; f < c->gptr_h[g + 1]; ++f) group_of_fn[f] = g;
+    }
+    c->bp.nfmax = nfmax;
+
+    // ---- supports of each group from the CSR rows of X (rows ascending -> slots sorted)
+    std::vector<long long> scount(c->ngroups + 1, 0);
+    std::vector<long long> last(c->ngroups, -1);
+    for (int64_t r = 0; r < ng; ++r)
+        for (int64_t p = d->Xp[r]; p < d->Xp[r + 1]; ++p) {
+            const int64_t f = d->Xi[p];
+            if (f < 0 || f >= nb) {
+                lres_set_error("X column index out of range");
+                return LRES_EINVAL;
+            }
+            const int g = group_of_fn[f];
+            if (last[g] != r) {
+                last[g] = r;
+                ++scount[g + 1];
+            }
+        }
+    std::vector<long long> soff(c->ngroups + 1, 0);
+    for (int g = 0; g < c->ngroups; ++g) soff[g + 1] = soff[g] + scount[g + 1];
+    const long long nslot = soff[c->ngroups];
+    std::vector<int> sgrid(nslot);
+    std::vector<double> sval((size_t)nslot * 8, 0.0);
+    std::vector<long long> cur(soff.begin(), soff.end() - 1);
+    std::fill(last.begin(), last.end(), -1);
+    for (int64_t r = 0; r < ng; ++r)
+        for (int64_t p = d->Xp[r]; p < d->Xp[r + 1]; ++p) {
+            const int f = (int)d->Xi[p];
+            const int g = group_of_fn[f];
+            if (last[g] != r) {
+                last[g] = r;
+                sgrid[cur[g]++] = (int)r;
+            }
+            sval[(size_t)(cur[g] - 1) * 8 + (f - c->gptr_h[g])] = d->Xv[p];
+        }
+    c->sp.nslot = nslot;
+
+    // ---- atom-pair block pattern: union of the S and T patterns, made symmetric
+    std::vector<std::vector<int>> nbr(c->ngroups);
+    {
+        std::vector<int> mark(c->ngroups, -1);
+        for (int g = 0; g < c->ngroups; ++g) {
+            nbr[g].push_back(g);
+            mark[g] = g;
+            for (int f = c->gptr_h[g]; f < c->gptr_h[g + 1]; ++f) {
+                for (int pass = 0; pass < 2; ++pass) {
+                    const int64_t* Ap = pass ? d->Tp : d->Sp;
+                    const int64_t* Ai = pass ? d->Ti : d->Si;
+                    if (!Ap) continue;
+                    for (int64_t p = Ap[f]; p < Ap[f + 1]; ++p) {
+                        const int64_t b = Ai[p];
+                        if (b < 0 || b >= nb) {
+                            lres_set_error("S/T column index out of range");
+                            return LRES_EINVAL;
+                        }
+                        const int h = group_of_fn[b];
+                        if (mark[h] != g) {
+                            mark[h] = g;
+                            nbr[g].push_back(h);
+                        }
+                    }
+                }
+            }
+        }
+        // symmetrise
+        std::vector<std::vector<int>> extra(c->ngroups);
+        for (int g = 0; g < c->ngroups; ++g)
+            for (int h : nbr[g]) extra[h].push_back(g);
+        for (int g = 0; g < c->ngroups; ++g) {
+            auto& v = nbr[g];
+            v.insert(v.end(), extra[g].begin(), extra[g].end());
+            std::sort(v.begin(), v.end());
+            v.erase(std::unique(v.begin(), v.end()), v.end());
+        }
+    }
+    c->bptr_h.assign(c->ngroups + 1, 0);
+    for (int g = 0; g < c->ngroups; ++g) c->bptr_h[g + 1] = c->bptr_h[g] + (int)nbr[g].size();
+    const int nblk = c->bptr_h[c->ngroups];
+    c->bcol_h.resize(nblk);
+    std::vector<int> brow(nblk), btrans(nblk);
+    c->boff_h.resize(nblk);
+    long long nval = 0;
+    for (int g = 0; g < c->ngroups; ++g)
+        for (int i = 0; i < (int)nbr[g].size(); ++i) {
+            const int b = c->bptr_h[g] + i, h = nbr[g][i];
+            c->bcol_h[b] = h;
+            brow[b] = g;
+            c->boff_h[b] = nval;
+            nval += (long long)(c->gptr_h[g + 1] - c->gptr_h[g]) * (c->gptr_h[h + 1] - c->gptr_h[h]);
+        }
+    std::vector<int> pair_blk, pair_g, pair_h;
+    for (int b = 0; b < nblk; ++b) {
+        btrans[b] = find_block(c->bptr_h, c->bcol_h, c->bcol_h[b], brow[b]);
+        if (brow[b] <= c->bcol_h[b]) {
+            pair_blk.push_back(b);
+            pair_g.push_back(brow[b]);
+            pair_h.push_back(c->bcol_h[b]);
+        }
+    }
+    c->bp.ngroups = c->ngroups;
+    c->bp.nblk = nblk;
+    c->bp.npair = (int)pair_blk.size();
+    c->bp.nval = nval;
+
+    // ---- windows: unions of whole groups, local offsets, group -> local map
+    c->n_w.resize(c->nwin);
+    c->m_w.resize(c->nwin);
+    c->offC.assign(c->nwin + 1, 0);
+    c->offF.assign(c->nwin + 1, 0);
+    c->offQ.assign(c->nwin + 1, 0);
+    std::vector<int> wgrp_off(c->nwin + 1, 0), wgrp, wgrp_lo;
+    std::vector<int> gloc((size_t)c->nwin * c->ngroups, -1);
+    for (int w = 0; w < c->nwin; ++w) {
+        const int64_t a0 = d->Woff[w], a1 = d->Woff[w + 1];
+        const int64_t o0 = d->Ooff[w], o1 = d->Ooff[w + 1];
+        if (a1 < a0 || o1 < o0 || (w == 0 && (a0 != 0 || o0 != 0))) {
+            lres_set_error("bad window / ownership offsets at window %d", w);
+            return LRES_EINVAL;
+        }
+        int64_t a = a0;
+        int lo = 0;
+        while (a < a1) {
+            const int64_t f = d->Wflat[a];
+            if (f < 0 || f >= nb) {
+                lres_set_error("window function index out of range");
+                return LRES_EINVAL;
+            }
+            const int g = group_of_fn[f];
+            const int nf = c->gptr_h[g + 1] - c->gptr_h[g];
+            if (f != c->gptr_h[g] || a + nf > a1) {
+                lres_set_error("window %d is not a union of whole atoms (function %lld)", w, (long long)f);
+                return LRES_EINVAL;
+            }
+            for (int k = 0; k < nf; ++k)
+                if (d->Wflat[a + k] != f + k) {
+                    lres_set_error("window %d lists the functions of atom %d out of order", w, g);
+                    return LRES_EINVAL;
+                }
+            if (gloc[(size_t)w * c->ngroups + g] >= 0) {
+                lres_set_error("window %d lists atom %d twice", w, g);
+                return LRES_EINVAL;
+            }
+            gloc[(size_t)w * c->ngroups + g] = lo;
+            wgrp.push_back(g);
+            wgrp_lo.push_back(lo);
+            lo += nf;
+            a += nf;
+        }
+        wgrp_off[w + 1] = (int)wgrp.size();
+        c->n_w[w] = (int)(a1 - a0);
+        c->m_w[w] = (int)(o1 - o0);
+        c->offC[w + 1] = c->offC[w] + (long long)c->n_w[w] * c->n_w[w];
+        c->offF[w + 1] = c->offF[w] + (long long)c->n_w[w] * c->m_w[w];
+        c->offQ[w] = o0;
+        c->offQ[w + 1] = o1;
+        c->nmax = std::max(c->nmax, c->n_w[w]);
+        c->mmax = std::max(c->mmax, c->m_w[w]);
+    }
+    c->npts = d->Ooff[c->nwin];
+    for (int64_t p = 0; p < c->npts; ++p)
+        if (d->Oflat[p] < 0 || d->Oflat[p] >= ng) {
+            lres_set_error("owned grid index out of range");
+            return LRES_EINVAL;
+        }
+    c->sizeC = c->offC[c->nwin];
+    c->sizeF = c->offF[c->nwin];
+
+    // ---- block values of S and T
+    std::vector<double> Sblk, Tblk;
+    TRY(scatter_csr(c.get(), group_of_fn, d->Sp, d->Si, d->Sv, Sblk));
+    if (c->have_T) TRY(scatter_csr(c.get(), group_of_fn, d->Tp, d->Ti, d->Tv, Tblk));
+    else Tblk.assign(nval, 0.0);
+
+    // ---- uploads
+    TRY(upload(&c->bp.gptr, c->gptr_h, s));
+    TRY(upload(&c->bp.bptr, c->bptr_h, s));
+    TRY(upload(&c->bp.bcol, c->bcol_h, s));
+    TRY(upload(&c->bp.brow, brow, s));
+    TRY(upload(&c->bp.boff, c->boff_h, s));
+    TRY(upload(&c->bp.btrans, btrans, s));
+    TRY(upload(&c->bp.pair_blk, pair_blk, s));
+    TRY(upload(&c->sp.soff, soff, s));
+    TRY(upload(&c->sp.sgrid, sgrid, s));
+    TRY(upload(&c->sp.sval, sval, s));
+    TRY(upload(&c->d_Sblk, Sblk, s));
+    TRY(upload(&c->d_Tblk, Tblk, s));
+    TRY(dalloc(&c->d_Hblk, nval));
+    TRY(upload(&c->d_n, c->n_w, s));
+    TRY(upload(&c->d_m, c->m_w, s));
+    TRY(upload(&c->d_offC, c->offC, s));
+    TRY(upload(&c->d_offF, c->offF, s));
+    TRY(upload(&c->d_offQ, c->offQ, s));
+    TRY(upload(&c->d_wgrp_off, wgrp_off, s));
+    TRY(upload(&c->d_wgrp, wgrp, s));
+    TRY(upload(&c->d_wgrp_lo, wgrp_lo, s));
+    TRY(upload(&c->d_gloc, gloc, s));
+    {
+        std::vector<long long> Oflat(d->Oflat, d->Oflat + c->npts);
+        TRY(upload(&c->d_Oflat, Oflat, s));
+    }
+    TRY(pair_common_points(c->bp, c->sp, c->ngroups, pair_g, pair_h, s));
+
+    // ---- dense window overlaps and owned-point blocks
+    TRY(dalloc(&c->d_SW, c->sizeC));
+    TRY(dalloc(&c->d_HW, c->sizeC));
+    LRES_CUDA_TRY(cudaMemsetAsync(c->d_SW, 0, sizeof(double) * c->sizeC, s));
+    TRY(gather_windows(c->bp, c->nwin, c->d_wgrp_off, c->d_wgrp, c->d_wgrp_lo, c->d_gloc, c->d_offC, c->d_n, c->nmax,
+                       c->d_Sblk, c->d_SW, s));
+    TRY(dalloc(&c->d_F, c->sizeF));
+    LRES_CUDA_TRY(cudaMemsetAsync(c->d_F, 0, sizeof(double) * c->sizeF, s));
+    {
+        long long* dXp = nullptr;
+        int* dXi = nullptr;
+        double* dXv = nullptr;
+        int* dgof = nullptr;
+        const int64_t nnz = d->Xp[ng];
+        std::vector<long long> Xp(d->Xp, d->Xp + ng + 1);
+        std::vector<int> Xi(nnz);
+        for (int64_t p = 0; p < nnz; ++p) Xi[p] = (int)d->Xi[p];
+        std::vector<double> Xv(d->Xv, d->Xv + nnz);
+        std::vector<long long> Ooff(d->Ooff, d->Ooff + c->nwin + 1);
+        long long* dOoff = nullptr;
+        TRY(upload(&dXp, Xp, s));
+        TRY(upload(&dXi, Xi, s));
+        TRY(upload(&dXv, Xv, s));
+        TRY(upload(&dgof, group_of_fn, s));
+        TRY(upload(&dOoff, Ooff, s));
+        int rc = build_F(c->nwin, dXp, dXi, dXv, dgof, c->bp.gptr, c->d_gloc, c->ngroups, dOoff, c->d_Oflat,
+                         c->d_offF, c->d_m, c->mmax, c->d_F, s);
+        LRES_CUDA_TRY(cudaStreamSynchronize(s));
+        cudaFree(dXp);
+        cudaFree(dXi);
+        cudaFree(dXv);
+        cudaFree(dgof);
+        cudaFree(dOoff);
+        if (rc) return rc;
+    }
+
+    // ---- work queue: windows by decreasing size (LPT), poles inner
+    c->order.resize(c->nwin);
+    std::iota(c->order.begin(), c->order.end(), 0);
+    std::stable_sort(c->order.begin(), c->order.end(), [&](int a, int b) {
+        const long long ca = (long long)c->n_w[a] * c->n_w[a] * (c->n_w[a] + 3 * c->m_w[a]);
+        const long long cb = (long long)c->n_w[b] * c->n_w[b] * (c->n_w[b] + 3 * c->m_w[b]);
+        return ca > cb;
+    });
+    std::vector<int2> items;
+    items.reserve((size_t)c->nwin * c->npoles);
+    for (int w : c->order)
+        for (int k = 0; k < c->npoles; ++k) items.push_back(make_int2(w, k));
+    c->nitems = (int)items.size();
+    TRY(upload(&c->d_items, items, s));
+    std::vector<int2> witems(c->nwin);
+    for (int w = 0; w < c->nwin; ++w) witems[w] = make_int2(w, 0);
+    TRY(upload(&c->d_items_win, witems, s));
+    TRY(dalloc(&c->d_counter, 1));
+    TRY(dalloc(&c->d_status, 1));
+    LRES_CUDA_TRY(cudaMemsetAsync(c->d_status, 0, sizeof(int), s));
+    TRY(dalloc(&c->d_npos, std::max(c->nitems, c->nwin)));
+
+    // workspace: one slot per SM, large enough for (n + n) x n real or (n + m) x n complex
+    const long long ldmax = std::max<long long>(c->nmax + c->mmax, 2LL * c->nmax);
+    const size_t slot = (size_t)ldmax * c->nmax * 16;
+    c->ws_bytes = slot * c->nsm;
+    TRY(dalloc((char**)&c->d_ws, c->ws_bytes));
+
+    // ---- standard form for the mixed path: L_c^-1 (as L^-T) and F^ = L_c^-1 F, FP64
+    if (precision == LRES_MIXED) {
+        TRY(dalloc(&c->d_LinvT, c->sizeC));
+        TRY(dalloc(&c->d_Y, c->sizeC));
+        TRY(dalloc(&c->d_Hhat, c->sizeC));
+        TRY(dalloc(&c->d_Hhat32, c->sizeC));
+        TRY(dalloc(&c->d_Fhat32, c->sizeF));
+        double* I = nullptr;
+        double* Fhat = nullptr;
+        double* one = nullptr;
+        TRY(dalloc(&I, c->sizeC));
+        TRY(dalloc(&Fhat, c->sizeF));
+        TRY(dalloc(&one, 1));
+        const double h_one = 1.0;
+        LRES_CUDA_TRY(cudaMemcpyAsync(one, &h_one, sizeof(double), cudaMemcpyHostToDevice, s));
+        LRES_CUDA_TRY(cudaMemsetAsync(I, 0, sizeof(double) * c->sizeC, s));
+        identity_kernel<<<c->nwin, 128, 0, s>>>(c->d_n, c->d_offC, I, c->nwin);
+        LRES_CUDA_TRY(cudaGetLastError());
+        LRES_CUDA_TRY(cudaMemsetAsync(c->d_status, 0, sizeof(int), s));
+        // A = 1*S - 0 with identity rows: multipliers sqrt(D) D^-1 L^-1 e_r = (L_c^-1)_{:,r}
+        int rc = ldl_launch(c.get(), LdlJob::R64, c->nwin, c->d_items_win, nullptr, c->d_SW, I, c->d_n, c->d_offC,
+                            one, nullptr, c->d_LinvT, 2 * c->nmax, c->nmax, s);
+        if (!rc)
+            rc = ldl_launch(c.get(), LdlJob::R64, c->nwin, c->d_items_win, nullptr, c->d_SW, c->d_F, c->d_m,
+                            c->d_offF, one, nullptr, Fhat, c->nmax + c->mmax, c->mmax, s);
+        if (!rc) rc = convert_f64_f32(Fhat, c->d_Fhat32, c->sizeF, s);
+        int st = 0;
+        if (!rc) rc = read_status(c.get(), s, &st);
+        cudaFree(I);
+        cudaFree(Fhat);
+        cudaFree(one);
+        if (rc) return rc;
+        if (st) {
+            lres_set_error("Cholesky of a window overlap S_W failed (status %d)", st);
+            return LRES_ENUMERIC;
+        }
+    }
+
+    // ---- pass buffers
+    TRY(dalloc((char**)&c->d_shifts, (size_t)c->npoles * 16));
+    TRY(dalloc(&c->d_wq, c->npoles));
+    TRY(dalloc(&c->d_wzq, c->npoles));
+    TRY(dalloc((char**)&c->d_q, (size_t)c->npoles * c->npts * (precision == LRES_MIXED ? 8 : 16)));
+    TRY(dalloc(&c->d_dens, ng));
+    TRY(dalloc(&c->d_v, ng));
+    TRY(dalloc(&c->d_nw, c->nwin));
+    TRY(dalloc(&c->d_ew, c->nwin));
+    LRES_CUDA_TRY(cudaMemsetAsync(c->d_dens, 0, sizeof(double) * ng, s));
+    c->nw_h.resize(c->nwin);
+    c->ew_h.resize(c->nwin);
+    TRY(fft3_create(&c->fft, c->shape));
+    TRY(dalloc(&c->d_fftwork, ng));
+    LRES_CUDA_TRY(cudaStreamSynchronize(s));
+    *out = c.release();
+    return LRES_OK;
+}
+
+extern "C" int lres_ctx_destroy(lres_ctx* c) {
+    if (!c) return LRES_OK;
+    cudaDeviceSynchronize();
+    delete c;
+    return LRES_OK;
+}
+
+extern "C" int lres_set_potential(lres_ctx* c, const double* v, int v_on_device, void* stream) {
+    if (!c || !v) {
+        lres_set_error("null argument");
+        return LRES_EINVAL;
+    }
+    if (!c->have_T) {
+        lres_set_error("lres_set_potential needs the kinetic matrix T in the system description");
+        return LRES_ESTATE;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    const double* dv = v;
+    if (!v_on_device) {
+        LRES_CUDA_TRY(cudaMemcpyAsync(c->d_v, v, sizeof(double) * c->ng, cudaMemcpyHostToDevice, s));
+        dv = c->d_v;
+    }
+    TRY(assemble_h(c->bp, c->sp, c->d_Tblk, dv, c->dV, c->d_Hblk, s));
+    return after_h_blocks(c, s);
+}
+
+extern "C" int lres_set_hamiltonian_csr(lres_ctx* c, const int64_t* Hp, const int64_t* Hi, const double* Hv,
+                                        void* stream) {
+    if (!c || !Hp || !Hi || !Hv) {
+        lres_set_error("null argument");
+        return LRES_EINVAL;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    std::vector<int> group_of_fn(c->nb);
+    for (int g = 0; g < c->ngroups; ++g)
+        for (int f = c->gptr_h[g]; f < c->gptr_h[g + 1]; ++f) group_of_fn[f] = g;
+    std::vector<double> blk;
+    TRY(scatter_csr(c, group_of_fn, Hp, Hi, Hv, blk));
+    LRES_CUDA_TRY(cudaMemcpyAsync(c->d_Hblk, blk.data(), sizeof(double) * blk.size(), cudaMemcpyHostToDevice, s));
+    TRY(after_h_blocks(c, s));
+    LRES_CUDA_TRY(cudaStreamSynchronize(s));   // blk is a host temporary
+    return LRES_OK;
+}
+
+extern "C" int lres_pass(lres_ctx* c, double mu, double e_lo, double* dens, int dens_on_device, double* out,
+                         void* stream) {
+    if (!c || !out) {
+        lres_set_error("null argument");
+        return LRES_EINVAL;
+    }
+    if (!c->have_h) {
+        lres_set_error("lres_pass before a Hamiltonian was set");
+        return LRES_ESTATE;
+    }
+    if (!(mu > e_lo) || !std::isfinite(mu) || !std::isfinite(e_lo)) {
+        lres_set_error("need finite e_lo < mu (got mu=%g, e_lo=%g)", mu, e_lo);
+        return LRES_EINVAL;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    const int P = c->npoles;
+    const double cc = 0.5 * (mu + e_lo), R = 0.5 * (mu - e_lo);
+    std::vector<double2> wq(P), wzq(P), z64(P);
+    std::vector<float2> z32(P);
+    for (int k = 0; k < P; ++k) {
+        // zeta_k = exp(i pi (2k+1)/M), z_k = c + R zeta_k, w_k = R zeta_k / M  (lrft/core.py:130-139)
+        const std::complex<double> zeta = std::exp(std::complex<double>(0.0, M_PI * (2 * k + 1) / c->M));
+        const std::complex<double> z = cc + R * zeta, w = R * zeta / (double)c->M, wz = w * z;
+        z64[k] = make_double2(z.real(), z.imag());
+        z32[k] = make_float2((float)z.real(), (float)z.imag());
+        wq[k] = make_double2(w.real(), w.imag());
+        wzq[k] = make_double2(wz.real(), wz.imag());
+    }
+    const bool mixed = c->precision == LRES_MIXED;
+    if (mixed) LRES_CUDA_TRY(cudaMemcpyAsync(c->d_shifts, z32.data(), sizeof(float2) * P, cudaMemcpyHostToDevice, s));
+    else LRES_CUDA_TRY(cudaMemcpyAsync(c->d_shifts, z64.data(), sizeof(double2) * P, cudaMemcpyHostToDevice, s));
+    LRES_CUDA_TRY(cudaMemcpyAsync(c->d_wq, wq.data(), sizeof(double2) * P, cudaMemcpyHostToDevice, s));
+    LRES_CUDA_TRY(cudaMemcpyAsync(c->d_wzq, wzq.data(), sizeof(double2) * P, cudaMemcpyHostToDevice, s));
+    LRES_CUDA_TRY(cudaMemsetAsync(c->d_status, 0, sizeof(int), s));
+    if (mixed)
+        TRY(ldl_launch(c, LdlJob::C64, c->nitems, c->d_items, c->d_Hhat32, nullptr, c->d_Fhat32, c->d_m, c->d_offF,
+                       c->d_shifts, c->d_q, nullptr, c->nmax + c->mmax, c->mmax, s));
+    else
+        TRY(ldl_launch(c, LdlJob::C128, c->nitems, c->d_items, c->d_HW, c->d_SW, c->d_F, c->d_m, c->d_offF,
+                       c->d_shifts, c->d_q, nullptr, c->nmax + c->mmax, c->mmax, s));
+    TRY(pole_sums(c->nwin, c->d_offQ, c->d_m, c->d_Oflat, mixed, c->d_q, c->npts, P, c->d_wq, c->d_wzq, c->dV,
+                  c->d_dens, c->d_nw, c->d_ew, s));
+    LRES_CUDA_TRY(cudaMemcpyAsync(c->nw_h.data(), c->d_nw, sizeof(double) * c->nwin, cudaMemcpyDeviceToHost, s));
+    LRES_CUDA_TRY(cudaMemcpyAsync(c->ew_h.data(), c->d_ew, sizeof(double) * c->nwin, cudaMemcpyDeviceToHost, s));
+    if (dens)
+        LRES_CUDA_TRY(cudaMemcpyAsync(dens, c->d_dens, sizeof(double) * c->ng,
+                                      dens_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+    int st = 0;
+    TRY(read_status(c, s, &st));
+    double N = 0.0, E = 0.0;
+    for (int w = 0; w < c->nwin; ++w) {
+        N += c->nw_h[w];
+        E += c->ew_h[w];
+    }
+    out[0] = N;
+    out[1] = E;
+    out[2] = (double)st;
+    if (st & ST_ZERO_PIVOT) {
+        lres_set_error("zero or non-finite pivot in a window factorisation");
+        return LRES_ENUMERIC;
+    }
+    if (st) {
+        lres_set_error("window kernel status %d", st);
+        return LRES_EINVAL;
+    }
+    return LRES_OK;
+}
+
+extern "C" int lres_window_sums(lres_ctx* c, double* n_w, double* e_w) {
+    if (!c) {
+        lres_set_error("null argument");
+        return LRES_EINVAL;
+    }
+    if (n_w) std::copy(c->nw_h.begin(), c->nw_h.end(), n_w);
+    if (e_w) std::copy(c->ew_h.begin(), c->ew_h.end(), e_w);
+    return LRES_OK;
+}
+
+extern "C" int lres_inertia(lres_ctx* c, double sigma, int32_t* below, int64_t* total, void* stream) {
+    if (!c) {
+        lres_set_error("null argument");
+        return LRES_EINVAL;
+    }
+    if (!c->have_h) {
+        lres_set_error("lres_inertia before a Hamiltonian was set");
+        return LRES_ESTATE;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    LRES_CUDA_TRY(cudaMemcpyAsync(c->d_shifts, &sigma, sizeof(double), cudaMemcpyHostToDevice, s));
+    LRES_CUDA_TRY(cudaMemsetAsync(c->d_status, 0, sizeof(int), s));
+    // positive pivots of (sigma S - H) = eigenvalues of (H, S) below sigma
+    TRY(ldl_launch(c, LdlJob::R64, c->nwin, c->d_items_win, c->d_HW, c->d_SW, nullptr, c->d_m, c->d_offF,
+                   c->d_shifts, nullptr, nullptr, c->nmax, 0, s));
+    std::vector<int> cnt(c->nwin);
+    LRES_CUDA_TRY(cudaMemcpyAsync(cnt.data(), c->d_npos, sizeof(int) * c->nwin, cudaMemcpyDeviceToHost, s));
+    LRES_CUDA_TRY(cudaStreamSynchronize(s));
+    int64_t t = 0;
+    for (int w = 0; w < c->nwin; ++w) {
+        t += cnt[w];
+        if (below) below[w] = cnt[w];
+    }
+    if (total) *total = t;
+    return LRES_OK;
+}
+
+extern "C" int lres_min_eig(lres_ctx* c, double lo, double hi, double tol, double* lam_min, void* stream) {
+    if (!c || !lam_min || !(hi > lo) || !(tol > 0)) {
+        lres_set_error("bad arguments to lres_min_eig");
+        return LRES_EINVAL;
+    }
+    int64_t t = 0;
+    for (int it = 0; it < 60; ++it) {   // lo must have no eigenvalue below it
+        TRY(lres_inertia(c, lo, nullptr, &t, stream));
+        if (t == 0) break;
+        const double wdt = hi - lo;
+        hi = lo;
+        lo -= 2 * wdt;
+        if (it == 59) {
+            lres_set_error("no lower bound found for the window spectra");
+            return LRES_ENUMERIC;
+        }
+    }
+    for (int it = 0; it < 60; ++it) {   // hi must have one below it
+        TRY(lres_inertia(c, hi, nullptr, &t, stream));
+        if (t > 0) break;
+        const double wdt = hi - lo;
+        lo = hi;
+        hi += 2 * wdt;
+        if (it == 59) {
+            lres_set_error("no upper bound found for the smallest window eigenvalue");
+            return LRES_ENUMERIC;
+        }
+    }
+    while (hi - lo > tol) {
+        const double mid = 0.5 * (lo + hi);
+        if (mid <= lo || mid >= hi) break;
+        TRY(lres_inertia(c, mid, nullptr, &t, stream));
+        if (t > 0) hi = mid; else lo = mid;
+    }
+    *lam_min = 0.5 * (lo + hi);
+    return LRES_OK;
+}
+
+extern "C" int lres_voronoi_owner(const int64_t shape[3], const double cell[3], int64_t ncent, const double* centres,
+                                  int32_t* owner) {
+    if (!shape || !cell || !centres || !owner || ncent <= 0) {
+        lres_set_error("bad arguments to lres_voronoi_owner");
+        return LRES_EINVAL;
+    }
+    const long long ng = shape[0] * shape[1] * shape[2];
+    double* dc = nullptr;
+    int* dow = nullptr;
+    TRY(dalloc(&dc, 3 * ncent));
+    int rc = dalloc(&dow, ng);
+    if (rc) {
+        cudaFree(dc);
+        return rc;
+    }
+    cudaStream_t s = 0;
+    rc = LRES_OK;
+    if (cudaMemcpy(dc, centres, sizeof(double) * 3 * ncent, cudaMemcpyHostToDevice) != cudaSuccess) rc = LRES_ECUDA;
+    if (!rc) rc = voronoi_apply(shape, cell, (int)ncent, dc, dow, s);
+    if (!rc && cudaMemcpy(owner, dow, sizeof(int) * ng, cudaMemcpyDeviceToHost) != cudaSuccess) rc = LRES_ECUDA;
+    if (rc == LRES_ECUDA) lres_set_error("voronoi: %s", cudaGetErrorString(cudaGetLastError()));
+    cudaFree(dc);
+    cudaFree(dow);
+    return rc;
+}
+
+extern "C" int lres_lda_xc(lres_ctx* c, const double* dens, double* exc, double* vxc, void* stream) {
+    if (!c || !dens || !exc || !vxc) {
+        lres_set_error("null argument");
+        return LRES_EINVAL;
+    }
+    return lda_apply(c->ng, dens, exc, vxc, (cudaStream_t)stream);
+}
+
+extern "C" int lres_hartree(lres_ctx* c, const double* dens, double* vh, void* stream) {
+    if (!c || !dens || !vh) {
+        lres_set_error("null argument");
+        return LRES_EINVAL;
+    }
+    return hartree_apply(c->fft, c->shape, c->cell, dens, vh, c->d_fftwork, (cudaStream_t)stream);
+}
+
+extern "C" int lres_ion_potential(lres_ctx* c, int64_t natoms, const double* pos, const double* Z, const double* rc,
+                                  double* vion, void* stream) {
+    if (!c || !pos || !Z || !rc || !vion || natoms <= 0) {
+        lres_set_error("bad arguments to lres_ion_potential");
+        return LRES_EINVAL;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    double *dp = nullptr, *dz = nullptr, *dr = nullptr;
+    TRY(dalloc(&dp, 3 * natoms));
+    TRY(dalloc(&dz, natoms));
+    TRY(dalloc(&dr, natoms));
+    LRES_CUDA_TRY(cudaMemcpyAsync(dp, pos, sizeof(double) * 3 * natoms, cudaMemcpyHostToDevice, s));
+    LRES_CUDA_TRY(cudaMemcpyAsync(dz, Z, sizeof(double) * natoms, cudaMemcpyHostToDevice, s));
+    LRES_CUDA_TRY(cudaMemcpyAsync(dr, rc, sizeof(double) * natoms, cudaMemcpyHostToDevice, s));
+    int r = ion_apply(c->fft, c->shape, c->cell, (int)natoms, dp, dz, dr, vion, c->d_fftwork, s);
+    cudaStreamSynchronize(s);
+    cudaFree(dp);
+    cudaFree(dz);
+    cudaFree(dr);
+    return r;
+}

@@ -1,0 +1,395 @@
+// Atom-pair assembly of H(v) = T + X^T diag(v) X dV, gathers of the dense window
+// blocks, the owned-point basis blocks F_W, a batched FP64 GEMM for the standard-form
+// transform, and the pole-weighted reductions to density / electron count / band
+// energy.  All bandwidth-bound except the GEMM.
+//
+// H(v) (lrft/lcao3d.py:98-100): functions of one atom share one support, so
+// H_gh = T_gh + dV sum_{r in supp g and supp h} v_r x_g(r) x_h(r)^T over the common
+// grid points of each overlapping atom pair, listed once per geometry.  Algorithmic
+// bytes per assembly: per common point 8 B slot pair + 8 B v + 2 x 8 x 8 B basis
+// values, plus the T and H blocks (8 B per stored value, read + write).
+#include "common.cuh"
+#include "lres_internal.h"
+
+#include <algorithm>
+#include <numeric>
+
+namespace lres {
+
+// ---------------------------------------------------------------------------
+// common points of overlapping atom pairs
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ long long lower_bound_int(const int* a, long long lo, long long hi, int key) {
+    while (lo < hi) {
+        long long mid = (lo + hi) >> 1;
+        if (a[mid] < key) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void pair_count_kernel(int npair, const int* pg, const int* ph, const long long* soff, const int* sgrid,
+                                  long long* counts) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= npair) return;
+    const int g = pg[warp], h = ph[warp];
+    const long long g0 = soff[g], g1 = soff[g + 1], h0 = soff[h], h1 = soff[h + 1];
+    long long c = 0;
+    for (long long s = g0 + lane; s < g1; s += 32) {
+        const int key = sgrid[s];
+        const long long pos = lower_bound_int(sgrid, h0, h1, key);
+        c += (pos < h1 && sgrid[pos] == key);
+    }
+    for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if (lane == 0) counts[warp] = c;
+}
+
+__global__ void pair_fill_kernel(int npair, const int* pg, const int* ph, const long long* soff, const int* sgrid,
+                                 const long long* coff, int2* cslot) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= npair) return;
+    const int g = pg[warp], h = ph[warp];
+    const long long g0 = soff[g], g1 = soff[g + 1], h0 = soff[h], h1 = soff[h + 1];
+    long long out = coff[warp];
+    for (long long base = g0; base < g1; base += 32) {
+        const long long s = base + lane;
+        bool hit = false;
+        long long pos = 0;
+        if (s < g1) {
+            const int key = sgrid[s];
+            pos = lower_bound_int(sgrid, h0, h1, key);
+            hit = pos < h1 && sgrid[pos] == key;
+        }
+        const unsigned mask = __ballot_sync(0xffffffffu, hit);
+        if (hit) {
+            const int before = __popc(mask & ((1u << lane) - 1u));
+            cslot[out + before] = make_int2((int)(s - g0), (int)(pos - h0));
+        }
+        out += __popc(mask);
+    }
+}
+
+int pair_common_points(const BlockPattern& bp, Supports& sp, int ngroups, const std::vector<int>& pair_g,
+                       const std::vector<int>& pair_h, cudaStream_t s) {
+    const int npair = (int)pair_g.size();
+    int *dg = nullptr, *dh = nullptr;
+    long long* dcount = nullptr;
+    LRES_CUDA_TRY(cudaMalloc(&dg, sizeof(int) * std::max(npair, 1)));
+    LRES_CUDA_TRY(cudaMalloc(&dh, sizeof(int) * std::max(npair, 1)));
+    LRES_CUDA_TRY(cudaMalloc(&dcount, sizeof(long long) * std::max(npair, 1)));
+    LRES_CUDA_TRY(cudaMemcpyAsync(dg, pair_g.data(), sizeof(int) * npair, cudaMemcpyHostToDevice, s));
+    LRES_CUDA_TRY(cudaMemcpyAsync(dh, pair_h.data(), sizeof(int) * npair, cudaMemcpyHostToDevice, s));
+    const int threads = 256, blocks = (int)(((long long)npair * 32 + threads - 1) / threads);
+    if (npair) pair_count_kernel<<<blocks, threads, 0, s>>>(npair, dg, dh, sp.soff, sp.sgrid, dcount);
+    LRES_CUDA_TRY(cudaGetLastError());
+    std::vector<long long> counts(npair), off(npair + 1, 0);
+    LRES_CUDA_TRY(cudaMemcpyAsync(counts.data(), dcount, sizeof(long long) * npair, cudaMemcpyDeviceToHost, s));
+    LRES_CUDA_TRY(cudaStreamSynchronize(s));
+    for (int p = 0; p < npair; ++p) off[p + 1] = off[p] + counts[p];
+    sp.ncommon = off[npair];
+    LRES_CUDA_TRY(cudaMalloc(&sp.coff, sizeof(long long) * (npair + 1)));
+    LRES_CUDA_TRY(cudaMalloc(&sp.cslot, sizeof(int2) * std::max<long long>(sp.ncommon, 1)));
+    LRES_CUDA_TRY(cudaMemcpyAsync(sp.coff, off.data(), sizeof(long long) * (npair + 1), cudaMemcpyHostToDevice, s));
+    if (npair) pair_fill_kernel<<<blocks, threads, 0, s>>>(npair, dg, dh, sp.soff, sp.sgrid, sp.coff, sp.cslot);
+    LRES_CUDA_TRY(cudaGetLastError());
+    LRES_CUDA_TRY(cudaStreamSynchronize(s));
+    cudaFree(dg);
+    cudaFree(dh);
+    cudaFree(dcount);
+    (void)bp;
+    (void)ngroups;
+    return LRES_OK;
+}
+
+// ---------------------------------------------------------------------------
+// H(v) assembly: one warp per overlapping pair (g <= h)
+// ---------------------------------------------------------------------------
+
+template <int NF>
+__global__ void __launch_bounds__(256) assemble_h_kernel(int npair, const int* pair_blk, const int* brow,
+                                                         const int* bcol, const long long* boff, const int* btrans,
+                                                         const int* gptr, const long long* soff, const int* sgrid,
+                                                         const double* sval, const long long* coff,
+                                                         const int2* cslot, const double* Tblk, const double* v,
+                                                         double dV, double* Hblk) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= npair) return;
+    const int b = pair_blk[warp];
+    const int g = brow[b], h = bcol[b];
+    const int nfg = gptr[g + 1] - gptr[g], nfh = gptr[h + 1] - gptr[h];
+    const long long sg0 = soff[g], sh0 = soff[h];
+    double acc[NF][NF];
+#pragma unroll
+    for (int f = 0; f < NF; ++f)
+#pragma unroll
+        for (int e = 0; e < NF; ++e) acc[f][e] = 0.0;
+    const long long c1 = coff[warp + 1];
+    for (long long c = coff[warp] + lane; c < c1; c += 32) {
+        const int2 ss = cslot[c];
+        const long long a = sg0 + ss.x, bb = sh0 + ss.y;
+        const double vv = v[sgrid[a]];
+        double xg[NF], xh[NF];
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+            xg[f] = sval[a * 8 + f];
+            xh[f] = sval[bb * 8 + f] * vv;
+        }
+#pragma unroll
+        for (int f = 0; f < NF; ++f)
+#pragma unroll
+            for (int e = 0; e < NF; ++e) acc[f][e] = fma(xg[f], xh[e], acc[f][e]);
+    }
+#pragma unroll
+    for (int f = 0; f < NF; ++f)
+#pragma unroll
+        for (int e = 0; e < NF; ++e) {
+            double x = acc[f][e];
+            for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+            acc[f][e] = x;
+        }
+    const long long o = boff[b];
+    const long long ot = boff[btrans[b]];
+#pragma unroll
+    for (int f = 0; f < NF; ++f)
+#pragma unroll
+        for (int e = 0; e < NF; ++e) {
+            if ((f * NF + e) % 32 != lane || f >= nfg || e >= nfh) continue;
+            const double val = Tblk[o + f * nfh + e] + acc[f][e] * dV;
+            Hblk[o + f * nfh + e] = val;
+            if (h != g) Hblk[ot + e * nfg + f] = Tblk[ot + e * nfg + f] + acc[f][e] * dV;
+        }
+}
+
+int assemble_h(const BlockPattern& bp, const Supports& sp, const double* Tblk, const double* v, double dV,
+               double* Hblk, cudaStream_t s) {
+    const int threads = 256;
+    const int blocks = (int)(((long long)bp.npair * 32 + threads - 1) / threads);
+    if (!bp.npair) return LRES_OK;
+    if (bp.nfmax <= 6)
+        assemble_h_kernel<6><<<blocks, threads, 0, s>>>(bp.npair, bp.pair_blk, bp.brow, bp.bcol, bp.boff, bp.btrans,
+                                                        bp.gptr, sp.soff, sp.sgrid, sp.sval, sp.coff, sp.cslot, Tblk,
+                                                        v, dV, Hblk);
+    else
+        assemble_h_kernel<8><<<blocks, threads, 0, s>>>(bp.npair, bp.pair_blk, bp.brow, bp.bcol, bp.boff, bp.btrans,
+                                                        bp.gptr, sp.soff, sp.sgrid, sp.sval, sp.coff, sp.cslot, Tblk,
+                                                        v, dV, Hblk);
+    LRES_CUDA_TRY(cudaGetLastError());
+    return LRES_OK;
+}
+
+// ---------------------------------------------------------------------------
+// dense window blocks from the block-sparse storage
+// ---------------------------------------------------------------------------
+
+__global__ void gather_windows_kernel(const int* bptr, const int* bcol, const long long* boff, const int* gptr,
+                                      const int* wgrp_off, const int* wgrp, const int* wgrp_lo, const int* gloc,
+                                      int ngroups, const long long* offC, const int* n_w, const double* blk,
+                                      double* dense) {
+    const int w = blockIdx.x;
+    const int n = n_w[w];
+    double* D = dense + offC[w];
+    const int* gl = gloc + (long long)w * ngroups;
+    const int i0 = wgrp_off[w], i1 = wgrp_off[w + 1];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
+    for (int i = i0 + warp; i < i1; i += nwarp) {
+        const int g = wgrp[i], lo = wgrp_lo[i];
+        const int nfg = gptr[g + 1] - gptr[g];
+        for (int b = bptr[g] + lane; b < bptr[g + 1]; b += 32) {
+            const int h = bcol[b];
+            const int lj = gl[h];
+            if (lj < 0) continue;
+            const int nfh = gptr[h + 1] - gptr[h];
+            const double* src = blk + boff[b];
+            for (int e = 0; e < nfh; ++e)
+                for (int f = 0; f < nfg; ++f) D[(lo + f) + (long long)(lj + e) * n] = src[f * nfh + e];
+        }
+    }
+}
+
+int gather_windows(const BlockPattern& bp, int nwin, const int* wgrp_off, const int* wgrp, const int* wgrp_lo,
+                   const int* gloc, const long long* offC, const int* n_w, int nmax, const double* blk,
+                   double* dense, cudaStream_t s) {
+    (void)nmax;
+    if (!nwin) return LRES_OK;
+    gather_windows_kernel<<<nwin, 256, 0, s>>>(bp.bptr, bp.bcol, bp.boff, bp.gptr, wgrp_off, wgrp, wgrp_lo, gloc,
+                                               bp.ngroups, offC, n_w, blk, dense);
+    LRES_CUDA_TRY(cudaGetLastError());
+    return LRES_OK;
+}
+
+// ---------------------------------------------------------------------------
+// F_W[r + a*m] = X[own_w[r], W[a]]
+// ---------------------------------------------------------------------------
+
+__global__ void build_F_kernel(const long long* Xp, const int* Xi, const double* Xv, const int* group_of_fn,
+                               const int* gptr, const int* gloc, int ngroups, const long long* Ooff,
+                               const long long* Oflat, const long long* offF, const int* m_w, double* F) {
+    const int w = blockIdx.x;
+    const int m = m_w[w];
+    const int* gl = gloc + (long long)w * ngroups;
+    double* Fw = F + offF[w];
+    for (int r = threadIdx.x; r < m; r += blockDim.x) {
+        const long long gpt = Oflat[Ooff[w] + r];
+        for (long long pidx = Xp[gpt]; pidx < Xp[gpt + 1]; ++pidx) {
+            const int f = Xi[pidx];
+            const int g = group_of_fn[f];
+            const int lo = gl[g];
+            if (lo < 0) continue;
+            Fw[r + (long long)(lo + f - gptr[g]) * m] = Xv[pidx];
+        }
+    }
+}
+
+int build_F(int nwin, const long long* Xp, const int* Xi, const double* Xv, const int* group_of_fn,
+            const int* gptr, const int* gloc, int ngroups, const long long* Ooff, const long long* Oflat,
+            const long long* offF, const int* m_w, int mmax, double* F, cudaStream_t s) {
+    (void)mmax;
+    if (!nwin) return LRES_OK;
+    build_F_kernel<<<nwin, 256, 0, s>>>(Xp, Xi, Xv, group_of_fn, gptr, gloc, ngroups, Ooff, Oflat, offF, m_w, F);
+    LRES_CUDA_TRY(cudaGetLastError());
+    return LRES_OK;
+}
+
+// ---------------------------------------------------------------------------
+// batched FP64 GEMM  C_w = op(A_w) B_w  (n_w x n_w, column-major, same offsets)
+// ---------------------------------------------------------------------------
+
+template <bool TA>
+__global__ void __launch_bounds__(256) gemm_f64_kernel(const int* n_w, const long long* off, const double* A,
+                                                       const double* B, double* C) {
+    constexpr int BM = 64, BN = 64, BK = 16;
+    const int w = blockIdx.z;
+    const int n = n_w[w];
+    const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+    if (m0 >= n || n0 >= n) return;
+    const double* Aw = A + off[w];
+    const double* Bw = B + off[w];
+    double* Cw = C + off[w];
+    __shared__ double As[BK][BM + 1];
+    __shared__ double Bs[BK][BN + 1];
+    const int tid = threadIdx.x;
+    const int tx = tid % 16, ty = tid / 16;   // 16 x 16 threads, 4 x 4 outputs each
+    double acc[4][4] = {};
+    for (int k0 = 0; k0 < n; k0 += BK) {
+        for (int idx = tid; idx < BK * BM; idx += 256) {
+            const int kk = idx / BM, i = idx % BM;
+            const int gi = m0 + i, gk = k0 + kk;
+            double a = 0.0;
+            if (gi < n && gk < n) a = TA ? Aw[gk + (long long)gi * n] : Aw[gi + (long long)gk * n];
+            As[kk][i] = a;
+        }
+        for (int idx = tid; idx < BK * BN; idx += 256) {
+            const int j = idx / BK, kk = idx % BK;
+            const int gj = n0 + j, gk = k0 + kk;
+            Bs[kk][j] = (gj < n && gk < n) ? Bw[gk + (long long)gj * n] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < BK; ++kk) {
+            double a[4], b[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) a[u] = As[kk][tx + 16 * u];
+#pragma unroll
+            for (int v = 0; v < 4; ++v) b[v] = Bs[kk][ty + 16 * v];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) acc[u][v] = fma(a[u], b[v], acc[u][v]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const int gi = m0 + tx + 16 * u, gj = n0 + ty + 16 * v;
+            if (gi < n && gj < n) Cw[gi + (long long)gj * n] = acc[u][v];
+        }
+}
+
+int batched_gemm(int nwin, const int* n_w, const long long* offA, int nmax, bool transA, const double* A,
+                 const double* B, double* C, cudaStream_t s) {
+    if (!nwin) return LRES_OK;
+    dim3 grid((nmax + 63) / 64, (nmax + 63) / 64, nwin);
+    if (transA) gemm_f64_kernel<true><<<grid, 256, 0, s>>>(n_w, offA, A, B, C);
+    else gemm_f64_kernel<false><<<grid, 256, 0, s>>>(n_w, offA, A, B, C);
+    LRES_CUDA_TRY(cudaGetLastError());
+    return LRES_OK;
+}
+
+__global__ void convert_kernel(const double* a, float* b, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+
+int convert_f64_f32(const double* a, float* b, long long n, cudaStream_t s) {
+    if (n <= 0) return LRES_OK;
+    convert_kernel<<<1216, 256, 0, s>>>(a, b, n);
+    LRES_CUDA_TRY(cudaGetLastError());
+    return LRES_OK;
+}
+
+// ---------------------------------------------------------------------------
+// pole sums: n(r) = 4 Re sum_k w_k q_k(r),  e(r) = 4 Re sum_k w_k z_k q_k(r)
+// (factor 2 for the conjugate half-plane, 2 for spin); one CTA per window,
+// fixed summation order (bitwise reproducible)
+// ---------------------------------------------------------------------------
+
+template <class T>
+__global__ void __launch_bounds__(256) pole_sum_kernel(const long long* offQ, const int* m_w, const long long* Oflat,
+                                                       const T* q, long long qstride, int npoles, const double2* wq,
+                                                       const double2* wzq, double dV, double* dens, double* n_out,
+                                                       double* e_out) {
+    const int w = blockIdx.x;
+    const int m = m_w[w];
+    const long long base = offQ[w];
+    double sn = 0.0, se = 0.0;
+    for (int r = threadIdx.x; r < m; r += blockDim.x) {
+        double an = 0.0, ae = 0.0;
+        for (int k = 0; k < npoles; ++k) {
+            const T x = q[(long long)k * qstride + base + r];
+            const double qx = (double)x.x, qy = (double)x.y;
+            const double2 a = wq[k], b = wzq[k];
+            an += a.x * qx - a.y * qy;
+            ae += b.x * qx - b.y * qy;
+        }
+        const double nr = 4.0 * an, er = 4.0 * ae;
+        dens[Oflat[base + r]] = nr;
+        sn += nr;
+        se += er;
+    }
+    __shared__ double red[2][256];
+    red[0][threadIdx.x] = sn;
+    red[1][threadIdx.x] = se;
+    __syncthreads();
+    for (int o = 128; o; o >>= 1) {
+        if (threadIdx.x < o) {
+            red[0][threadIdx.x] += red[0][threadIdx.x + o];
+            red[1][threadIdx.x] += red[1][threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        n_out[w] = red[0][0] * dV;
+        e_out[w] = red[1][0] * dV;
+    }
+}
+
+int pole_sums(int nwin, const long long* offQ, const int* m_w, const long long* Oflat, bool fp32, const void* q,
+              long long qstride, int npoles, const double2* wq, const double2* wzq, double dV, double* dens,
+              double* n_w, double* e_w, cudaStream_t s) {
+    if (!nwin) return LRES_OK;
+    if (fp32)
+        pole_sum_kernel<float2><<<nwin, 256, 0, s>>>(offQ, m_w, Oflat, (const float2*)q, qstride, npoles, wq, wzq, dV,
+                                                     dens, n_w, e_w);
+    else
+        pole_sum_kernel<double2><<<nwin, 256, 0, s>>>(offQ, m_w, Oflat, (const double2*)q, qstride, npoles, wq, wzq,
+                                                      dV, dens, n_w, e_w);
+    LRES_CUDA_TRY(cudaGetLastError());
+    return LRES_OK;
+}
+
+}  // namespace lres

@@ -1,0 +1,98 @@
+// Internal declarations shared by the translation units of liblres_gb300.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <vector>
+#include "../../include/lres_gb300.h"
+
+namespace lres {
+
+// One launch of the fused window LDL^T kernel (window_ldl.cu).
+struct LdlJob {
+    enum Kind { C128, C64, R64 } kind;
+    int nitems = 0;
+    const int2* items = nullptr;
+    int* counter = nullptr;
+    const int* n_w = nullptr;
+    const int* m_w = nullptr;
+    const long long* offC = nullptr;
+    const long long* offF = nullptr;
+    const long long* offQ = nullptr;
+    const void* C = nullptr;
+    const void* B = nullptr;
+    const void* F = nullptr;
+    const void* shifts = nullptr;
+    void* q = nullptr;
+    long long qstride = 0;
+    double* mult = nullptr;
+    int* npos = nullptr;
+    int* status = nullptr;
+    void* ws = nullptr;
+    long long ws_stride = 0;
+    int ldp = 0, nmax = 0, mmax = 0;
+    int grid = 0;
+    size_t smem_budget = 0;
+};
+
+int run_ldl(const LdlJob& j, cudaStream_t s);
+size_t ldl_smem_bytes(int elem_bytes, int nb, int ldp, int mmax);
+
+// Block-sparse (atom-pair) storage of the nb x nb matrices S, T, H.
+struct BlockPattern {
+    int ngroups = 0;
+    int nblk = 0;                     // stored blocks (both triangles)
+    int npair = 0;                    // blocks with g <= h (assembled by the H(v) kernel)
+    int nfmax = 0;                    // largest group (functions per atom)
+    // device arrays
+    int* gptr = nullptr;              // [ngroups+1] first function of each group
+    int* bptr = nullptr;              // [ngroups+1] blocks of block-row g: [bptr[g], bptr[g+1])
+    int* bcol = nullptr;              // [nblk] column group
+    int* brow = nullptr;              // [nblk] row group
+    long long* boff = nullptr;        // [nblk] value offset (nf_g * nf_h values, row-major)
+    int* btrans = nullptr;            // [nblk] index of the transposed block
+    int* pair_blk = nullptr;          // [npair] block index of pair p (g <= h)
+    long long nval = 0;
+};
+
+// Group supports on the grid and common-point lists of overlapping pairs.
+struct Supports {
+    long long nslot = 0;
+    long long* soff = nullptr;        // [ngroups+1] slot range of each group
+    int* sgrid = nullptr;             // [nslot] grid index of each slot
+    double* sval = nullptr;           // [nslot * 8] basis values, 8 per slot (zero padded)
+    long long ncommon = 0;
+    long long* coff = nullptr;        // [npair+1] common-point range of each pair
+    int2* cslot = nullptr;            // [ncommon] (slot in g, slot in h)
+};
+
+// Kernel launchers implemented in hamiltonian.cu / grid.cu / dense.cu
+int pair_common_points(const BlockPattern& bp, Supports& sp, int ngroups, const std::vector<int>& pair_g,
+                       const std::vector<int>& pair_h, cudaStream_t s);
+int assemble_h(const BlockPattern& bp, const Supports& sp, const double* Tblk, const double* v, double dV,
+               double* Hblk, cudaStream_t s);
+int gather_windows(const BlockPattern& bp, int nwin, const int* wgrp_off, const int* wgrp, const int* wgrp_lo,
+                   const int* gloc, const long long* offC, const int* n_w, int nmax, const double* blk,
+                   double* dense, cudaStream_t s);
+int build_F(int nwin, const long long* Xp, const int* Xi, const double* Xv, const int* group_of_fn,
+            const int* gptr, const int* gloc, int ngroups, const long long* Ooff, const long long* Oflat,
+            const long long* offF, const int* m_w, int mmax, double* F, cudaStream_t s);
+int batched_gemm(int nwin, const int* n_w, const long long* offA, int nmax, bool transA, const double* A,
+                 const double* B, double* C, cudaStream_t s);
+int convert_f64_f32(const double* a, float* b, long long n, cudaStream_t s);
+int pole_sums(int nwin, const long long* offQ, const int* m_w, const long long* Oflat, bool fp32,
+              const void* q, long long qstride, int npoles, const double2* wq, const double2* wzq, double dV,
+              double* dens, double* n_w, double* e_w, cudaStream_t s);
+
+struct FFT3;
+int fft3_create(FFT3** out, const int64_t shape[3]);
+void fft3_destroy(FFT3* f);
+int fft3_exec(FFT3* f, double2* data, int inverse, cudaStream_t s);
+int hartree_apply(FFT3* f, const int64_t shape[3], const double cell[3], const double* dens, double* vh,
+                  double2* work, cudaStream_t s);
+int lda_apply(long long n, const double* dens, double* exc, double* vxc, cudaStream_t s);
+int ion_apply(FFT3* f, const int64_t shape[3], const double cell[3], int natoms, const double* pos,
+              const double* Z, const double* rc, double* vion, double2* work, cudaStream_t s);
+int voronoi_apply(const int64_t shape[3], const double cell[3], int ncent, const double* centres, int* owner,
+                  cudaStream_t s);
+
+}  // namespace lres

@@ -1,0 +1,157 @@
+"""Parity of the sm_103a path (through the C ABI) with the reference's own outputs
+(tests/golden, produced by the reference code) and with the CPU oracle.
+
+Tolerances: FP64 path 1e-10 on densities, 1e-9 on band energies (the reference's own
+C++-vs-Python gate, tests/test_three_d.py:86-100) and 1e-10 Ha/electron on SCF
+energies; mixed path (complex64 factor/solve + FP64 refinement-free sums) 2e-7
+Ha/electron on energies."""
+import numpy as np
+import pytest
+
+from golden_util import check_basis, crystal, load
+
+pytestmark = pytest.mark.gpu
+
+CASES = ["jit2", "cubic3"]
+
+
+@pytest.fixture(scope="module")
+def systems():
+    from lresdft_gb300 import system
+    out = {}
+    for name in CASES:
+        g = load(name)
+        cr = crystal(g)
+        b = system.LCAOBasis(cr)
+        check_basis(b, g)
+        out[name] = (g, cr, b)
+    return out
+
+
+def _solver(b, cr, g, precision="fp64"):
+    from lresdft_gb300 import LResGPU
+    return LResGPU(b, cr.pos, R_w=float(g["R_w"]), M=int(g["M"]), precision=precision)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_voronoi_and_windows_match_reference(systems, name):
+    g, cr, b = systems[name]
+    s = _solver(b, cr, g)
+    assert np.array_equal(s.owner, g["owner"])
+    assert np.array_equal(s.Wflat, g["Wflat"])
+    s.close()
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("hpath", ["gpu", "csr"])
+def test_single_pass_matches_reference_density(systems, name, hpath):
+    """One pole pass at the reference's (mu, e_lo) reproduces its cold density call."""
+    g, cr, b = systems[name]
+    s = _solver(b, cr, g)
+    v = g["v"].reshape(cr.shape)
+    if hpath == "gpu":
+        s.set_potential(v)
+    else:
+        s.set_hamiltonian(b.H(v))
+    dens, N, eb = s.pole_pass(float(g["cold_mu"]), float(g["cold_elo"]))
+    assert np.max(np.abs(dens - g["cold_dens"])) < 1e-10
+    assert abs(eb - g["cold_eband"]) < 1e-9
+    assert abs(N - cr.n_elec) < 1e-7
+    s.close()
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_pass_is_bitwise_reproducible(systems, name):
+    g, cr, b = systems[name]
+    s = _solver(b, cr, g)
+    s.set_potential(g["v"].reshape(cr.shape))
+    a = s.pole_pass(float(g["cold_mu"]), float(g["cold_elo"]))
+    c = s.pole_pass(float(g["cold_mu"]), float(g["cold_elo"]))
+    assert np.array_equal(a[0], c[0]) and a[1] == c[1] and a[2] == c[2]
+    s.close()
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_inertia_counts_bracket_window_minima(systems, name):
+    g, cr, b = systems[name]
+    s = _solver(b, cr, g)
+    s.set_potential(g["v"].reshape(cr.shape))
+    lm = g["lam_min"]
+    below_lo = s.inertia(float(lm.min()) - 1e-7, per_window=True)
+    assert below_lo.sum() == 0
+    per = np.array([s.inertia(float(x) + 1e-7, per_window=True)[w] for w, x in enumerate(lm)])
+    assert np.all(per >= 1)
+    assert abs(s.min_eig(-1.0, 0.0, tol=1e-12) - lm.min()) < 1e-10
+    s.close()
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_density_protocol_matches_reference_calls(systems, name):
+    """Cold call, warm call with a forced mu re-solve, and a warm call that keeps mu
+    (the three calls of tests/golden/make_golden.py, reuse_vectors=False)."""
+    g, cr, b = systems[name]
+    s = _solver(b, cr, g)
+    v = g["v"].reshape(cr.shape)
+    n1, e1, mu1 = s.density(v)
+    assert abs(s.e_lo - g["cold_elo"]) < 1e-9
+    assert abs(mu1 - g["cold_mu"]) < 1e-9
+    assert abs(e1 - g["cold_eband"]) < 1e-9
+    assert np.max(np.abs(n1.ravel() - g["cold_dens"])) < 1e-10
+    s.mu += 0.02
+    n2, e2, mu2 = s.density(0.999 * v)
+    assert abs(mu2 - g["warm_mu"]) < 1e-9
+    assert abs(e2 - g["warm_eband"]) < 1e-9
+    assert np.max(np.abs(n2.ravel() - g["warm_dens"])) < 1e-10
+    p0 = s.passes
+    n3, e3, mu3 = s.density(0.999 * v)
+    assert s.passes - p0 == 1 and mu3 == mu2
+    assert abs(e3 - g["keep_eband"]) < 1e-9
+    assert np.max(np.abs(n3.ravel() - g["keep_dens"])) < 1e-10
+    s.close()
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_mixed_precision_density_within_gate(systems, name):
+    g, cr, b = systems[name]
+    s = _solver(b, cr, g, precision="mixed")
+    v = g["v"].reshape(cr.shape)
+    s.set_potential(v)
+    dens, N, eb = s.pole_pass(float(g["cold_mu"]), float(g["cold_elo"]))
+    ne = cr.n_elec
+    assert abs(eb - g["cold_eband"]) / ne < 2e-7
+    assert abs(N - ne) / ne < 1e-6
+    assert np.sqrt(np.sum((dens - g["cold_dens"]) ** 2) * cr.dV) / ne < 1e-6
+    n1, e1, mu1 = s.density(v)
+    assert abs(e1 - g["cold_eband"]) / ne < 2e-7
+    s.close()
+
+
+def test_grid_kernels_match_oracle(systems):
+    from lresdft_gb300.scf import GridOps
+    from oracle import lrft_oracle as orc
+    g, cr, b = systems["cubic3"]
+    s = _solver(b, cr, g)
+    go = GridOps(s)
+    vion = go.ion_potential()
+    assert np.max(np.abs(vion.ravel() - g["vion"])) < 1e-11
+    rng = np.random.default_rng(3)
+    dens = np.abs(rng.normal(size=cr.shape)) * 0.05 + 1e-3
+    exc, vxc, vh = go.lda_hartree(dens)
+    e0, v0 = orc.lda_xc(dens)
+    assert np.max(np.abs(exc - e0)) < 1e-13 and np.max(np.abs(vxc - v0)) < 1e-13
+    assert np.max(np.abs(vh - orc.hartree(cr, dens))) < 1e-12
+    s.close()
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_scf_energy_matches_reference(systems, name):
+    """SCF to tol 1e-8 (reference driver conventions) against the reference's
+    LRFTLCAOCpp(reuse_vectors=False) SCF: FP64 to 1e-10 Ha/e, mixed to 2e-7 Ha/e."""
+    from lresdft_gb300.scf import scf_lcao
+    g, cr, b = systems[name]
+    for precision, gate in (("fp64", 1e-10), ("mixed", 2e-7)):
+        s = _solver(b, cr, g, precision)
+        r = scf_lcao(cr, s, tol=1e-8)
+        assert r["converged"]
+        assert abs(r["energy"] - g["scf_energy"]) / cr.n_elec < gate, (precision, r["energy"], g["scf_energy"])
+        s.close()
