@@ -100,9 +100,16 @@ int lres_set_hamiltonian_csr(lres_ctx* ctx, const int64_t* Hp, const int64_t* Hi
  *             NULL to skip the copy-out, the device copy stays in the context)
  *   out[0]    electron count N(mu) = dV sum dens
  *   out[1]    band energy E_band = 2 sum_w tr(P^lambda_W O_W)
- *   out[2]    number of windows whose factorisation met a zero / non-finite pivot
- * and returns LRES_ENUMERIC when out[2] > 0. */
+ *   out[2]    status bits of the window kernels: 1 = some window met a zero or non-finite
+ *             pivot, 2 = some window exceeded the launch limits; 0 when clean
+ * and returns LRES_ENUMERIC (bit 1) or LRES_EINVAL (bit 2) when out[2] != 0. */
 int lres_pass(lres_ctx* ctx, double mu, double e_lo, double* dens, int dens_on_device, double* out, void* stream);
+
+/* Device time (ms, CUDA events on the launching stream) of the most recent launch of:
+ * ms[0] the fused pole kernel, ms[1] the pole sums, ms[2] the H(v) assembly, ms[3] the
+ * window gather, ms[4] the standard-form transform (LRES_MIXED), ms[5] the inertia kernel;
+ * -1 for one not launched yet.  Fills min(n, 6) entries, waits for their end events. */
+int lres_timings(lres_ctx* ctx, double* ms, int n);
 
 /* Per-window electron counts and band energies of the last pass (host arrays of nwin). */
 int lres_window_sums(lres_ctx* ctx, double* n_w, double* e_w);

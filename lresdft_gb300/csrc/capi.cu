@@ -97,6 +97,10 @@ struct lres_ctx {
     // grid
     FFT3* fft = nullptr;
     double2* d_fftwork = nullptr;
+    // CUDA events bracketing the launches, for lres_timings: pairs (begin, end) of
+    // 0 pole kernel, 1 pole sums, 2 H(v) assembly, 3 window gather, 4 standard-form transform, 5 inertia kernel
+    cudaEvent_t ev[12] = {};
+    bool ev_used[6] = {};
     ~lres_ctx();
 };
 
@@ -109,6 +113,8 @@ lres_ctx::~lres_ctx() {
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (fft) fft3_destroy(fft);
+    for (cudaEvent_t e : ev)
+        if (e) cudaEventDestroy(e);
 }
 
 namespace {
@@ -174,11 +180,23 @@ int window_transform(lres_ctx* c, cudaStream_t s) {
     return LRES_OK;
 }
 
+int mark(lres_ctx* c, int which, int end, cudaStream_t s) {
+    LRES_CUDA_TRY(cudaEventRecord(c->ev[2 * which + end], s));
+    c->ev_used[which] = true;
+    return LRES_OK;
+}
+
 int after_h_blocks(lres_ctx* c, cudaStream_t s) {
+    TRY(mark(c, 3, 0, s));
     LRES_CUDA_TRY(cudaMemsetAsync(c->d_HW, 0, sizeof(double) * c->sizeC, s));
     TRY(gather_windows(c->bp, c->nwin, c->d_wgrp_off, c->d_wgrp, c->d_wgrp_lo, c->d_gloc, c->d_offC, c->d_n, c->nmax,
                        c->d_Hblk, c->d_HW, s));
-    if (c->precision == LRES_MIXED) TRY(window_transform(c, s));
+    TRY(mark(c, 3, 1, s));
+    if (c->precision == LRES_MIXED) {
+        TRY(mark(c, 4, 0, s));
+        TRY(window_transform(c, s));
+        TRY(mark(c, 4, 1, s));
+    }
     c->have_h = true;
     return LRES_OK;
 }
@@ -243,6 +261,7 @@ extern "C" int lres_ctx_create(lres_ctx** out, const lres_system_desc* d, int pr
     int optin = 0;
     LRES_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
     c->smem_budget = (size_t)optin - 1024;
+    for (cudaEvent_t& e : c->ev) LRES_CUDA_TRY(cudaEventCreate(&e));
     c->precision = precision;
     c->M = M;
     c->npoles = M / 2;
@@ -621,7 +640,9 @@ extern "C" int lres_set_potential(lres_ctx* c, const double* v, int v_on_device,
         LRES_CUDA_TRY(cudaMemcpyAsync(c->d_v, v, sizeof(double) * c->ng, cudaMemcpyHostToDevice, s));
         dv = c->d_v;
     }
+    TRY(mark(c, 2, 0, s));
     TRY(assemble_h(c->bp, c->sp, c->d_Tblk, dv, c->dV, c->d_Hblk, s));
+    TRY(mark(c, 2, 1, s));
     return after_h_blocks(c, s);
 }
 
@@ -677,14 +698,19 @@ extern "C" int lres_pass(lres_ctx* c, double mu, double e_lo, double* dens, int 
     LRES_CUDA_TRY(cudaMemcpyAsync(c->d_wq, wq.data(), sizeof(double2) * P, cudaMemcpyHostToDevice, s));
     LRES_CUDA_TRY(cudaMemcpyAsync(c->d_wzq, wzq.data(), sizeof(double2) * P, cudaMemcpyHostToDevice, s));
     LRES_CUDA_TRY(cudaMemsetAsync(c->d_status, 0, sizeof(int), s));
+    LRES_CUDA_TRY(cudaMemsetAsync(c->d_counter, 0, sizeof(int), s));
+    TRY(mark(c, 0, 0, s));
     if (mixed)
         TRY(ldl_launch(c, LdlJob::C64, c->nitems, c->d_items, c->d_Hhat32, nullptr, c->d_Fhat32, c->d_m, c->d_offF,
                        c->d_shifts, c->d_q, nullptr, c->nmax + c->mmax, c->mmax, s));
     else
         TRY(ldl_launch(c, LdlJob::C128, c->nitems, c->d_items, c->d_HW, c->d_SW, c->d_F, c->d_m, c->d_offF,
                        c->d_shifts, c->d_q, nullptr, c->nmax + c->mmax, c->mmax, s));
+    TRY(mark(c, 0, 1, s));
+    TRY(mark(c, 1, 0, s));
     TRY(pole_sums(c->nwin, c->d_offQ, c->d_m, c->d_Oflat, mixed, c->d_q, c->npts, P, c->d_wq, c->d_wzq, c->dV,
                   c->d_dens, c->d_nw, c->d_ew, s));
+    TRY(mark(c, 1, 1, s));
     LRES_CUDA_TRY(cudaMemcpyAsync(c->nw_h.data(), c->d_nw, sizeof(double) * c->nwin, cudaMemcpyDeviceToHost, s));
     LRES_CUDA_TRY(cudaMemcpyAsync(c->ew_h.data(), c->d_ew, sizeof(double) * c->nwin, cudaMemcpyDeviceToHost, s));
     if (dens)
@@ -711,6 +737,23 @@ extern "C" int lres_pass(lres_ctx* c, double mu, double e_lo, double* dens, int 
     return LRES_OK;
 }
 
+extern "C" int lres_timings(lres_ctx* c, double* ms, int n) {
+    if (!c || !ms || n < 0) {
+        lres_set_error("bad arguments to lres_timings");
+        return LRES_EINVAL;
+    }
+    for (int i = 0; i < n && i < 6; ++i) {
+        ms[i] = -1.0;
+        if (!c->ev_used[i]) continue;
+        LRES_CUDA_TRY(cudaEventSynchronize(c->ev[2 * i + 1]));
+        float t = 0.f;
+        LRES_CUDA_TRY(cudaEventElapsedTime(&t, c->ev[2 * i], c->ev[2 * i + 1]));
+        ms[i] = t;
+    }
+    for (int i = 6; i < n; ++i) ms[i] = -1.0;
+    return LRES_OK;
+}
+
 extern "C" int lres_window_sums(lres_ctx* c, double* n_w, double* e_w) {
     if (!c) {
         lres_set_error("null argument");
@@ -734,8 +777,11 @@ extern "C" int lres_inertia(lres_ctx* c, double sigma, int32_t* below, int64_t* 
     LRES_CUDA_TRY(cudaMemcpyAsync(c->d_shifts, &sigma, sizeof(double), cudaMemcpyHostToDevice, s));
     LRES_CUDA_TRY(cudaMemsetAsync(c->d_status, 0, sizeof(int), s));
     // positive pivots of (sigma S - H) = eigenvalues of (H, S) below sigma
+    LRES_CUDA_TRY(cudaMemsetAsync(c->d_counter, 0, sizeof(int), s));
+    TRY(mark(c, 5, 0, s));
     TRY(ldl_launch(c, LdlJob::R64, c->nwin, c->d_items_win, c->d_HW, c->d_SW, nullptr, c->d_m, c->d_offF,
                    c->d_shifts, nullptr, nullptr, c->nmax, 0, s));
+    TRY(mark(c, 5, 1, s));
     std::vector<int> cnt(c->nwin);
     LRES_CUDA_TRY(cudaMemcpyAsync(cnt.data(), c->d_npos, sizeof(int) * c->nwin, cudaMemcpyDeviceToHost, s));
     LRES_CUDA_TRY(cudaStreamSynchronize(s));

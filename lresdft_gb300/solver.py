@@ -144,6 +144,17 @@ class LResGPU:
         else:
             self.set_hamiltonian(self.b.H(v))
 
+    def set_potential_device(self, v_ptr):
+        """H(v) from a device array of ng doubles (stream-ordered, no host copy)."""
+        _lib.check(_lib.lib.lres_set_potential(self._ctx, v_ptr, 1, None))
+
+    def pole_pass_device(self, mu, e_lo, dens_ptr=None):
+        """Pole pass leaving the density on the device (copied to dens_ptr if given);
+        returns (N(mu), E_band)."""
+        self.passes += 1
+        _lib.check(_lib.lib.lres_pass(self._ctx, float(mu), float(e_lo), dens_ptr, 1, _lib.ptrd(self._out), None))
+        return float(self._out[0]), float(self._out[1])
+
     def set_hamiltonian(self, H):
         Hp, Hi, Hv = csr64(H)
         _lib.check(_lib.lib.lres_set_hamiltonian_csr(self._ctx, _lib.ptr64(Hp), _lib.ptr64(Hi), _lib.ptrd(Hv), None))
@@ -155,6 +166,13 @@ class LResGPU:
         ptr = dens.ctypes.data if want_density else None
         _lib.check(_lib.lib.lres_pass(self._ctx, float(mu), float(e_lo), ptr, 0, _lib.ptrd(self._out), None))
         return (dens.copy() if want_density else None), float(self._out[0]), float(self._out[1])
+
+    def timings(self):
+        """Device milliseconds of the last launches: pole kernel, pole sums, H(v)
+        assembly, window gather, standard-form transform, inertia kernel (-1 = none)."""
+        ms = np.empty(6)
+        _lib.check(_lib.lib.lres_timings(self._ctx, _lib.ptrd(ms), 6))
+        return dict(zip(("pole_kernel", "pole_sums", "assemble_h", "gather", "transform", "inertia"), ms))
 
     def window_sums(self):
         nw = np.empty(len(self.windows))

@@ -145,13 +145,15 @@ def test_grid_kernels_match_oracle(systems):
 
 @pytest.mark.parametrize("name", CASES)
 def test_scf_energy_matches_reference(systems, name):
-    """SCF to tol 1e-8 (reference driver conventions) against the reference's
-    LRFTLCAOCpp(reuse_vectors=False) SCF: FP64 to 1e-10 Ha/e, mixed to 2e-7 Ha/e."""
+    """SCF against the reference's LRFTLCAOCpp(reuse_vectors=False) SCF converged to
+    tol 1e-8: FP64 with the same tolerance to 1e-10 Ha/e; mixed precision (whose
+    density carries ~1e-7 relative FP32 noise, so |dn|/N cannot reach 1e-8) to tol 1e-6,
+    energy within 2e-7 Ha/e."""
     from lresdft_gb300.scf import scf_lcao
     g, cr, b = systems[name]
-    for precision, gate in (("fp64", 1e-10), ("mixed", 2e-7)):
+    for precision, tol, gate in (("fp64", 1e-8, 1e-10), ("mixed", 1e-6, 2e-7)):
         s = _solver(b, cr, g, precision)
-        r = scf_lcao(cr, s, tol=1e-8)
+        r = scf_lcao(cr, s, tol=tol)
         assert r["converged"]
         assert abs(r["energy"] - g["scf_energy"]) / cr.n_elec < gate, (precision, r["energy"], g["scf_energy"])
         s.close()
