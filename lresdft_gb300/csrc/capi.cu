@@ -173,9 +173,10 @@ __global__ void identity_kernel(const int* n_w, const long long* off, double* I,
 }
 
 int window_transform(lres_ctx* c, cudaStream_t s) {
-    // H^_W = L^-1 H_W L^-T with LinvT = L^-T stored column-major:  Y = H LinvT,  H^ = LinvT^T Y
-    TRY(batched_gemm(c->nwin, c->d_n, c->d_offC, c->nmax, false, c->d_HW, c->d_LinvT, c->d_Y, s));
-    TRY(batched_gemm(c->nwin, c->d_n, c->d_offC, c->nmax, true, c->d_LinvT, c->d_Y, c->d_Hhat, s));
+    // H^_W = L^-1 H_W L^-T with LinvT = L^-T (upper triangular) stored column-major:
+    // Y = H LinvT (k <= column), then the lower triangle of H^ = LinvT^T Y (k <= row)
+    TRY(batched_gemm(c->nwin, c->d_n, c->d_offC, c->nmax, false, c->d_HW, c->d_LinvT, c->d_Y, s, 1));
+    TRY(batched_gemm(c->nwin, c->d_n, c->d_offC, c->nmax, true, c->d_LinvT, c->d_Y, c->d_Hhat, s, 2));
     TRY(convert_f64_f32(c->d_Hhat, c->d_Hhat32, c->sizeC, s));
     return LRES_OK;
 }

@@ -25,6 +25,7 @@ template <> struct El<double> {
     __device__ __forceinline__ static double re(double a) { return a; }
     __device__ __forceinline__ static double mag2(double a) { return a * a; }
     __device__ __forceinline__ static double shift_minus(double z, double b, double c) { return ::fma(z, b, -c); } // z*b - c
+    __device__ __forceinline__ static double csqrt(double a) { return sqrt(fabs(a)); }   // unused for real pivots
 };
 
 template <> struct El<double2> {
@@ -59,6 +60,18 @@ template <> struct El<double2> {
     __device__ __forceinline__ static double2 shift_minus(double2 z, double b, double c) {
         return make_double2(::fma(z.x, b, -c), z.y * b);
     }
+    // principal square root: sqrt(z) = (sqrt((|z|+x)/2), sign(y) sqrt((|z|-x)/2))
+    __device__ __forceinline__ static double2 csqrt(double2 a) {
+        const double r = hypot(a.x, a.y);
+        double re = sqrt(0.5 * (r + fabs(a.x)));
+        double im = (re > 0.0) ? 0.5 * a.y / re : 0.0;
+        if (a.x < 0.0) {
+            const double t = re;
+            re = fabs(im);
+            im = copysign(t, a.y);
+        }
+        return make_double2(re, im);
+    }
 };
 
 template <> struct El<float2> {
@@ -91,6 +104,17 @@ template <> struct El<float2> {
     __device__ __forceinline__ static float mag2(float2 a) { return a.x * a.x + a.y * a.y; }
     __device__ __forceinline__ static float2 shift_minus(float2 z, float b, float c) {
         return make_float2(fmaf(z.x, b, -c), z.y * b);
+    }
+    __device__ __forceinline__ static float2 csqrt(float2 a) {
+        const float r = hypotf(a.x, a.y);
+        float re = sqrtf(0.5f * (r + fabsf(a.x)));
+        float im = (re > 0.f) ? 0.5f * a.y / re : 0.f;
+        if (a.x < 0.f) {
+            const float t = re;
+            re = fabsf(im);
+            im = copysignf(t, a.y);
+        }
+        return make_float2(re, im);
     }
 };
 

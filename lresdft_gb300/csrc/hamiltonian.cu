@@ -257,7 +257,9 @@ int build_F(int nwin, const long long* Xp, const int* Xi, const double* Xv, cons
 // batched FP64 GEMM  C_w = op(A_w) B_w  (n_w x n_w, column-major, same offsets)
 // ---------------------------------------------------------------------------
 
-template <bool TA>
+// KLIM = 0: full product.  KLIM = 1: B upper triangular (k <= column).  KLIM = 2: op(A)
+// lower triangular (k <= row) and only the lower triangle of C is needed.
+template <bool TA, int KLIM>
 __global__ void __launch_bounds__(256) gemm_f64_kernel(const int* n_w, const long long* off, const double* A,
                                                        const double* B, double* C) {
     constexpr int BM = 64, BN = 64, BK = 16;
@@ -265,6 +267,8 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(const int* n_w, const lon
     const int n = n_w[w];
     const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
     if (m0 >= n || n0 >= n) return;
+    if (KLIM == 2 && m0 + BM - 1 < n0) return;
+    const int kend = KLIM == 1 ? min(n, n0 + BN) : KLIM == 2 ? min(n, m0 + BM) : n;
     const double* Aw = A + off[w];
     const double* Bw = B + off[w];
     double* Cw = C + off[w];
@@ -273,7 +277,7 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(const int* n_w, const lon
     const int tid = threadIdx.x;
     const int tx = tid % 16, ty = tid / 16;   // 16 x 16 threads, 4 x 4 outputs each
     double acc[4][4] = {};
-    for (int k0 = 0; k0 < n; k0 += BK) {
+    for (int k0 = 0; k0 < kend; k0 += BK) {
         for (int idx = tid; idx < BK * BM; idx += 256) {
             const int kk = idx / BM, i = idx % BM;
             const int gi = m0 + i, gk = k0 + kk;
@@ -311,11 +315,16 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(const int* n_w, const lon
 }
 
 int batched_gemm(int nwin, const int* n_w, const long long* offA, int nmax, bool transA, const double* A,
-                 const double* B, double* C, cudaStream_t s) {
+                 const double* B, double* C, cudaStream_t s, int klim) {
     if (!nwin) return LRES_OK;
     dim3 grid((nmax + 63) / 64, (nmax + 63) / 64, nwin);
-    if (transA) gemm_f64_kernel<true><<<grid, 256, 0, s>>>(n_w, offA, A, B, C);
-    else gemm_f64_kernel<false><<<grid, 256, 0, s>>>(n_w, offA, A, B, C);
+    if (transA) {
+        if (klim == 2) gemm_f64_kernel<true, 2><<<grid, 256, 0, s>>>(n_w, offA, A, B, C);
+        else gemm_f64_kernel<true, 0><<<grid, 256, 0, s>>>(n_w, offA, A, B, C);
+    } else {
+        if (klim == 1) gemm_f64_kernel<false, 1><<<grid, 256, 0, s>>>(n_w, offA, A, B, C);
+        else gemm_f64_kernel<false, 0><<<grid, 256, 0, s>>>(n_w, offA, A, B, C);
+    }
     LRES_CUDA_TRY(cudaGetLastError());
     return LRES_OK;
 }

@@ -77,7 +77,7 @@ int build_F(int nwin, const long long* Xp, const int* Xi, const double* Xv, cons
             const int* gptr, const int* gloc, int ngroups, const long long* Ooff, const long long* Oflat,
             const long long* offF, const int* m_w, int mmax, double* F, cudaStream_t s);
 int batched_gemm(int nwin, const int* n_w, const long long* offA, int nmax, bool transA, const double* A,
-                 const double* B, double* C, cudaStream_t s);
+                 const double* B, double* C, cudaStream_t s, int klim = 0);
 int convert_f64_f32(const double* a, float* b, long long n, cudaStream_t s);
 int pole_sums(int nwin, const long long* offQ, const int* m_w, const long long* Oflat, bool fp32,
               const void* q, long long qstride, int npoles, const double2* wq, const double2* wzq, double dV,

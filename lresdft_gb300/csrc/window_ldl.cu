@@ -35,6 +35,14 @@
 
 namespace lres {
 
+__device__ __forceinline__ double shfl(double x, int src) { return __shfl_sync(0xffffffffu, x, src); }
+__device__ __forceinline__ double2 shfl(double2 x, int src) {
+    return make_double2(__shfl_sync(0xffffffffu, x.x, src), __shfl_sync(0xffffffffu, x.y, src));
+}
+__device__ __forceinline__ float2 shfl(float2 x, int src) {
+    return make_float2(__shfl_sync(0xffffffffu, x.x, src), __shfl_sync(0xffffffffu, x.y, src));
+}
+
 template <class T>
 struct LdlParams {
     int nitems;
@@ -60,8 +68,8 @@ struct LdlParams {
     int nmax, mmax;
 };
 
-template <class T, int NB, int TR, int TC>
-__global__ void __launch_bounds__(256) ldl_aug_kernel(LdlParams<T> p) {
+template <class T, int NB, int TR, int TC, int NT>
+__global__ void __launch_bounds__(NT) ldl_aug_kernel(LdlParams<T> p) {
     using E = El<T>;
     using R = typename E::R;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -69,7 +77,8 @@ __global__ void __launch_bounds__(256) ldl_aug_kernel(LdlParams<T> p) {
     T* WL = P + (size_t)NB * p.ldp;                  // WL[kk*NB + kk2] = D_kk L_kk2,kk
     T* Dsh = WL + NB * NB;
     T* Dinv = Dsh + NB;
-    T* qsh = Dinv + NB;                              // mmax
+    T* Dsq = Dinv + NB;                              // sqrt(D) (complex case)
+    T* qsh = Dsq + NB;                               // mmax
     __shared__ int item_sh;
     __shared__ int npos_sh;
     const int tid = threadIdx.x;
@@ -96,20 +105,21 @@ __global__ void __launch_bounds__(256) ldl_aug_kernel(LdlParams<T> p) {
         const R* B = p.B ? p.B + p.offC[w] : nullptr;
         const R* F = p.F ? p.F + p.offF[w] : nullptr;
 
-        // ---- build the augmented lower trapezoid
-        const long long tot = (long long)rows * n;
-        for (long long idx = tid; idx < tot; idx += blockDim.x) {
-            const int i = (int)(idx % rows), j = (int)(idx / rows);
-            T val;
-            if (i < n) {
-                if (i < j) continue;
-                const R b = B ? B[i + (long long)j * n] : (i == j ? R(1) : R(0));
-                const R c = C ? C[i + (long long)j * n] : R(0);
-                val = E::shift_minus(z, b, c);
-            } else {
-                val = E::from(F[(i - n) + (long long)j * m]);
+        // ---- build the augmented lower trapezoid (one warp per column, lanes down the rows)
+        {
+            const int warp = tid >> 5, lane = tid & 31;
+            for (int j = warp; j < n; j += NT / 32) {
+                T* wcol = ws + (long long)j * ld;
+                const R* Ccol = C ? C + (long long)j * n : nullptr;
+                const R* Bcol = B ? B + (long long)j * n : nullptr;
+                for (int i = j + lane; i < n; i += 32) {
+                    const R b = Bcol ? Bcol[i] : (i == j ? R(1) : R(0));
+                    const R c = Ccol ? Ccol[i] : R(0);
+                    wcol[i] = E::shift_minus(z, b, c);
+                }
+                const R* Fcol = F ? F + (long long)j * m : nullptr;
+                for (int r = lane; r < m; r += 32) wcol[n + r] = E::from(Fcol[r]);
             }
-            ws[i + (long long)j * ld] = val;
         }
         for (int r = tid; r < m; r += blockDim.x) qsh[r] = E::zero();
         if (tid == 0) npos_sh = 0;
@@ -119,42 +129,52 @@ __global__ void __launch_bounds__(256) ldl_aug_kernel(LdlParams<T> p) {
             const int nbj = min(NB, n - j0);
             const int prow = rows - j0;
             // ---- load panel columns [j0, j0+nbj), rows [j0, rows)
-            for (int idx = tid; idx < nbj * prow; idx += blockDim.x) {
-                const int i = idx % prow, kk = idx / prow;
-                if (i >= kk) P[kk * ldp + i] = ws[(j0 + i) + (long long)(j0 + kk) * ld];
+            for (int kk = tid >> 5; kk < nbj; kk += NT / 32) {
+                const T* src = ws + j0 + (long long)(j0 + kk) * ld;
+                for (int i = kk + (tid & 31); i < prow; i += 32) P[kk * ldp + i] = src[i];
             }
             __syncthreads();
 
-            // ---- (1) diagonal block, one warp, lane = row
+            // ---- (1) diagonal block, one warp: lane = row, the row held in registers,
+            //      multipliers exchanged by warp shuffles
             if (tid < 32) {
                 const int lane = tid;
-                for (int kk = 0; kk < nbj; ++kk) {
-                    __syncwarp();
-                    const T d = P[kk * ldp + kk];
-                    const T dinv = E::inv(d);
-                    T l = E::zero();
-                    const bool mine = lane > kk && lane < nbj;
-                    if (mine) l = E::mul(P[kk * ldp + lane], dinv);
-                    __syncwarp();
-                    if (mine) P[kk * ldp + lane] = l;
-                    if (lane == kk) {
-                        Dsh[kk] = d;
-                        Dinv[kk] = dinv;
-                        const double m2 = (double)E::mag2(d);
-                        if (!(m2 > 0.0) || !isfinite(m2)) atomicOr(p.status, ST_ZERO_PIVOT);
-                        if (E::re(d) > R(0)) ++npos_sh;
-                    }
-                    __syncwarp();
-                    if (mine) {
+                T row[NB];
+#pragma unroll
+                for (int c = 0; c < NB; ++c)
+                    row[c] = (c < nbj && lane < nbj && c <= lane) ? P[c * ldp + lane] : E::zero();
+#pragma unroll
+                for (int kk = 0; kk < NB; ++kk) {
+                    if (kk < nbj) {
+                        const T d = shfl(row[kk], kk);
+                        const T dinv = E::inv(d);
+                        const bool mine = lane > kk && lane < nbj;
+                        const T l = mine ? E::mul(row[kk], dinv) : E::zero();
+                        if (mine) row[kk] = l;
+                        if (lane == kk) {
+                            Dsh[kk] = d;
+                            Dinv[kk] = dinv;
+                            if constexpr (E::complex) Dsq[kk] = E::csqrt(d);
+                            const double m2 = (double)E::mag2(d);
+                            if (!(m2 > 0.0) || !isfinite(m2)) atomicOr(p.status, ST_ZERO_PIVOT);
+                            if (E::re(d) > R(0)) ++npos_sh;
+                        }
                         const T ldv = E::mul(l, d);
-                        for (int c = kk + 1; c <= lane; ++c)
-                            P[c * ldp + lane] = E::fms(ldv, P[kk * ldp + c], P[c * ldp + lane]);
+#pragma unroll
+                        for (int c = kk + 1; c < NB; ++c) {
+                            const T lc = shfl(l, c);
+                            if (mine && c <= lane) row[c] = E::fms(ldv, lc, row[c]);
+                        }
                     }
                 }
                 __syncwarp();
-                for (int idx = lane; idx < nbj * nbj; idx += 32) {
-                    const int kk = idx / nbj, kk2 = idx % nbj;
-                    if (kk2 > kk) WL[kk * NB + kk2] = E::mul(Dsh[kk], P[kk * ldp + kk2]);
+                // L below the diagonal back to shared memory; WL[kk*NB + lane] = D_kk L_lane,kk
+#pragma unroll
+                for (int kk = 0; kk < NB; ++kk) {
+                    if (kk < nbj && lane > kk && lane < nbj) {
+                        P[kk * ldp + lane] = row[kk];
+                        WL[kk * NB + lane] = E::mul(Dsh[kk], row[kk]);
+                    }
                 }
             }
             __syncthreads();
@@ -174,9 +194,11 @@ __global__ void __launch_bounds__(256) ldl_aug_kernel(LdlParams<T> p) {
                         a[kk] = l;
                     }
                 }
+                // complex case: store l sqrt(D), so that the trailing update is a plain product
+                // (L D L^T = (L sqrt D)(L sqrt D)^T for complex-symmetric A); real case: l
 #pragma unroll
                 for (int kk = 0; kk < NB; ++kk)
-                    if (kk < nbj) P[kk * ldp + i] = a[kk];
+                    if (kk < nbj) P[kk * ldp + i] = E::complex ? E::mul(a[kk], Dsq[kk]) : a[kk];
                 const int gi = j0 + i;
                 if (gi >= n) {
                     const int r = gi - n;
@@ -199,45 +221,62 @@ __global__ void __launch_bounds__(256) ldl_aug_kernel(LdlParams<T> p) {
             }
             __syncthreads();
 
-            // ---- (3) trailing update of rows [r0, rows) x cols [r0, n), lower part
+            // ---- (3) trailing update of rows [r0, rows) x cols [r0, n), lower part.
+            //      Warp tile = (32*TR rows) x TC columns; lane l owns rows base + l + 32u, so
+            //      shared loads are consecutive across the warp and column operands broadcast.
             const int r0 = j0 + nbj;
             if (r0 < n) {
+                const int warp = tid >> 5, lane = tid & 31;
                 const int nr = rows - r0, nc = n - r0;
-                const int nrt = (nr + TR - 1) / TR, nct = (nc + TC - 1) / TC;
-                for (int t = tid; t < nrt * nct; t += blockDim.x) {
-                    const int ti = t % nrt, tc = t / nrt;
-                    const int i0 = r0 + ti * TR, c0 = r0 + tc * TC;
-                    if (i0 + TR - 1 < c0) continue;          // tile strictly above the diagonal
+                const int nrb = (nr + 32 * TR - 1) / (32 * TR), ncb = (nc + TC - 1) / TC;
+                for (int wt = warp; wt < nrb * ncb; wt += NT / 32) {
+                    const int rb = wt % nrb, cb = wt / nrb;
+                    const int ib = r0 + rb * 32 * TR, c0 = r0 + cb * TC;
+                    if (ib + 32 * TR - 1 < c0) continue;     // warp tile strictly above the diagonal
+                    T cur[TR][TC];
+                    bool ok[TR][TC];
+#pragma unroll
+                    for (int u = 0; u < TR; ++u) {
+                        const int i = ib + lane + 32 * u;
+#pragma unroll
+                        for (int v = 0; v < TC; ++v) {
+                            const int c = c0 + v;
+                            ok[u][v] = i < rows && c < n && (i >= n || i >= c);
+                            cur[u][v] = ok[u][v] ? ws[i + (long long)c * ld] : E::zero();
+                        }
+                    }
                     T acc[TR][TC];
 #pragma unroll
                     for (int u = 0; u < TR; ++u)
 #pragma unroll
                         for (int v = 0; v < TC; ++v) acc[u][v] = E::zero();
+                    const T* Pr = P - j0 + ib + lane;
+                    const T* Pc = P - j0 + c0;
                     for (int kk = 0; kk < nbj; ++kk) {
-                        const T dk = Dsh[kk];
-                        const T* Pk = P + kk * ldp - j0;
                         T wr[TR], lc[TC];
+                        if constexpr (E::complex) {
 #pragma unroll
-                        for (int u = 0; u < TR; ++u) wr[u] = (i0 + u < rows) ? Pk[i0 + u] : E::zero();
+                            for (int u = 0; u < TR; ++u)
+                                wr[u] = (ib + lane + 32 * u < rows) ? Pr[kk * ldp + 32 * u] : E::zero();
+                        } else {
+                            const T dk = Dsh[kk];
 #pragma unroll
-                        for (int v = 0; v < TC; ++v) lc[v] = (c0 + v < n) ? E::mul(Pk[c0 + v], dk) : E::zero();
+                            for (int u = 0; u < TR; ++u)
+                                wr[u] = (ib + lane + 32 * u < rows) ? E::mul(Pr[kk * ldp + 32 * u], dk) : E::zero();
+                        }
+#pragma unroll
+                        for (int v = 0; v < TC; ++v) lc[v] = (c0 + v < n) ? Pc[kk * ldp + v] : E::zero();
 #pragma unroll
                         for (int u = 0; u < TR; ++u)
 #pragma unroll
                             for (int v = 0; v < TC; ++v) acc[u][v] = E::fma(wr[u], lc[v], acc[u][v]);
                     }
 #pragma unroll
-                    for (int v = 0; v < TC; ++v) {
-                        const int c = c0 + v;
-                        if (c >= n) continue;
+                    for (int u = 0; u < TR; ++u) {
+                        const int i = ib + lane + 32 * u;
 #pragma unroll
-                        for (int u = 0; u < TR; ++u) {
-                            const int i = i0 + u;
-                            if (i < rows && (i >= n || i >= c)) {
-                                T* x = ws + i + (long long)c * ld;
-                                *x = E::sub(*x, acc[u][v]);
-                            }
-                        }
+                        for (int v = 0; v < TC; ++v)
+                            if (ok[u][v]) ws[i + (long long)(c0 + v) * ld] = E::sub(cur[u][v], acc[u][v]);
                     }
                 }
             }
@@ -258,18 +297,18 @@ __global__ void __launch_bounds__(256) ldl_aug_kernel(LdlParams<T> p) {
 // host launchers
 // ---------------------------------------------------------------------------
 
-template <class T, int NB, int TR, int TC>
+template <class T, int NB, int TR, int TC, int NT>
 static int launch_ldl(const LdlParams<T>& p, int grid, cudaStream_t s) {
-    const size_t smem = sizeof(T) * ((size_t)NB * p.ldp + NB * NB + 2 * NB + p.mmax);
-    auto kern = ldl_aug_kernel<T, NB, TR, TC>;
+    const size_t smem = sizeof(T) * ((size_t)NB * p.ldp + NB * NB + 3 * NB + p.mmax);
+    auto kern = ldl_aug_kernel<T, NB, TR, TC, NT>;
     LRES_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<grid, 256, smem, s>>>(p);
+    kern<<<grid, NT, smem, s>>>(p);
     LRES_CUDA_TRY(cudaGetLastError());
     return LRES_OK;
 }
 
 size_t ldl_smem_bytes(int elem_bytes, int nb, int ldp, int mmax) {
-    return (size_t)elem_bytes * ((size_t)nb * ldp + nb * nb + 2 * nb + mmax);
+    return (size_t)elem_bytes * ((size_t)nb * ldp + nb * nb + 3 * nb + mmax);
 }
 
 // Chooses the widest panel that fits the shared-memory budget.
@@ -284,10 +323,12 @@ template <class T>
 static int dispatch(const LdlParams<T>& p, int grid, size_t budget, cudaStream_t s) {
     int nb = pick_nb<T>(p.ldp, p.mmax, budget);
     if constexpr (sizeof(T) == 16) nb = nb > 16 ? 16 : nb;     // complex double: register budget
+    constexpr int NT = sizeof(T) == 8 && El<T>::complex ? 512 : 256;   // complex float: 16 warps
+    constexpr int TC = 4;
     switch (nb) {
-        case 32: return launch_ldl<T, 32, 4, 4>(p, grid, s);
-        case 16: return launch_ldl<T, 16, 4, 4>(p, grid, s);
-        case 8: return launch_ldl<T, 8, 4, 4>(p, grid, s);
+        case 32: return launch_ldl<T, 32, 4, TC, NT>(p, grid, s);
+        case 16: return launch_ldl<T, 16, 4, TC, NT>(p, grid, s);
+        case 8: return launch_ldl<T, 8, 4, TC, NT>(p, grid, s);
         default:
             lres_set_error("window too large for the shared-memory panel (ldp=%d, mmax=%d)", p.ldp, p.mmax);
             return LRES_EINVAL;

@@ -98,6 +98,8 @@ class LResGPU:
         self.mu = self.e_lo = None
         self.passes = 0
         self.inertia_calls = 0
+        self._slope = None
+        self.trace = None          # set to a list to record (mu, N(mu)) of every pass
         self._gpu_h = _plain_lcao(basis)
         X, S = csr64(basis.Xr), csr64(basis.S)
         T = csr64(basis.T) if hasattr(basis, "T") else None
@@ -165,6 +167,8 @@ class LResGPU:
         dens = self.dens_buf if want_density else None
         ptr = dens.ctypes.data if want_density else None
         _lib.check(_lib.lib.lres_pass(self._ctx, float(mu), float(e_lo), ptr, 0, _lib.ptrd(self._out), None))
+        if self.trace is not None:
+            self.trace.append((float(mu), float(self._out[0])))
         return (dens.copy() if want_density else None), float(self._out[0]), float(self._out[1])
 
     def timings(self):
@@ -208,32 +212,40 @@ class LResGPU:
 
     def _solve_mu(self, e_lo, N, ftol, start=None, lo_start=None):
         """Root of N(mu) - N by Brent's method on pole passes.  `start` = (mu, f, dens,
-        eb) of a pass already done.  Returns (mu, dens, e_band) of the accepted pass."""
+        eb) of a pass already done (warm step: a secant step with the slope of the last
+        solve, then widening secant steps until the count changes sign).  Returns
+        (mu, dens, e_band) of the accepted pass."""
         cache = {}
+        hist = []
 
         def f(x):
             dens, n, eb = self.pole_pass(x, e_lo)
             cache[x] = (dens, eb)
+            hist.append((x, n - N))
             return n - N
 
+        lo_bound = e_lo + 1e-6
         if start is not None:
             x0, f0, d0, e0 = start
             cache[x0] = (d0, e0)
-            # step towards the root, doubling until the sign changes
-            step = max(1e-3, min(0.05, abs(f0) / max(N, 1.0)))
-            lo_bound = e_lo + 1e-6
+            hist.append((x0, f0))
+            slope = self._slope if self._slope and self._slope > 0 else max(N, 1.0)
+            step = -f0 / slope
+            step = math.copysign(min(max(abs(step) * 1.2, 1e-7), 0.25), step)
             a, fa = x0, f0
             b = None
             for _ in range(40):
-                x1 = a - step if fa > 0 else a + step
-                if fa > 0 and x1 <= lo_bound:
+                x1 = a + step
+                if x1 <= lo_bound:
                     x1 = 0.5 * (a + lo_bound)
                 f1 = f(x1)
                 if (f1 > 0) != (fa > 0) or f1 == 0:
                     b, fb = x1, f1
                     break
+                # secant extrapolation from the last two points, at least doubling the step
+                sec = -f1 * (x1 - a) / (f1 - fa) if f1 != fa else 2 * step
+                step = math.copysign(min(max(abs(sec) * 1.2, 2 * abs(step)), 1.0), step)
                 a, fa = x1, f1
-                step *= 2
             if b is None:
                 raise StaleMu("no sign change of the electron count near the warm-start mu")
         else:
@@ -251,7 +263,15 @@ class LResGPU:
                     raise StaleMu("window spectra hold fewer than N electrons")
                 fhi = f(hi)
             a, fa, b, fb = lo, flo, hi, fhi
-        x = self._brent(f, a, fa, b, fb, ftol)
+        x = self._brent(f, a, fa, b, fb, ftol, xtol=getattr(self, "_xtol", 1e-12))
+        # local slope dN/dmu for the next warm start: the closest points on both sides
+        below = [h for h in hist if h[1] < 0]
+        above = [h for h in hist if h[1] > 0]
+        if below and above:
+            lb = min(below, key=lambda h: abs(h[0] - x))
+            ub = min(above, key=lambda h: abs(h[0] - x))
+            if ub[0] != lb[0]:
+                self._slope = (ub[1] - lb[1]) / (ub[0] - lb[0])
         dens, eb = cache[x]
         return x, dens, eb
 
@@ -310,8 +330,13 @@ class LResGPU:
         cr = self.b.cr
         N = cr.n_elec if N is None else N
         self.set_potential(v)
-        tol = 1e-8 * N
-        ftol = 1e-11 * N if self.precision == "fp64" else 1e-9 * N
+        # count tolerances: the reference's 1e-8 N (lrft/lcao3d.py:412) for the FP64 path
+        # and a root tolerance far below it; the complex64 path's counts carry ~1e-7 N of
+        # FP32 noise, so both tolerances sit at that floor
+        if self.precision == "fp64":
+            tol, ftol, self._xtol = 1e-8 * N, 1e-11 * N, 1e-12
+        else:
+            tol, ftol, self._xtol = 1e-7 * N, 1e-7 * N, 1e-9
         if self.mu is not None:
             mu, e_lo = self.mu, self.e_lo
             if self._edge_ok(mu, e_lo):
