@@ -129,6 +129,24 @@ int lres_min_eig(lres_ctx* ctx, double lo, double hi, double tol, double* lam_mi
 int lres_voronoi_owner(const int64_t shape[3], const double cell[3], int64_t ncent, const double* centres,
                        int32_t* owner);
 
+/* Window inertia counts that allocate nothing — no counterpart in the reference.
+ * For callers that cannot allocate device memory themselves: hosts that own all GPU
+ * memory through their own arena or caching allocator, or loops that cannot afford the
+ * device-wide synchronisation of cudaMalloc / cudaFree.  Same result as lres_inertia,
+ * computed from caller-provided device arrays: n_w[nwin] (int32 window dimensions),
+ * offC[nwin] (int64 offsets of each window's column-major n_w x n_w block in H and S),
+ * dense window blocks H and S (float64), output below[nwin] (int32, device) = number of
+ * generalised eigenvalues of (H_W, S_W) below sigma.  nmax bounds every n_w.
+ * Scratch comes from one fixed array inside the library (16.5 MiB, held by every GPU
+ * that loads it until the process exits): at most 65536 windows and nmax <= 512 per
+ * call, larger requests return LRES_EINVAL.  The first call on each device looks up the
+ * array's device address (once per device; make that first call before any stream
+ * capture).  All calls on a device share the array and reset its work queue and status
+ * at the start: calls that overlap on the GPU race and must be serialised by the caller
+ * (one stream, or events).  Waits for the stream to read the kernel status. */
+int lres_inertia_noalloc(int32_t nwin, const int32_t* n_w, const int64_t* offC, const double* H, const double* S,
+                         double sigma, int32_t* below, int32_t nmax, void* stream);
+
 /* Grid kernels on device arrays of ng doubles (context supplies shape and cell). */
 int lres_lda_xc(lres_ctx* ctx, const double* dens, double* exc, double* vxc, void* stream);
 int lres_hartree(lres_ctx* ctx, const double* dens, double* vh, void* stream);

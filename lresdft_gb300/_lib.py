@@ -18,7 +18,7 @@ ERRORS = {-22: "EINVAL", -12: "ENOMEM", -5: "ECUDA", -33: "ENUMERIC", -71: "ESTA
 
 EXPORTS = ("lres_version", "lres_last_error", "lres_ctx_create", "lres_ctx_destroy", "lres_set_potential",
            "lres_set_hamiltonian_csr", "lres_pass", "lres_timings", "lres_window_sums", "lres_inertia", "lres_min_eig",
-           "lres_voronoi_owner", "lres_lda_xc", "lres_hartree", "lres_ion_potential")
+           "lres_voronoi_owner", "lres_lda_xc", "lres_hartree", "lres_ion_potential", "lres_inertia_noalloc")
 
 
 class LResError(RuntimeError):
@@ -67,6 +67,7 @@ def _load():
         "lres_lda_xc": (i32, [vp, vp, vp, vp, vp]),
         "lres_hartree": (i32, [vp, vp, vp, vp]),
         "lres_ion_potential": (i32, [vp, i64, PD, PD, PD, vp, vp]),
+        "lres_inertia_noalloc": (i32, [C.c_int32, vp, vp, vp, vp, dbl, vp, C.c_int32, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

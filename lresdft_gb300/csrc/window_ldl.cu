@@ -33,6 +33,9 @@
 #include "common.cuh"
 #include "lres_internal.h"
 
+#include <cmath>
+#include <mutex>
+
 namespace lres {
 
 __device__ __forceinline__ double shfl(double x, int src) { return __shfl_sync(0xffffffffu, x, src); }
@@ -368,3 +371,139 @@ int run_ldl(const LdlJob& j, cudaStream_t s) {
 }
 
 }  // namespace lres
+
+// ---------------------------------------------------------------------------
+// Window inertia counts with no device allocation.
+//
+// Some callers cannot allocate GPU memory on their own: hosts that hand out all device
+// memory from their own arena or caching allocator and forbid foreign cudaMalloc, and
+// latency-critical loops where the device-wide synchronisation of cudaMalloc/cudaFree
+// is not acceptable.  lres_inertia_noalloc serves them: the caller passes device
+// arrays for inputs and outputs, and the kernel's scratch (work queue, status word,
+// shift, work items, per-CTA factorisation workspaces) lives in the file-scope array
+// below, which every GPU that loads this library holds until the process exits.
+// ---------------------------------------------------------------------------
+
+namespace lres {
+namespace {
+
+constexpr int NOALLOC_MAX_N = 512;            // largest window dimension
+constexpr int NOALLOC_MAX_WIN = 65536;        // most windows per call
+constexpr int NOALLOC_SLOTS = 8;              // CTAs (one factorisation workspace each)
+constexpr size_t NA_HDR = 256;                // counter, status, shift
+constexpr size_t NA_ITEMS = sizeof(int2) * NOALLOC_MAX_WIN;
+constexpr size_t NA_WS = sizeof(double) * (size_t)NOALLOC_MAX_N * NOALLOC_MAX_N * NOALLOC_SLOTS;
+constexpr size_t NA_BYTES = NA_HDR + NA_ITEMS + NA_WS;   // 16.5 MiB
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
+
+struct NoallocDevice {
+    bool ready = false;
+    unsigned char* base = nullptr;   // device address of g_noalloc_scratch on this device
+    int smem_budget = 0;
+};
+std::mutex g_noalloc_mu;
+NoallocDevice g_noalloc_dev[64];
+
+__global__ void noalloc_init_kernel(unsigned char* base, int nwin, double sigma) {
+    int* counter = reinterpret_cast<int*>(base);
+    int* status = counter + 1;
+    double* shift = reinterpret_cast<double*>(base + 8);
+    int2* items = reinterpret_cast<int2*>(base + NA_HDR);
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t == 0) {
+        *counter = 0;
+        *status = 0;
+        *shift = sigma;
+    }
+    for (int w = t; w < nwin; w += gridDim.x * blockDim.x) items[w] = make_int2(w, 0);
+}
+
+// Device address of the scratch array on the current device (set up on first use).
+int noalloc_device(NoallocDevice** out) {
+    int dev = 0;
+    LRES_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) {
+        lres_set_error("device index %d out of range", dev);
+        return LRES_EINVAL;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    NoallocDevice& d = g_noalloc_dev[dev];
+    if (!d.ready) {
+        void* ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess) {
+            lres_set_error("cudaGetSymbolAddress of the scratch array failed: %s", cudaGetErrorString(e));
+            return LRES_ECUDA;
+        }
+        int optin = 0;
+        LRES_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        d.base = static_cast<unsigned char*>(ptr);
+        d.smem_budget = optin - 1024;
+        d.ready = true;
+    }
+    *out = &d;
+    return LRES_OK;
+}
+
+}  // namespace
+
+}  // namespace lres
+
+extern "C" int lres_inertia_noalloc(int32_t nwin, const int32_t* n_w, const int64_t* offC, const double* H,
+                                    const double* S, double sigma, int32_t* below, int32_t nmax, void* stream) {
+    using namespace lres;
+    if (nwin <= 0 || !n_w || !offC || !H || !S || !below) {
+        lres_set_error("lres_inertia_noalloc: null or empty argument");
+        return LRES_EINVAL;
+    }
+    if (nwin > NOALLOC_MAX_WIN || nmax <= 0 || nmax > NOALLOC_MAX_N) {
+        lres_set_error("lres_inertia_noalloc: %d windows of dimension up to %d exceed the limits "
+                       "(%d windows, dimension %d)", nwin, nmax, NOALLOC_MAX_WIN, NOALLOC_MAX_N);
+        return LRES_EINVAL;
+    }
+    if (!std::isfinite(sigma)) {
+        lres_set_error("lres_inertia_noalloc: sigma must be finite");
+        return LRES_EINVAL;
+    }
+    NoallocDevice* dv = nullptr;
+    int rc = noalloc_device(&dv);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned char* base = dv->base;
+    // counter, status, shift and the work items must start fresh on every call
+    noalloc_init_kernel<<<(nwin + 255) / 256, 256, 0, s>>>(base, nwin, sigma);
+    LRES_CUDA_TRY(cudaGetLastError());
+    LdlParams<double> p{};
+    p.nitems = nwin;
+    p.items = reinterpret_cast<const int2*>(base + NA_HDR);
+    p.counter = reinterpret_cast<int*>(base);
+    p.status = reinterpret_cast<int*>(base) + 1;
+    p.n_w = n_w;
+    p.m_w = n_w;
+    p.offC = reinterpret_cast<const long long*>(offC);
+    p.offF = reinterpret_cast<const long long*>(offC);
+    p.offQ = reinterpret_cast<const long long*>(offC);
+    p.C = H;
+    p.B = S;
+    p.F = nullptr;
+    p.shifts = reinterpret_cast<const double*>(base + 8);
+    p.q = nullptr;
+    p.mult = nullptr;
+    p.npos = below;        // work item w is window w: positive pivots of (sigma S - H) = eigenvalues below sigma
+    p.ws = reinterpret_cast<double*>(base + NA_HDR + NA_ITEMS);
+    p.ws_stride = (long long)NOALLOC_MAX_N * NOALLOC_MAX_N;
+    p.ldp = nmax;
+    p.nmax = nmax;
+    p.mmax = 0;
+    rc = dispatch(p, NOALLOC_SLOTS, (size_t)dv->smem_budget, s);
+    if (rc) return rc;
+    int st = 0;
+    LRES_CUDA_TRY(cudaMemcpyAsync(&st, p.status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    LRES_CUDA_TRY(cudaStreamSynchronize(s));
+    if (st & ST_BAD_SHAPE) {
+        lres_set_error("lres_inertia_noalloc: a window is larger than nmax = %d", nmax);
+        return LRES_EINVAL;
+    }
+    return LRES_OK;
+}
