@@ -84,7 +84,7 @@ struct lres_ctx {
     float *d_Hhat32 = nullptr, *d_Fhat32 = nullptr;
     long long sizeC = 0, sizeF = 0;
     // pole work
-    int2 *d_items = nullptr, *d_items_win = nullptr;
+    int2 *d_items = nullptr, *d_items_win = nullptr, *d_items_sub = nullptr;
     int nitems = 0;
     int *d_counter = nullptr, *d_status = nullptr, *d_npos = nullptr;
     void* d_ws = nullptr;
@@ -108,7 +108,7 @@ lres_ctx::~lres_ctx() {
     void* ptrs[] = {d_n, d_m, d_offC, d_offF, d_offQ, d_Oflat, d_wgrp_off, d_wgrp, d_wgrp_lo, d_gloc,
                     bp.gptr, bp.bptr, bp.bcol, bp.brow, bp.boff, bp.btrans, bp.pair_blk, sp.soff, sp.sgrid,
                     sp.sval, sp.coff, sp.cslot, d_Sblk, d_Tblk, d_Hblk, d_SW, d_HW, d_F, d_LinvT, d_Y, d_Hhat,
-                    d_Hhat32, d_Fhat32, d_items, d_items_win, d_counter, d_status, d_npos, d_ws, d_shifts,
+                    d_Hhat32, d_Fhat32, d_items, d_items_win, d_items_sub, d_counter, d_status, d_npos, d_ws, d_shifts,
                     d_wq, d_wzq, d_q, d_dens, d_nw, d_ew, d_v, d_fftwork};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -551,6 +551,7 @@ extern "C" int lres_ctx_create(lres_ctx** out, const lres_system_desc* d, int pr
     std::vector<int2> witems(c->nwin);
     for (int w = 0; w < c->nwin; ++w) witems[w] = make_int2(w, 0);
     TRY(upload(&c->d_items_win, witems, s));
+    TRY(dalloc(&c->d_items_sub, c->nwin));
     TRY(dalloc(&c->d_counter, 1));
     TRY(dalloc(&c->d_status, 1));
     LRES_CUDA_TRY(cudaMemsetAsync(c->d_status, 0, sizeof(int), s));
@@ -795,39 +796,84 @@ extern "C" int lres_inertia(lres_ctx* c, double sigma, int32_t* below, int64_t* 
     return LRES_OK;
 }
 
+// Inertia of the windows listed in `wins` (host), counts into cnt (host).
+static int inertia_subset(lres_ctx* c, double sigma, const std::vector<int>& wins, std::vector<int>& cnt,
+                          cudaStream_t s) {
+    std::vector<int2> items(wins.size());
+    for (size_t i = 0; i < wins.size(); ++i) items[i] = make_int2(wins[i], 0);
+    LRES_CUDA_TRY(cudaMemcpyAsync(c->d_items_sub, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice, s));
+    LRES_CUDA_TRY(cudaMemcpyAsync(c->d_shifts, &sigma, sizeof(double), cudaMemcpyHostToDevice, s));
+    TRY(ldl_launch(c, LdlJob::R64, (int)wins.size(), c->d_items_sub, c->d_HW, c->d_SW, nullptr, c->d_m, c->d_offF,
+                   c->d_shifts, nullptr, nullptr, c->nmax, 0, s));
+    cnt.resize(wins.size());
+    LRES_CUDA_TRY(cudaMemcpyAsync(cnt.data(), c->d_npos, sizeof(int) * wins.size(), cudaMemcpyDeviceToHost, s));
+    LRES_CUDA_TRY(cudaStreamSynchronize(s));
+    return LRES_OK;
+}
+
 extern "C" int lres_min_eig(lres_ctx* c, double lo, double hi, double tol, double* lam_min, void* stream) {
     if (!c || !lam_min || !(hi > lo) || !(tol > 0)) {
         lres_set_error("bad arguments to lres_min_eig");
         return LRES_EINVAL;
     }
-    int64_t t = 0;
-    for (int it = 0; it < 60; ++it) {   // lo must have no eigenvalue below it
-        TRY(lres_inertia(c, lo, nullptr, &t, stream));
-        if (t == 0) break;
-        const double wdt = hi - lo;
-        hi = lo;
-        lo -= 2 * wdt;
+    if (!c->have_h) {
+        lres_set_error("lres_min_eig before a Hamiltonian was set");
+        return LRES_ESTATE;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    std::vector<int> all(c->nwin), cnt;
+    std::iota(all.begin(), all.end(), 0);
+    auto any_below = [&](double sigma, const std::vector<int>& wins, std::vector<int>* keep) -> int {
+        TRY(inertia_subset(c, sigma, wins, cnt, s));
+        int found = 0;
+        if (keep) keep->clear();
+        for (size_t i = 0; i < wins.size(); ++i)
+            if (cnt[i] > 0) {
+                found = 1;
+                if (keep) keep->push_back(wins[i]);
+            }
+        return found ? 1 : 0;
+    };
+    // lo must have no eigenvalue below it in any window
+    for (int it = 0;; ++it) {
+        const int r = any_below(lo, all, nullptr);
+        if (r < 0) return r;
+        if (r == 0) break;
         if (it == 59) {
             lres_set_error("no lower bound found for the window spectra");
             return LRES_ENUMERIC;
         }
-    }
-    for (int it = 0; it < 60; ++it) {   // hi must have one below it
-        TRY(lres_inertia(c, hi, nullptr, &t, stream));
-        if (t > 0) break;
         const double wdt = hi - lo;
-        lo = hi;
-        hi += 2 * wdt;
+        hi = lo;
+        lo -= 2 * wdt;
+    }
+    // hi must have an eigenvalue below it; only windows with one can hold the minimum
+    std::vector<int> cand;
+    for (int it = 0;; ++it) {
+        const int r = any_below(hi, all, &cand);
+        if (r < 0) return r;
+        if (r == 1) break;
         if (it == 59) {
             lres_set_error("no upper bound found for the smallest window eigenvalue");
             return LRES_ENUMERIC;
         }
+        const double wdt = hi - lo;
+        lo = hi;
+        hi += 2 * wdt;
     }
+    // bisection on the candidate windows, pruning those with no eigenvalue below hi
+    std::vector<int> next;
     while (hi - lo > tol) {
         const double mid = 0.5 * (lo + hi);
         if (mid <= lo || mid >= hi) break;
-        TRY(lres_inertia(c, mid, nullptr, &t, stream));
-        if (t > 0) hi = mid; else lo = mid;
+        const int r = any_below(mid, cand, &next);
+        if (r < 0) return r;
+        if (r == 1) {
+            hi = mid;
+            cand.swap(next);
+        } else {
+            lo = mid;
+        }
     }
     *lam_min = 0.5 * (lo + hi);
     return LRES_OK;

@@ -99,6 +99,8 @@ class LResGPU:
         self.passes = 0
         self.inertia_calls = 0
         self._slope = None
+        self._mu_last = None       # last accepted mu (survives StaleMu / cold steps)
+        self._lam_min = None       # last smallest window eigenvalue
         self.trace = None          # set to a list to record (mu, N(mu)) of every pass
         self._gpu_h = _plain_lcao(basis)
         X, S = csr64(basis.Xr), csr64(basis.S)
@@ -347,11 +349,28 @@ class LResGPU:
                     return dens.reshape(cr.shape), eb, mu
                 if abs(cnt) > tol:
                     mu, dens, eb = self._solve_mu(e_lo, N, ftol, start=(mu, cnt, dens, eb))
-                self.mu = mu
+                self.mu = self._mu_last = mu
                 return dens.reshape(cr.shape), eb, mu
-        # cold path
-        lam_min = self.min_eig(-1.0, 0.0, tol=1e-10)
+        # cold path: new filter edge from the smallest window eigenvalue (inertia bisection,
+        # bracketed around the previous one when there is one)
+        if self._lam_min is not None:
+            lam_min = self.min_eig(self._lam_min - 0.05, self._lam_min + 0.05, tol=1e-10)
+        else:
+            lam_min = self.min_eig(-1.0, 0.0, tol=1e-10)
+        self._lam_min = lam_min
         e_lo = lam_min - self.margin
-        mu, dens, eb = self._solve_mu(e_lo, N, ftol, lo_start=max(lam_min, e_lo + 1e-6))
+        lo = max(lam_min, e_lo + 1e-6)
+        found = False
+        if self._mu_last is not None and self._mu_last > lo:
+            # the root of the (monotone) count is unique: start from the previous mu
+            try:
+                dens, n, eb = self.pole_pass(self._mu_last, e_lo)
+                mu, dens, eb = self._solve_mu(e_lo, N, ftol, start=(self._mu_last, n - N, dens, eb))
+                found = True
+            except StaleMu:
+                pass
+        if not found:
+            mu, dens, eb = self._solve_mu(e_lo, N, ftol, lo_start=lo)
         self.mu, self.e_lo = mu, e_lo
+        self._mu_last = mu
         return dens.reshape(cr.shape), eb, mu
