@@ -147,12 +147,15 @@ int ldl_launch(lres_ctx* c, LdlJob::Kind kind, int nitems, const int2* items, co
     j.nmax = c->nmax;
     j.mmax = mmax;
     const size_t el = kind == LdlJob::C128 ? 16 : 8;
-    j.ws_stride = (long long)(c->ws_bytes / el / c->nsm);
-    if ((long long)ldp * c->nmax > j.ws_stride) {
+    const int slots = kind == LdlJob::R64 ? c->nsm : 2 * c->nsm;   // complex: 2 CTAs per SM
+    j.ws_stride = (long long)(c->ws_bytes / el / slots);
+    const long long nmaxp = (c->nmax + 31) / 32 * 32;   // padded window dimension (complex kernel)
+    const long long need = kind == LdlJob::R64 ? (long long)ldp * c->nmax : (nmaxp + mmax) * nmaxp;
+    if (need > j.ws_stride) {
         lres_set_error("workspace too small");
         return LRES_EINVAL;
     }
-    j.grid = c->nsm;
+    j.grid = slots;
     j.smem_budget = c->smem_budget;
     LRES_CUDA_TRY(cudaMemsetAsync(c->d_counter, 0, sizeof(int), s));
     return run_ldl(j, s);
@@ -558,9 +561,10 @@ extern "C" int lres_ctx_create(lres_ctx** out, const lres_system_desc* d, int pr
     TRY(dalloc(&c->d_npos, std::max(c->nitems, c->nwin)));
 
     // workspace: one slot per SM, large enough for (n + n) x n real or (n + m) x n complex
+    const long long nmaxp = (c->nmax + 31) / 32 * 32;
     const long long ldmax = std::max<long long>(c->nmax + c->mmax, 2LL * c->nmax);
-    const size_t slot = (size_t)ldmax * c->nmax * 16;
-    c->ws_bytes = slot * c->nsm;
+    const size_t slot = std::max<size_t>((size_t)ldmax * c->nmax, (size_t)(nmaxp + c->mmax) * nmaxp) * 16;
+    c->ws_bytes = slot * 2 * c->nsm;
     TRY(dalloc((char**)&c->d_ws, c->ws_bytes));
 
     // ---- standard form for the mixed path: L_c^-1 (as L^-T) and F^ = L_c^-1 F, FP64

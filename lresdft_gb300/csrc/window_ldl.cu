@@ -297,6 +297,230 @@ __global__ void __launch_bounds__(NT) ldl_aug_kernel(LdlParams<T> p) {
 }
 
 // ---------------------------------------------------------------------------
+// Left-looking variant for the complex pole solves (the production path).
+//
+// Panel j (columns [j0, j0+NB)) is accumulated in registers, one augmented row per
+// thread, as  A[i, panel] - sum_{k < j0} G[i, k] G[panel, k]^T  with G = L sqrt(D)
+// (complex symmetric: L D L^T = G G^T); the G rows of the panel columns are staged in
+// shared memory in chunks of KC and broadcast, the row's own G[i, k] streams from the
+// L2-resident workspace with coalesced loads.  The panel is then factored in place: the
+// NB x NB diagonal block by one warp (registers and shuffles), every other row by a
+// forward solve in its own registers, and only the finished G columns are written back.
+// Compared with the right-looking form the trailing matrix is never read-modified-written:
+// global traffic per item drops from ~rows*n*n/NB to ~rows*n*n/(2 NB) reads plus one write
+// of G, and all loads are independent of the FMAs they feed.
+// ---------------------------------------------------------------------------
+template <class T, int NB, int NT, int KC>
+__global__ void __launch_bounds__(NT, 2) ldl_left_kernel(LdlParams<T> p) {
+    using E = El<T>;
+    using R = typename E::R;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* Bs = reinterpret_cast<T*>(smem_raw);          // [KC][NB]: Bs[kk*NB + c] = G[j0 + c, k0 + kk]
+    T* Dg = Bs + KC * NB;                            // [32][NB+1]: warp 0's rows (the diagonal block first)
+    T* WL = Dg + 32 * (NB + 1);                      // [NB][NB]: WL[kk*NB + kk2] = D_kk L_kk2,kk
+    T* Dsh = WL + NB * NB;
+    T* Dinv = Dsh + NB;
+    T* Dsq = Dinv + NB;
+    T* qsh = Dsq + NB;                               // mmax
+    T* accS = qsh + p.mmax;                          // [NB][NT]: the row's running panel values
+    __shared__ int item_sh;
+    const int tid = threadIdx.x;
+    T* G = p.ws + (size_t)blockIdx.x * p.ws_stride;
+
+    for (;;) {
+        if (tid == 0) item_sh = atomicAdd(p.counter, 1);
+        __syncthreads();
+        const int it = item_sh;
+        if (it >= p.nitems) return;
+        const int w = p.items[it].x, k = p.items[it].y;
+        const int n = p.n_w[w];
+        const int m = p.F ? p.m_w[w] : 0;
+        // The window is padded to np = a multiple of NB with identity rows/columns
+        // (pivot 1, no coupling): every panel is full and the quadratic forms are unchanged.
+        const int np = (n + NB - 1) / NB * NB;
+        const int rows = np + m;
+        const long long ld = rows;
+        if (n > p.nmax || m > p.mmax) {
+            if (tid == 0) atomicOr(p.status, ST_BAD_SHAPE);
+            __syncthreads();
+            continue;
+        }
+        const T z = p.shifts[k];
+        const R* C = p.C ? p.C + p.offC[w] : nullptr;
+        const R* B = p.B ? p.B + p.offC[w] : nullptr;
+        const R* F = p.F ? p.F + p.offF[w] : nullptr;
+        for (int r = tid; r < m; r += NT) qsh[r] = E::zero();
+        __syncthreads();
+
+        for (int j0 = 0; j0 < np; j0 += NB) {
+            const int na = rows - j0;
+            for (int b0 = 0; b0 < na; b0 += NT) {
+                const int ir = b0 + tid;              // row within the panel
+                const int i = j0 + ir;
+                const bool active = ir < na;
+                T acc[NB];
+                if (active && i < n) {
+                    const R* cp = C ? C + i + (long long)j0 * n : nullptr;
+                    const R* bp = B ? B + i + (long long)j0 * n : nullptr;
+#pragma unroll
+                    for (int c = 0; c < NB; ++c) {
+                        const int col = j0 + c;
+                        T a = E::zero();
+                        if (col <= i) {                // lower triangle (col < n follows)
+                            const R bb = bp ? bp[(long long)c * n] : (i == col ? R(1) : R(0));
+                            const R cc = cp ? cp[(long long)c * n] : R(0);
+                            a = E::shift_minus(z, bb, cc);
+                        }
+                        acc[c] = a;
+                    }
+                } else if (active && i < np) {        // padding row: identity
+#pragma unroll
+                    for (int c = 0; c < NB; ++c) acc[c] = (j0 + c == i) ? E::from(R(1)) : E::zero();
+                } else if (active) {                  // right-hand-side row r = i - np
+                    const R* fp = F + (i - np) + (long long)j0 * m;
+#pragma unroll
+                    for (int c = 0; c < NB; ++c) acc[c] = (j0 + c < n) ? E::from(fp[(long long)c * m]) : E::zero();
+                } else {
+#pragma unroll
+                    for (int c = 0; c < NB; ++c) acc[c] = E::zero();
+                }
+                // Blocked accumulation: each KC-chunk of the k sum is formed from zero in
+                // registers and subtracted from the row's running value, kept in shared memory
+                // (the same rounding pattern as a right-looking update by KC-wide panels).
+                if (j0 > 0) {
+#pragma unroll
+                    for (int c = 0; c < NB; ++c) accS[c * NT + tid] = acc[c];
+                }
+                for (int k0 = 0; k0 < j0; k0 += KC) {
+                    const int kc = min(KC, j0 - k0);
+                    __syncthreads();                  // previous chunk consumed
+                    for (int idx = tid; idx < kc * NB; idx += NT) {
+                        const int kk = idx / NB, c = idx % NB;
+                        Bs[idx] = G[(j0 + c) + (long long)(k0 + kk) * ld];
+                    }
+                    __syncthreads();
+                    if (active) {
+                        const T* gi = G + i + (long long)k0 * ld;
+                        T tmp[NB];
+#pragma unroll
+                        for (int c = 0; c < NB; ++c) tmp[c] = E::zero();
+                        int kk = 0;
+                        for (; kk + 2 <= kc; kk += 2) {
+                            const T g0 = gi[(long long)kk * ld], g1 = gi[(long long)(kk + 1) * ld];
+                            const T* b = Bs + kk * NB;
+#pragma unroll
+                            for (int c = 0; c < NB; ++c) {
+                                T a = tmp[c];
+                                a = E::fma(g0, b[c], a);
+                                a = E::fma(g1, b[NB + c], a);
+                                tmp[c] = a;
+                            }
+                        }
+                        for (; kk < kc; ++kk) {
+                            const T g0 = gi[(long long)kk * ld];
+                            const T* b = Bs + kk * NB;
+#pragma unroll
+                            for (int c = 0; c < NB; ++c) tmp[c] = E::fma(g0, b[c], tmp[c]);
+                        }
+#pragma unroll
+                        for (int c = 0; c < NB; ++c) accS[c * NT + tid] = E::sub(accS[c * NT + tid], tmp[c]);
+                    }
+                }
+                if (j0 > 0) {
+#pragma unroll
+                    for (int c = 0; c < NB; ++c) acc[c] = accS[c * NT + tid];
+                }
+                if (b0 == 0) {
+                    // warp 0 parks its accumulated rows (the diagonal block is rows 0..NB-1)
+                    // in shared memory while it factors the block, then reloads them
+                    if (tid < 32) {
+#pragma unroll
+                        for (int c = 0; c < NB; ++c) Dg[tid * (NB + 1) + c] = acc[c];
+                    }
+                    __syncthreads();
+                    if (tid < 32) {
+                        // LDL^T of the NB x NB diagonal block in shared memory: lane = row;
+                        // the column operand L_c,kk is a broadcast read of row c
+                        const int lane = tid;
+                        T* myrow = Dg + lane * (NB + 1);
+                        for (int kk = 0; kk < NB; ++kk) {
+                            __syncwarp();
+                            const T d = Dg[kk * (NB + 1) + kk];
+                            const T dinv = E::inv(d);
+                            const bool mine = lane > kk && lane < NB;
+                            T l = E::zero();
+                            if (mine) {
+                                l = E::mul(myrow[kk], dinv);
+                                myrow[kk] = l;
+                            }
+                            if (lane == kk) {
+                                Dsh[kk] = d;
+                                Dinv[kk] = dinv;
+                                Dsq[kk] = E::csqrt(d);
+                                const double m2 = (double)E::mag2(d);
+                                if (!(m2 > 0.0) || !isfinite(m2)) atomicOr(p.status, ST_ZERO_PIVOT);
+                            }
+                            __syncwarp();
+                            if (mine) {
+                                const T ldv = E::mul(l, d);
+                                for (int c = kk + 1; c <= lane; ++c)
+                                    myrow[c] = E::fms(ldv, Dg[c * (NB + 1) + kk], myrow[c]);
+                            }
+                        }
+                        __syncwarp();
+                        for (int kk = 0; kk < NB; ++kk)
+                            if (lane > kk && lane < NB) WL[kk * NB + lane] = E::mul(Dsh[kk], myrow[kk]);
+                    }
+                    __syncthreads();
+                    // warp 0 reloads its parked rows (rows below the block still need the solve)
+                    if (tid < 32) {
+#pragma unroll
+                        for (int c = 0; c < NB; ++c) acc[c] = Dg[tid * (NB + 1) + c];
+                    }
+                    __syncthreads();
+                }
+                if (active && ir >= NB) {
+#pragma unroll
+                    for (int kk = 0; kk < NB; ++kk) {
+                        const T l = E::mul(acc[kk], Dinv[kk]);
+#pragma unroll
+                        for (int kk2 = kk + 1; kk2 < NB; ++kk2) acc[kk2] = E::fms(l, WL[kk * NB + kk2], acc[kk2]);
+                        acc[kk] = l;
+                    }
+                    if (i >= np) {
+                        T qv = qsh[i - np];
+#pragma unroll
+                        for (int kk = 0; kk < NB; ++kk) qv = E::fma(E::mul(acc[kk], acc[kk]), Dsh[kk], qv);
+                        qsh[i - np] = qv;
+                    }
+                    if (j0 + NB < np) {
+                        T* gout = G + i + (long long)j0 * ld;
+#pragma unroll
+                        for (int kk = 0; kk < NB; ++kk) gout[(long long)kk * ld] = E::mul(acc[kk], Dsq[kk]);
+                    }
+                }
+            }
+            __syncthreads();                          // finished G columns visible to the next panel
+        }
+        if (p.q) {
+            T* qo = p.q + (long long)k * p.qstride + p.offQ[w];
+            for (int r = tid; r < m; r += NT) qo[r] = qsh[r];
+        }
+        __syncthreads();
+    }
+}
+
+template <class T, int NB, int NT, int KC>
+static int launch_left(const LdlParams<T>& p, int grid, cudaStream_t s) {
+    const size_t smem = sizeof(T) * ((size_t)KC * NB + 32 * (NB + 1) + NB * NB + 3 * NB + p.mmax + (size_t)NB * NT);
+    auto kern = ldl_left_kernel<T, NB, NT, KC>;
+    LRES_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<grid, NT, smem, s>>>(p);
+    LRES_CUDA_TRY(cudaGetLastError());
+    return LRES_OK;
+}
+
+// ---------------------------------------------------------------------------
 // host launchers
 // ---------------------------------------------------------------------------
 
@@ -348,7 +572,7 @@ int run_ldl(const LdlJob& j, cudaStream_t s) {
         p.shifts = (const double2*)j.shifts; p.q = (double2*)j.q; p.qstride = j.qstride;
         p.mult = nullptr; p.npos = j.npos; p.status = j.status;
         p.ws = (double2*)j.ws; p.ws_stride = j.ws_stride; p.ldp = j.ldp; p.nmax = j.nmax; p.mmax = j.mmax;
-        return dispatch(p, j.grid, budget, s);
+        return launch_left<double2, 16, 256, 32>(p, j.grid, s);
     } else if (j.kind == LdlJob::C64) {
         LdlParams<float2> p{};
         p.nitems = j.nitems; p.items = j.items; p.counter = j.counter;
@@ -357,7 +581,7 @@ int run_ldl(const LdlJob& j, cudaStream_t s) {
         p.shifts = (const float2*)j.shifts; p.q = (float2*)j.q; p.qstride = j.qstride;
         p.mult = nullptr; p.npos = j.npos; p.status = j.status;
         p.ws = (float2*)j.ws; p.ws_stride = j.ws_stride; p.ldp = j.ldp; p.nmax = j.nmax; p.mmax = j.mmax;
-        return dispatch(p, j.grid, budget, s);
+        return launch_left<float2, 32, 256, 32>(p, j.grid, s);
     } else {
         LdlParams<double> p{};
         p.nitems = j.nitems; p.items = j.items; p.counter = j.counter;
