@@ -64,6 +64,7 @@ struct lres_ctx {
     int nwin = 0, ngroups = 0, nmax = 0, mmax = 0, nsm = 0;
     long long npts = 0;
     bool have_T = false, have_h = false;
+    int config = 0;                      // tile configuration of the complex pole kernel
     size_t smem_budget = 0;
     // host copies
     std::vector<int> n_w, m_w, gptr_h, order;
@@ -147,7 +148,7 @@ int ldl_launch(lres_ctx* c, LdlJob::Kind kind, int nitems, const int2* items, co
     j.nmax = c->nmax;
     j.mmax = mmax;
     const size_t el = kind == LdlJob::C128 ? 16 : 8;
-    const int slots = kind == LdlJob::R64 ? c->nsm : 2 * c->nsm;   // complex: 2 CTAs per SM
+    const int slots = kind == LdlJob::R64 ? c->nsm : 4 * c->nsm;   // complex: up to 4 CTAs per SM
     j.ws_stride = (long long)(c->ws_bytes / el / slots);
     const long long nmaxp = (c->nmax + 31) / 32 * 32;   // padded window dimension (complex kernel)
     const long long need = kind == LdlJob::R64 ? (long long)ldp * c->nmax : (nmaxp + mmax) * nmaxp;
@@ -157,6 +158,7 @@ int ldl_launch(lres_ctx* c, LdlJob::Kind kind, int nitems, const int2* items, co
     }
     j.grid = slots;
     j.smem_budget = c->smem_budget;
+    j.config = c->config;
     LRES_CUDA_TRY(cudaMemsetAsync(c->d_counter, 0, sizeof(int), s));
     return run_ldl(j, s);
 }
@@ -564,7 +566,7 @@ extern "C" int lres_ctx_create(lres_ctx** out, const lres_system_desc* d, int pr
     const long long nmaxp = (c->nmax + 31) / 32 * 32;
     const long long ldmax = std::max<long long>(c->nmax + c->mmax, 2LL * c->nmax);
     const size_t slot = std::max<size_t>((size_t)ldmax * c->nmax, (size_t)(nmaxp + c->mmax) * nmaxp) * 16;
-    c->ws_bytes = slot * 2 * c->nsm;
+    c->ws_bytes = slot * 4 * c->nsm;
     TRY(dalloc((char**)&c->d_ws, c->ws_bytes));
 
     // ---- standard form for the mixed path: L_c^-1 (as L^-T) and F^ = L_c^-1 F, FP64
@@ -740,6 +742,44 @@ extern "C" int lres_pass(lres_ctx* c, double mu, double e_lo, double* dens, int 
         lres_set_error("window kernel status %d", st);
         return LRES_EINVAL;
     }
+    return LRES_OK;
+}
+
+extern "C" int lres_autotune(lres_ctx* c, double mu, double e_lo, int32_t force_config, int32_t* chosen,
+                             double* ms_per_config, void* stream) {
+    if (!c) {
+        lres_set_error("null argument");
+        return LRES_EINVAL;
+    }
+    if (force_config >= kLeftConfigs) {
+        lres_set_error("configuration %d out of range (0..%d)", force_config, kLeftConfigs - 1);
+        return LRES_EINVAL;
+    }
+    if (force_config >= 0) {
+        c->config = force_config;
+        if (chosen) *chosen = force_config;
+        return LRES_OK;
+    }
+    double out[3];
+    double best = 1e300;
+    int arg = 0;
+    for (int cfg = 0; cfg < kLeftConfigs; ++cfg) {
+        c->config = cfg;
+        double ms = 0.0;
+        for (int rep = 0; rep < 2; ++rep) {          // first repetition warms up
+            TRY(lres_pass(c, mu, e_lo, nullptr, 0, out, stream));
+            double t[1];
+            TRY(lres_timings(c, t, 1));
+            ms = t[0];
+        }
+        if (ms_per_config) ms_per_config[cfg] = ms;
+        if (ms < best) {
+            best = ms;
+            arg = cfg;
+        }
+    }
+    c->config = arg;
+    if (chosen) *chosen = arg;
     return LRES_OK;
 }
 

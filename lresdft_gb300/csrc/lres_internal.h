@@ -32,7 +32,14 @@ struct LdlJob {
     int ldp = 0, nmax = 0, mmax = 0;
     int grid = 0;
     size_t smem_budget = 0;
+    int config = 0;                 // complex kernels: tile configuration (see lres_tune)
 };
+
+// Tile configurations of the complex pole kernel, index = LdlJob::config:
+//   0: NB 32 (c64) / 16 (c128), 256 threads, k-chunk 32     1: 128 threads
+//   2: k-chunk 16                                           3: NB 16 (c64) / 8 (c128)
+constexpr int kLeftConfigs = 4;
+constexpr int kLeftNB[2][kLeftConfigs] = {{32, 32, 32, 16}, {16, 16, 16, 8}};   // [c64, c128]
 
 int run_ldl(const LdlJob& j, cudaStream_t s);
 size_t ldl_smem_bytes(int elem_bytes, int nb, int ldp, int mmax);

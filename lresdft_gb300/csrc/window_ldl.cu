@@ -33,6 +33,7 @@
 #include "common.cuh"
 #include "lres_internal.h"
 
+#include <algorithm>
 #include <cmath>
 #include <mutex>
 
@@ -311,7 +312,7 @@ __global__ void __launch_bounds__(NT) ldl_aug_kernel(LdlParams<T> p) {
 // of G, and all loads are independent of the FMAs they feed.
 // ---------------------------------------------------------------------------
 template <class T, int NB, int NT, int KC>
-__global__ void __launch_bounds__(NT, 2) ldl_left_kernel(LdlParams<T> p) {
+__global__ void __launch_bounds__(NT, 512 / NT) ldl_left_kernel(LdlParams<T> p) {
     using E = El<T>;
     using R = typename E::R;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -515,6 +516,12 @@ static int launch_left(const LdlParams<T>& p, int grid, cudaStream_t s) {
     const size_t smem = sizeof(T) * ((size_t)KC * NB + 32 * (NB + 1) + NB * NB + 3 * NB + p.mmax + (size_t)NB * NT);
     auto kern = ldl_left_kernel<T, NB, NT, KC>;
     LRES_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // persistent grid: as many CTAs as fit on the device, at most one workspace slot each
+    int dev = 0, nsm = 0, per_sm = 0;
+    LRES_CUDA_TRY(cudaGetDevice(&dev));
+    LRES_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    LRES_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem));
+    grid = std::min(grid, std::max(1, per_sm) * nsm);
     kern<<<grid, NT, smem, s>>>(p);
     LRES_CUDA_TRY(cudaGetLastError());
     return LRES_OK;
@@ -572,7 +579,12 @@ int run_ldl(const LdlJob& j, cudaStream_t s) {
         p.shifts = (const double2*)j.shifts; p.q = (double2*)j.q; p.qstride = j.qstride;
         p.mult = nullptr; p.npos = j.npos; p.status = j.status;
         p.ws = (double2*)j.ws; p.ws_stride = j.ws_stride; p.ldp = j.ldp; p.nmax = j.nmax; p.mmax = j.mmax;
-        return launch_left<double2, 16, 256, 32>(p, j.grid, s);
+        switch (j.config) {
+            case 1: return launch_left<double2, 16, 128, 32>(p, j.grid, s);
+            case 2: return launch_left<double2, 16, 256, 16>(p, j.grid, s);
+            case 3: return launch_left<double2, 8, 256, 32>(p, j.grid, s);
+            default: return launch_left<double2, 16, 256, 32>(p, j.grid, s);
+        }
     } else if (j.kind == LdlJob::C64) {
         LdlParams<float2> p{};
         p.nitems = j.nitems; p.items = j.items; p.counter = j.counter;
@@ -581,7 +593,12 @@ int run_ldl(const LdlJob& j, cudaStream_t s) {
         p.shifts = (const float2*)j.shifts; p.q = (float2*)j.q; p.qstride = j.qstride;
         p.mult = nullptr; p.npos = j.npos; p.status = j.status;
         p.ws = (float2*)j.ws; p.ws_stride = j.ws_stride; p.ldp = j.ldp; p.nmax = j.nmax; p.mmax = j.mmax;
-        return launch_left<float2, 32, 256, 32>(p, j.grid, s);
+        switch (j.config) {
+            case 1: return launch_left<float2, 32, 128, 32>(p, j.grid, s);
+            case 2: return launch_left<float2, 32, 256, 16>(p, j.grid, s);
+            case 3: return launch_left<float2, 16, 256, 32>(p, j.grid, s);
+            default: return launch_left<float2, 32, 256, 32>(p, j.grid, s);
+        }
     } else {
         LdlParams<double> p{};
         p.nitems = j.nitems; p.items = j.items; p.counter = j.counter;
