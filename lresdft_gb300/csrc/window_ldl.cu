@@ -311,13 +311,35 @@ __global__ void __launch_bounds__(NT) ldl_aug_kernel(LdlParams<T> p) {
 // global traffic per item drops from ~rows*n*n/NB to ~rows*n*n/(2 NB) reads plus one write
 // of G, and all loads are independent of the FMAs they feed.
 // ---------------------------------------------------------------------------
+// asynchronous global -> shared copies (cp.async, one element per instruction)
+template <class T>
+__device__ __forceinline__ void cp_async_el(T* dst, const T* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    if constexpr (sizeof(T) == 16)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src));
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Copies rows [j0, j0+NB) x columns [k0, k0+kc) of G into buf[kk*NB + c].
+template <class T, int NB, int NT, int KC>
+__device__ __forceinline__ void stage_chunk(T* buf, const T* G, long long ld, int j0, int k0, int kc) {
+    for (int idx = threadIdx.x; idx < kc * NB; idx += NT) {
+        const int kk = idx / NB, c = idx % NB;
+        cp_async_el(buf + idx, G + (j0 + c) + (long long)(k0 + kk) * ld);
+    }
+    cp_async_commit();
+}
+
 template <class T, int NB, int NT, int KC>
 __global__ void __launch_bounds__(NT, 512 / NT) ldl_left_kernel(LdlParams<T> p) {
     using E = El<T>;
     using R = typename E::R;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* Bs = reinterpret_cast<T*>(smem_raw);          // [KC][NB]: Bs[kk*NB + c] = G[j0 + c, k0 + kk]
-    T* Dg = Bs + KC * NB;                            // [32][NB+1]: warp 0's rows (the diagonal block first)
+    T* Bs = reinterpret_cast<T*>(smem_raw);          // [2][KC][NB]: Bs[kk*NB + c] = G[j0 + c, k0 + kk], double-buffered
+    T* Dg = Bs + 2 * KC * NB;                        // [32][NB+1]: warp 0's rows (the diagonal block first)
     T* WL = Dg + 32 * (NB + 1);                      // [NB][NB]: WL[kk*NB + kk2] = D_kk L_kk2,kk
     T* Dsh = WL + NB * NB;
     T* Dinv = Dsh + NB;
@@ -392,23 +414,35 @@ __global__ void __launch_bounds__(NT, 512 / NT) ldl_left_kernel(LdlParams<T> p) 
 #pragma unroll
                     for (int c = 0; c < NB; ++c) accS[c * NT + tid] = acc[c];
                 }
-                for (int k0 = 0; k0 < j0; k0 += KC) {
-                    const int kc = min(KC, j0 - k0);
-                    __syncthreads();                  // previous chunk consumed
-                    for (int idx = tid; idx < kc * NB; idx += NT) {
-                        const int kk = idx / NB, c = idx % NB;
-                        Bs[idx] = G[(j0 + c) + (long long)(k0 + kk) * ld];
-                    }
-                    __syncthreads();
+                // chunks of the panel's G rows are copied asynchronously into a double buffer:
+                // chunk ci+1 is in flight while chunk ci is used; one barrier per chunk
+                const int nch = (j0 + KC - 1) / KC;
+                if (nch > 0) {
+                    __syncthreads();                  // the previous loop's last buffer is free
+                    stage_chunk<T, NB, NT, KC>(Bs, G, ld, j0, 0, min(KC, j0));
+                }
+                for (int ci = 0; ci < nch; ++ci) {
+                    const int k0 = ci * KC;
+                    const int kc = min(KC, j0 - k0);   // a multiple of 8
+                    cp_async_wait_all();
+                    __syncthreads();                  // chunk ci visible; chunk ci-1 consumed
+                    if (ci + 1 < nch)
+                        stage_chunk<T, NB, NT, KC>(Bs + ((ci + 1) & 1) * KC * NB, G, ld, j0, k0 + KC,
+                                                   min(KC, j0 - k0 - KC));
                     if (active) {
                         const T* gi = G + i + (long long)k0 * ld;
+                        const T* bbuf = Bs + (ci & 1) * KC * NB;
                         T tmp[NB];
 #pragma unroll
                         for (int c = 0; c < NB; ++c) tmp[c] = E::zero();
-                        int kk = 0;
-                        for (; kk + 2 <= kc; kk += 2) {
-                            const T g0 = gi[(long long)kk * ld], g1 = gi[(long long)(kk + 1) * ld];
-                            const T* b = Bs + kk * NB;
+                        T g0 = gi[0], g1 = gi[ld];
+                        for (int kk = 0; kk < kc; kk += 2) {
+                            T n0 = g0, n1 = g1;
+                            if (kk + 2 < kc) {        // prefetch the next pair of the row's G values
+                                n0 = gi[(long long)(kk + 2) * ld];
+                                n1 = gi[(long long)(kk + 3) * ld];
+                            }
+                            const T* b = bbuf + kk * NB;
 #pragma unroll
                             for (int c = 0; c < NB; ++c) {
                                 T a = tmp[c];
@@ -416,12 +450,8 @@ __global__ void __launch_bounds__(NT, 512 / NT) ldl_left_kernel(LdlParams<T> p) 
                                 a = E::fma(g1, b[NB + c], a);
                                 tmp[c] = a;
                             }
-                        }
-                        for (; kk < kc; ++kk) {
-                            const T g0 = gi[(long long)kk * ld];
-                            const T* b = Bs + kk * NB;
-#pragma unroll
-                            for (int c = 0; c < NB; ++c) tmp[c] = E::fma(g0, b[c], tmp[c]);
+                            g0 = n0;
+                            g1 = n1;
                         }
 #pragma unroll
                         for (int c = 0; c < NB; ++c) accS[c * NT + tid] = E::sub(accS[c * NT + tid], tmp[c]);
@@ -513,7 +543,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) ldl_left_kernel(LdlParams<T> p) 
 
 template <class T, int NB, int NT, int KC>
 static int launch_left(const LdlParams<T>& p, int grid, cudaStream_t s) {
-    const size_t smem = sizeof(T) * ((size_t)KC * NB + 32 * (NB + 1) + NB * NB + 3 * NB + p.mmax + (size_t)NB * NT);
+    const size_t smem = sizeof(T) * ((size_t)2 * KC * NB + 32 * (NB + 1) + NB * NB + 3 * NB + p.mmax + (size_t)NB * NT);
     auto kern = ldl_left_kernel<T, NB, NT, KC>;
     LRES_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     // persistent grid: as many CTAs as fit on the device, at most one workspace slot each
