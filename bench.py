@@ -115,7 +115,7 @@ def run_ours(args):
     if args.cells != 8:
         WORKLOAD.update(workload=f"{args.cells}^3 H2 crystal (profiling size), {cr.n_elec} electrons",
                         natoms=len(cr.pos), nwin=len(cr.pos), basis_functions=6 * len(cr.pos), grid=f"{cr.shape[0]}^3")
-    s = LResGPU(b, cr.pos, R_w=8.0, M=64, precision=args.precision)
+    s = LResGPU(b, cr.pos, R_w=8.0, M=64, precision=args.precision, tile_config="auto")
     go = GridOps(s)
     vion = go.ion_potential()
     d0 = np.full(cr.shape, cr.n_elec / (cr.ng * cr.dV))
@@ -224,11 +224,12 @@ def run_ours(args):
                          "gather": round(float(np.mean(gather_ms)), 3),
                          "transform": round(float(np.mean(transform_ms)), 3)},
         "setup_s": round(setup_s, 2), "accuracy": err,
+        "tile_config": {"chosen": s.tile_config, "pole_kernel_ms_per_config": [round(float(x), 2) for x in s.tune_ms]},
     }
 
     # FP64 path on the same potential (the target ratio is mixed vs FP64)
     if args.precision == "mixed" and args.fp64_steps > 0:
-        s64 = LResGPU(b, cr.pos, R_w=8.0, M=64, precision="fp64")
+        s64 = LResGPU(b, cr.pos, R_w=8.0, M=64, precision="fp64", tile_config=3)
         s64.set_potential_device(v_dev.data_ptr())
         s64.pole_pass_device(mu, e_lo)
         torch.cuda.synchronize()

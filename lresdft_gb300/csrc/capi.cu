@@ -82,6 +82,7 @@ struct lres_ctx {
     // dense windows
     double *d_SW = nullptr, *d_HW = nullptr, *d_F = nullptr;
     double *d_LinvT = nullptr, *d_Y = nullptr, *d_Hhat = nullptr;
+    float2 *d_LinvT_df = nullptr, *d_H_df = nullptr, *d_Y_df = nullptr;   // double-float operands
     float *d_Hhat32 = nullptr, *d_Fhat32 = nullptr;
     long long sizeC = 0, sizeF = 0;
     // pole work
@@ -109,7 +110,7 @@ lres_ctx::~lres_ctx() {
     void* ptrs[] = {d_n, d_m, d_offC, d_offF, d_offQ, d_Oflat, d_wgrp_off, d_wgrp, d_wgrp_lo, d_gloc,
                     bp.gptr, bp.bptr, bp.bcol, bp.brow, bp.boff, bp.btrans, bp.pair_blk, sp.soff, sp.sgrid,
                     sp.sval, sp.coff, sp.cslot, d_Sblk, d_Tblk, d_Hblk, d_SW, d_HW, d_F, d_LinvT, d_Y, d_Hhat,
-                    d_Hhat32, d_Fhat32, d_items, d_items_win, d_items_sub, d_counter, d_status, d_npos, d_ws, d_shifts,
+                    d_Hhat32, d_Fhat32, d_LinvT_df, d_H_df, d_Y_df, d_items, d_items_win, d_items_sub, d_counter, d_status, d_npos, d_ws, d_shifts,
                     d_wq, d_wzq, d_q, d_dens, d_nw, d_ew, d_v, d_fftwork};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -179,10 +180,13 @@ __global__ void identity_kernel(const int* n_w, const long long* off, double* I,
 
 int window_transform(lres_ctx* c, cudaStream_t s) {
     // H^_W = L^-1 H_W L^-T with LinvT = L^-T (upper triangular) stored column-major:
-    // Y = H LinvT (k <= column), then the lower triangle of H^ = LinvT^T Y (k <= row)
-    TRY(batched_gemm(c->nwin, c->d_n, c->d_offC, c->nmax, false, c->d_HW, c->d_LinvT, c->d_Y, s, 1));
-    TRY(batched_gemm(c->nwin, c->d_n, c->d_offC, c->nmax, true, c->d_LinvT, c->d_Y, c->d_Hhat, s, 2));
-    TRY(convert_f64_f32(c->d_Hhat, c->d_Hhat32, c->sizeC, s));
+    // Y = H LinvT (k <= column), then the lower triangle of H^ = LinvT^T Y (k <= row),
+    // both in double-float arithmetic on the FP32 pipes, H^ rounded to FP32 at the end
+    TRY(split_f64(c->d_HW, c->d_H_df, c->sizeC, s));
+    TRY(batched_gemm_df64(c->nwin, c->d_n, c->d_offC, c->nmax, false, 1, c->d_H_df, c->d_LinvT_df, c->d_Y_df,
+                          nullptr, s));
+    TRY(batched_gemm_df64(c->nwin, c->d_n, c->d_offC, c->nmax, true, 2, c->d_LinvT_df, c->d_Y_df, nullptr,
+                          c->d_Hhat32, s));
     return LRES_OK;
 }
 
@@ -572,8 +576,9 @@ extern "C" int lres_ctx_create(lres_ctx** out, const lres_system_desc* d, int pr
     // ---- standard form for the mixed path: L_c^-1 (as L^-T) and F^ = L_c^-1 F, FP64
     if (precision == LRES_MIXED) {
         TRY(dalloc(&c->d_LinvT, c->sizeC));
-        TRY(dalloc(&c->d_Y, c->sizeC));
-        TRY(dalloc(&c->d_Hhat, c->sizeC));
+        TRY(dalloc(&c->d_LinvT_df, c->sizeC));
+        TRY(dalloc(&c->d_H_df, c->sizeC));
+        TRY(dalloc(&c->d_Y_df, c->sizeC));
         TRY(dalloc(&c->d_Hhat32, c->sizeC));
         TRY(dalloc(&c->d_Fhat32, c->sizeF));
         double* I = nullptr;
@@ -595,6 +600,7 @@ extern "C" int lres_ctx_create(lres_ctx** out, const lres_system_desc* d, int pr
             rc = ldl_launch(c.get(), LdlJob::R64, c->nwin, c->d_items_win, nullptr, c->d_SW, c->d_F, c->d_m,
                             c->d_offF, one, nullptr, Fhat, c->nmax + c->mmax, c->mmax, s);
         if (!rc) rc = convert_f64_f32(Fhat, c->d_Fhat32, c->sizeF, s);
+        if (!rc) rc = split_f64(c->d_LinvT, c->d_LinvT_df, c->sizeC, s);
         int st = 0;
         if (!rc) rc = read_status(c.get(), s, &st);
         cudaFree(I);

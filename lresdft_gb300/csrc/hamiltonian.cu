@@ -401,4 +401,125 @@ int pole_sums(int nwin, const long long* offQ, const int* m_w, const long long* 
     return LRES_OK;
 }
 
+
+
+// ---------------------------------------------------------------------------
+// Standard-form transform in double-float arithmetic on the FP32 pipes.
+// Every FP64 operand x is carried as an unevaluated pair (hi, lo) of floats with
+// hi = fl32(x), lo = fl32(x - hi) (about 48 significant bits); products use the exact
+// FMA residual of hi*hi plus the two cross terms, sums use Knuth's TwoSum, so the
+// accumulated result keeps ~1e-14 relative accuracy — far below the FP32 rounding of
+// the final H^ — at ~11 FP32 operations per multiply-add instead of one FP64 FMA.
+// ---------------------------------------------------------------------------
+
+__global__ void split_f64_kernel(const double* a, float2* b, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const double x = a[i];
+        const float hi = (float)x;
+        b[i] = make_float2(hi, (float)(x - (double)hi));
+    }
+}
+
+int split_f64(const double* a, float2* b, long long n, cudaStream_t s) {
+    if (n <= 0) return LRES_OK;
+    split_f64_kernel<<<1216, 256, 0, s>>>(a, b, n);
+    LRES_CUDA_TRY(cudaGetLastError());
+    return LRES_OK;
+}
+
+// Explicitly rounded operations keep the compiler from contracting the error-free
+// transformations into fused multiply-adds.
+__device__ __forceinline__ void df_mac(float2 a, float2 b, float& sh, float& sl) {
+    const float ph = __fmul_rn(a.x, b.x);
+    float pl = fmaf(a.x, b.x, -ph);          // exact residual of the leading product
+    pl = fmaf(a.x, b.y, pl);
+    pl = fmaf(a.y, b.x, pl);
+    const float t = __fadd_rn(sh, ph);       // TwoSum(sh, ph)
+    const float v = __fsub_rn(t, sh);
+    const float e = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, v)), __fsub_rn(ph, v));
+    sl = __fadd_rn(sl, __fadd_rn(e, pl));
+    sh = t;
+}
+
+// KLIM as gemm_f64_kernel.  OUT32: write fl32(hi + lo) to a float array, else (hi, lo).
+template <bool TA, int KLIM, bool OUT32>
+__global__ void __launch_bounds__(256) gemm_df64_kernel(const int* n_w, const long long* off, const float2* A,
+                                                        const float2* B, float2* C, float* C32) {
+    constexpr int BM = 64, BN = 64, BK = 16;
+    const int w = blockIdx.z;
+    const int n = n_w[w];
+    const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+    if (m0 >= n || n0 >= n) return;
+    if (KLIM == 2 && m0 + BM - 1 < n0) return;
+    const int kend = KLIM == 1 ? min(n, n0 + BN) : KLIM == 2 ? min(n, m0 + BM) : n;
+    const float2* Aw = A + off[w];
+    const float2* Bw = B + off[w];
+    __shared__ float2 As[BK][BM + 1];
+    __shared__ float2 Bs[BK][BN + 1];
+    const int tid = threadIdx.x;
+    const int tx = tid % 16, ty = tid / 16;
+    float sh[4][4], sl[4][4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) sh[u][v] = sl[u][v] = 0.f;
+    for (int k0 = 0; k0 < kend; k0 += BK) {
+        for (int idx = tid; idx < BK * BM; idx += 256) {
+            const int kk = idx / BM, i = idx % BM;
+            const int gi = m0 + i, gk = k0 + kk;
+            float2 a = make_float2(0.f, 0.f);
+            if (gi < n && gk < n) a = TA ? Aw[gk + (long long)gi * n] : Aw[gi + (long long)gk * n];
+            As[kk][i] = a;
+        }
+        for (int idx = tid; idx < BK * BN; idx += 256) {
+            const int j = idx / BK, kk = idx % BK;
+            const int gj = n0 + j, gk = k0 + kk;
+            Bs[kk][j] = (gj < n && gk < n) ? Bw[gk + (long long)gj * n] : make_float2(0.f, 0.f);
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int kk = 0; kk < BK; ++kk) {
+            float2 a[4], b[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) a[u] = As[kk][tx + 16 * u];
+#pragma unroll
+            for (int v = 0; v < 4; ++v) b[v] = Bs[kk][ty + 16 * v];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) df_mac(a[u], b[v], sh[u][v], sl[u][v]);
+        }
+        __syncthreads();
+    }
+    float* C32w = OUT32 ? C32 + off[w] : nullptr;
+    float2* Cw = OUT32 ? nullptr : C + off[w];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const int gi = m0 + tx + 16 * u, gj = n0 + ty + 16 * v;
+            if (gi >= n || gj >= n) continue;
+            const float hi = __fadd_rn(sh[u][v], sl[u][v]);          // renormalise (fast TwoSum)
+            const float lo = __fsub_rn(sl[u][v], __fsub_rn(hi, sh[u][v]));
+            if (OUT32) C32w[gi + (long long)gj * n] = hi;
+            else Cw[gi + (long long)gj * n] = make_float2(hi, lo);
+        }
+}
+
+int batched_gemm_df64(int nwin, const int* n_w, const long long* off, int nmax, bool transA, int klim,
+                      const float2* A, const float2* B, float2* C, float* C32, cudaStream_t s) {
+    if (!nwin) return LRES_OK;
+    dim3 grid((nmax + 63) / 64, (nmax + 63) / 64, nwin);
+    if (!transA && klim == 1 && C)
+        gemm_df64_kernel<false, 1, false><<<grid, 256, 0, s>>>(n_w, off, A, B, C, nullptr);
+    else if (transA && klim == 2 && C32)
+        gemm_df64_kernel<true, 2, true><<<grid, 256, 0, s>>>(n_w, off, A, B, nullptr, C32);
+    else {
+        lres_set_error("unsupported double-float GEMM variant");
+        return LRES_EINVAL;
+    }
+    LRES_CUDA_TRY(cudaGetLastError());
+    return LRES_OK;
+}
+
 }  // namespace lres

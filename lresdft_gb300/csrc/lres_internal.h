@@ -86,6 +86,9 @@ int build_F(int nwin, const long long* Xp, const int* Xi, const double* Xv, cons
 int batched_gemm(int nwin, const int* n_w, const long long* offA, int nmax, bool transA, const double* A,
                  const double* B, double* C, cudaStream_t s, int klim = 0);
 int convert_f64_f32(const double* a, float* b, long long n, cudaStream_t s);
+int split_f64(const double* a, float2* b, long long n, cudaStream_t s);
+int batched_gemm_df64(int nwin, const int* n_w, const long long* off, int nmax, bool transA, int klim,
+                      const float2* A, const float2* B, float2* C, float* C32, cudaStream_t s);
 int pole_sums(int nwin, const long long* offQ, const int* m_w, const long long* Oflat, bool fp32,
               const void* q, long long qstride, int npoles, const double2* wq, const double2* wzq, double dV,
               double* dens, double* n_w, double* e_w, cudaStream_t s);

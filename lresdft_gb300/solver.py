@@ -80,7 +80,7 @@ class LResGPU:
     count and energies)."""
 
     def __init__(self, basis, cells, R_w=12.1, M=64, margin=0.3, nthreads=1, lag_mu=False, reuse_vectors=True,
-                 precision="fp64"):
+                 precision="fp64", tile_config=None):
         if M % 2:
             raise ValueError("M must be even")
         self.b, self.M, self.margin = basis, M, margin
@@ -124,6 +124,12 @@ class LResGPU:
         _lib.check(_lib.lib.lres_ctx_create(C.byref(ctx), C.byref(d), prec, M, None))
         self._ctx = ctx
         self._keep = (X, S, T)      # host arrays referenced by the descriptor during creation
+        # tile configuration of the pole kernel: an index, or "auto" to time all of them on
+        # the first Hamiltonian (see autotune); None keeps the library default
+        self.tile_config = tile_config
+        self._tuned = not (tile_config == "auto")
+        if isinstance(tile_config, int):
+            self.autotune(0.0, -1.0, config=tile_config)
         self._out = np.zeros(3)
         self.dens_buf = np.zeros(cr.ng)
 
@@ -341,6 +347,11 @@ class LResGPU:
         cr = self.b.cr
         N = cr.n_elec if N is None else N
         self.set_potential(v)
+        if not self._tuned:
+            # time the tile configurations once, on this Hamiltonian, at a mu near the gap
+            lm = self.min_eig(-1.0, 0.0, tol=1e-6)
+            self.tile_config, self.tune_ms = self.autotune(lm + 0.4, lm - 0.3)
+            self._tuned = True
         # count tolerances: the reference's 1e-8 N (lrft/lcao3d.py:412) for the FP64 path
         # and a root tolerance far below it; the complex64 path's counts carry ~1e-7 N of
         # FP32 noise, so both tolerances sit at that floor
