@@ -105,10 +105,12 @@ int lres_set_hamiltonian_csr(lres_ctx* ctx, const int64_t* Hp, const int64_t* Hi
  * and returns LRES_ENUMERIC (bit 1) or LRES_EINVAL (bit 2) when out[2] != 0. */
 int lres_pass(lres_ctx* ctx, double mu, double e_lo, double* dens, int dens_on_device, double* out, void* stream);
 
-/* Tile configuration of the fused pole kernel: force_config in [0, 3] selects one; -1
- * times every configuration with full passes at (mu, e_lo) on the current Hamiltonian
- * and keeps the fastest for this context.  *chosen (may be NULL) receives the choice,
- * ms_per_config[4] (may be NULL) the measured kernel times. */
+/* Tile configuration of the fused pole kernel: force_config in [0, 4] selects one
+ * (LRES_MIXED configuration 4 runs the chunk products on the tensor cores, tcgen05 with a
+ * 3xTF32 split; it is timed but kept only when forced, its error being ~5x that of the FP32
+ * configurations); -1 times every configuration with full passes at (mu, e_lo) on the
+ * current Hamiltonian and keeps the fastest eligible one for this context.  *chosen (may be NULL) receives the choice, ms_per_config[5]
+ * (may be NULL) the measured kernel times. */
 int lres_autotune(lres_ctx* ctx, double mu, double e_lo, int32_t force_config, int32_t* chosen,
                   double* ms_per_config, void* stream);
 

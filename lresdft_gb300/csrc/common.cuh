@@ -122,6 +122,7 @@ template <> struct El<float2> {
 enum : int {
     ST_ZERO_PIVOT = 1,      // a pivot was zero or not finite
     ST_BAD_SHAPE = 2,       // a work item exceeded the launch's size limits
+    ST_TIMEOUT = 4,         // a bounded wait on a tensor-core completion barrier ran out
 };
 
 }  // namespace lres

@@ -541,6 +541,308 @@ __global__ void __launch_bounds__(NT, 512 / NT) ldl_left_kernel(LdlParams<T> p) 
     }
 }
 
+// ---------------------------------------------------------------------------
+// Tensor-core variant of the left-looking kernel (complex FP32 path, tile configuration 4).
+//
+// The panel update of a 32-column chunk, tmp[r, c] = sum_k g[r, k] b[c, k] (complex), is a
+// real GEMM  [Re g | Im g] (128 x 64) . B' (64 x 64)  with B' built from the panel's G rows
+// ([b_re, -b_im ; b_im, b_re] per complex entry), run on the 5th-generation tensor cores:
+// operands in shared memory (K-major, no swizzle, 8 x 16-byte core matrices), accumulator
+// in tensor memory, tcgen05.mma issued by one thread, completion through an mbarrier.
+// FP32 accuracy from TF32 operands by the 3xTF32 split x = hi + lo (hi, lo rounded to
+// TF32): hi.hi + hi.lo + lo.hi, each chunk accumulated from zero in FP32 and subtracted
+// from the row's running value in registers (blocked summation, as the SIMT kernel).
+// 128 threads = 128 rows = 128 TMEM lanes; thread t reads its row with tcgen05.ld.
+// ---------------------------------------------------------------------------
+namespace tc {
+constexpr int M = 128, N = 64, KR = 64;             // real GEMM per chunk
+constexpr int LBO = 128;                             // bytes between core matrices along K
+constexpr int SBO = (KR / 4) * 128;                  // bytes between 8-row groups
+constexpr int A_BYTES = M * KR * 4, B_BYTES = N * KR * 4;
+__device__ __forceinline__ int off(int row, int k) { return (row >> 3) * SBO + (k >> 2) * LBO + (row & 7) * 16 + (k & 3) * 4; }
+__device__ __forceinline__ uint64_t desc(uint32_t saddr) {
+    return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)((LBO >> 4) & 0x3FFF) << 16) |
+           ((uint64_t)((SBO >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
+}
+constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+__device__ __forceinline__ float tf32(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+__device__ __forceinline__ void split(float x, float& hi, float& lo) {
+    hi = tf32(x);
+    lo = tf32(x - hi);
+}
+__device__ __forceinline__ void mma(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t accumulate) {
+    asm volatile("{ .reg .pred p; setp.ne.u32 p, %4, 0;\n"
+                 "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p; }"
+                 ::"r"(tmem), "l"(ad), "l"(bd), "r"(IDESC), "r"(accumulate));
+}
+__device__ __forceinline__ void ld64(uint32_t taddr, float* v) {
+    uint32_t r[64];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x64.b32 "
+                 "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                 "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,"
+                 "%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,"
+                 "%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%64];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+                   "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+                   "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]),
+                   "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]),
+                   "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]),
+                   "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]),
+                   "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < 64; ++j) v[j] = __uint_as_float(r[j]);
+}
+}  // namespace tc
+
+__global__ void __launch_bounds__(128, 1) ldl_left_tc_kernel(LdlParams<float2> p) {
+    using T = float2;
+    using E = El<T>;
+    constexpr int NB = 32, NT = 128;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    unsigned char* Ahi = smem_raw;
+    unsigned char* Alo = Ahi + tc::A_BYTES;
+    unsigned char* Bhi = Alo + tc::A_BYTES;
+    unsigned char* Blo = Bhi + tc::B_BYTES;
+    T* Dg = reinterpret_cast<T*>(Blo + tc::B_BYTES);   // [32][NB+1]
+    T* WL = Dg + 32 * (NB + 1);
+    T* Dsh = WL + NB * NB;
+    T* Dinv = Dsh + NB;
+    T* Dsq = Dinv + NB;
+    T* qsh = Dsq + NB;                                  // mmax
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_slot;
+    __shared__ int item_sh, bail_sh;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    T* G = p.ws + (size_t)blockIdx.x * p.ws_stride;
+    const uint32_t mbar_a = (uint32_t)__cvta_generic_to_shared(&mbar);
+    const uint32_t aH = (uint32_t)__cvta_generic_to_shared(Ahi), aL = (uint32_t)__cvta_generic_to_shared(Alo);
+    const uint32_t bH = (uint32_t)__cvta_generic_to_shared(Bhi), bL = (uint32_t)__cvta_generic_to_shared(Blo);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_a));
+        bail_sh = 0;
+    }
+    if (warp == 0) {
+        const uint32_t slot = (uint32_t)__cvta_generic_to_shared(&tmem_slot);
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" ::"r"(slot));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = tmem_slot;
+    const uint32_t my_taddr = tmem + ((uint32_t)(warp * 32) << 16);
+    uint32_t phase = 0;
+
+    for (;;) {
+        if (tid == 0) item_sh = atomicAdd(p.counter, 1);
+        __syncthreads();
+        const int it = item_sh;
+        if (it >= p.nitems || bail_sh) break;
+        const int w = p.items[it].x, k = p.items[it].y;
+        const int n = p.n_w[w];
+        const int m = p.F ? p.m_w[w] : 0;
+        const int np = (n + NB - 1) / NB * NB;
+        const int rows = np + m;
+        const long long ld = rows;
+        if (n > p.nmax || m > p.mmax) {
+            if (tid == 0) atomicOr(p.status, ST_BAD_SHAPE);
+            __syncthreads();
+            continue;
+        }
+        const T z = p.shifts[k];
+        const float* C = p.C ? p.C + p.offC[w] : nullptr;
+        const float* F = p.F ? p.F + p.offF[w] : nullptr;
+        for (int r = tid; r < m; r += NT) qsh[r] = E::zero();
+        __syncthreads();
+
+        for (int j0 = 0; j0 < np && !bail_sh; j0 += NB) {
+            const int na = rows - j0;
+            for (int b0 = 0; b0 < na; b0 += NT) {
+                const int ir = b0 + tid;
+                const int i = j0 + ir;
+                const bool active = ir < na;
+                T acc[NB];
+                if (active && i < n) {
+                    const float* cp = C + i + (long long)j0 * n;
+#pragma unroll
+                    for (int c = 0; c < NB; ++c) {
+                        const int col = j0 + c;
+                        acc[c] = (col <= i) ? E::shift_minus(z, (i == col ? 1.f : 0.f), cp[(long long)c * n]) : E::zero();
+                    }
+                } else if (active && i < np) {
+#pragma unroll
+                    for (int c = 0; c < NB; ++c) acc[c] = (j0 + c == i) ? E::from(1.f) : E::zero();
+                } else if (active) {
+                    const float* fp = F + (i - np) + (long long)j0 * m;
+#pragma unroll
+                    for (int c = 0; c < NB; ++c) acc[c] = (j0 + c < n) ? E::from(fp[(long long)c * m]) : E::zero();
+                } else {
+#pragma unroll
+                    for (int c = 0; c < NB; ++c) acc[c] = E::zero();
+                }
+                for (int k0 = 0; k0 < j0; k0 += 32) {
+                    // ---- stage B' (panel rows x chunk) and A (this thread's row x chunk), split hi/lo
+                    for (int idx = tid; idx < 32 * 32; idx += NT) {
+                        const int c = idx & 31, kk = idx >> 5;
+                        const T b = G[(j0 + c) + (long long)(k0 + kk) * ld];
+                        float rh, rl, ih, il;
+                        tc::split(b.x, rh, rl);
+                        tc::split(b.y, ih, il);
+                        // rows 2c (real part of the output) and 2c+1 (imaginary), K columns 2kk, 2kk+1
+                        *reinterpret_cast<float2*>(Bhi + tc::off(2 * c, 2 * kk)) = make_float2(rh, -ih);
+                        *reinterpret_cast<float2*>(Blo + tc::off(2 * c, 2 * kk)) = make_float2(rl, -il);
+                        *reinterpret_cast<float2*>(Bhi + tc::off(2 * c + 1, 2 * kk)) = make_float2(ih, rh);
+                        *reinterpret_cast<float2*>(Blo + tc::off(2 * c + 1, 2 * kk)) = make_float2(il, rl);
+                    }
+                    {
+                        const T* gi = G + i + (long long)k0 * ld;
+#pragma unroll 8
+                        for (int kk = 0; kk < 32; ++kk) {
+                            const T g = active ? gi[(long long)kk * ld] : E::zero();
+                            float rh, rl, ih, il;
+                            tc::split(g.x, rh, rl);
+                            tc::split(g.y, ih, il);
+                            *reinterpret_cast<float2*>(Ahi + tc::off(tid, 2 * kk)) = make_float2(rh, ih);
+                            *reinterpret_cast<float2*>(Alo + tc::off(tid, 2 * kk)) = make_float2(rl, il);
+                        }
+                    }
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    asm volatile("tcgen05.fence::before_thread_sync;");
+                    __syncthreads();
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    if (tid == 0) {
+                        // 3xTF32: hi.hi, hi.lo, lo.hi, 8 instructions (K = 8) each
+#pragma unroll
+                        for (int kb = 0; kb < tc::KR / 8; ++kb)
+                            tc::mma(tmem, tc::desc(aH + kb * 2 * tc::LBO), tc::desc(bH + kb * 2 * tc::LBO), kb > 0);
+#pragma unroll
+                        for (int kb = 0; kb < tc::KR / 8; ++kb)
+                            tc::mma(tmem, tc::desc(aH + kb * 2 * tc::LBO), tc::desc(bL + kb * 2 * tc::LBO), 1);
+#pragma unroll
+                        for (int kb = 0; kb < tc::KR / 8; ++kb)
+                            tc::mma(tmem, tc::desc(aL + kb * 2 * tc::LBO), tc::desc(bH + kb * 2 * tc::LBO), 1);
+                        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                                     ::"r"(mbar_a));
+                    }
+                    uint32_t done = 0;
+                    for (int spin = 0; spin < (1 << 24) && !done; ++spin)
+                        asm volatile("{ .reg .pred q; mbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\n"
+                                     "selp.u32 %0, 1, 0, q; }" : "=r"(done) : "r"(mbar_a), "r"(phase));
+                    phase ^= 1u;
+                    if (!done) {
+                        atomicOr(p.status, ST_TIMEOUT);
+                        atomicOr(&bail_sh, 1);
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    if (done) {
+                        float v[64];
+                        tc::ld64(my_taddr, v);
+#pragma unroll
+                        for (int c = 0; c < NB; ++c) acc[c] = E::sub(acc[c], make_float2(v[2 * c], v[2 * c + 1]));
+                    }
+                    asm volatile("tcgen05.fence::before_thread_sync;");
+                    __syncthreads();                  // tiles free for the next chunk
+                    if (bail_sh) break;
+                }
+                if (bail_sh) break;
+                if (b0 == 0) {
+                    if (tid < 32) {
+#pragma unroll
+                        for (int c = 0; c < NB; ++c) Dg[tid * (NB + 1) + c] = acc[c];
+                    }
+                    __syncthreads();
+                    if (tid < 32) {
+                        const int lane = tid;
+                        T* myrow = Dg + lane * (NB + 1);
+                        for (int kk = 0; kk < NB; ++kk) {
+                            __syncwarp();
+                            const T d = Dg[kk * (NB + 1) + kk];
+                            const T dinv = E::inv(d);
+                            const bool mine = lane > kk;
+                            T l = E::zero();
+                            if (mine) {
+                                l = E::mul(myrow[kk], dinv);
+                                myrow[kk] = l;
+                            }
+                            if (lane == kk) {
+                                Dsh[kk] = d;
+                                Dinv[kk] = dinv;
+                                Dsq[kk] = E::csqrt(d);
+                                const double m2 = (double)E::mag2(d);
+                                if (!(m2 > 0.0) || !isfinite(m2)) atomicOr(p.status, ST_ZERO_PIVOT);
+                            }
+                            __syncwarp();
+                            if (mine) {
+                                const T ldv = E::mul(l, d);
+                                for (int c = kk + 1; c <= lane; ++c)
+                                    myrow[c] = E::fms(ldv, Dg[c * (NB + 1) + kk], myrow[c]);
+                            }
+                        }
+                        __syncwarp();
+                        for (int kk = 0; kk < NB; ++kk)
+                            if (lane > kk) WL[kk * NB + lane] = E::mul(Dsh[kk], myrow[kk]);
+                    }
+                    __syncthreads();
+                    if (tid < 32) {
+#pragma unroll
+                        for (int c = 0; c < NB; ++c) acc[c] = Dg[tid * (NB + 1) + c];
+                    }
+                }
+                if (active && ir >= NB) {
+#pragma unroll
+                    for (int kk = 0; kk < NB; ++kk) {
+                        const T l = E::mul(acc[kk], Dinv[kk]);
+#pragma unroll
+                        for (int kk2 = kk + 1; kk2 < NB; ++kk2) acc[kk2] = E::fms(l, WL[kk * NB + kk2], acc[kk2]);
+                        acc[kk] = l;
+                    }
+                    if (i >= np) {
+                        T qv = qsh[i - np];
+#pragma unroll
+                        for (int kk = 0; kk < NB; ++kk) qv = E::fma(E::mul(acc[kk], acc[kk]), Dsh[kk], qv);
+                        qsh[i - np] = qv;
+                    }
+                    if (j0 + NB < np) {
+                        T* gout = G + i + (long long)j0 * ld;
+#pragma unroll
+                        for (int kk = 0; kk < NB; ++kk) gout[(long long)kk * ld] = E::mul(acc[kk], Dsq[kk]);
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        if (p.q && !bail_sh) {
+            T* qo = p.q + (long long)k * p.qstride + p.offQ[w];
+            for (int r = tid; r < m; r += NT) qo[r] = qsh[r];
+        }
+        __syncthreads();
+    }
+    // release the tensor memory (the MMA of every chunk was waited for above)
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem));
+}
+
+static int launch_left_tc(const LdlParams<float2>& p, int grid, cudaStream_t s) {
+    const size_t smem = 2 * (size_t)tc::A_BYTES + 2 * (size_t)tc::B_BYTES +
+                        sizeof(float2) * ((size_t)32 * 33 + 32 * 32 + 3 * 32 + p.mmax);
+    LRES_CUDA_TRY(cudaFuncSetAttribute(ldl_left_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int dev = 0, nsm = 0;
+    LRES_CUDA_TRY(cudaGetDevice(&dev));
+    LRES_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    grid = std::min(grid, nsm);                         // one CTA (one TMEM allocation) per SM
+    ldl_left_tc_kernel<<<grid, 128, smem, s>>>(p);
+    LRES_CUDA_TRY(cudaGetLastError());
+    return LRES_OK;
+}
+
 template <class T, int NB, int NT, int KC>
 static int launch_left(const LdlParams<T>& p, int grid, cudaStream_t s) {
     const size_t smem = sizeof(T) * ((size_t)2 * KC * NB + 32 * (NB + 1) + NB * NB + 3 * NB + p.mmax + (size_t)NB * NT);
@@ -613,6 +915,7 @@ int run_ldl(const LdlJob& j, cudaStream_t s) {
             case 1: return launch_left<double2, 16, 128, 32>(p, j.grid, s);
             case 2: return launch_left<double2, 16, 256, 16>(p, j.grid, s);
             case 3: return launch_left<double2, 8, 256, 32>(p, j.grid, s);
+            case 4: return launch_left<double2, 8, 128, 32>(p, j.grid, s);
             default: return launch_left<double2, 16, 256, 32>(p, j.grid, s);
         }
     } else if (j.kind == LdlJob::C64) {
@@ -627,6 +930,7 @@ int run_ldl(const LdlJob& j, cudaStream_t s) {
             case 1: return launch_left<float2, 32, 128, 32>(p, j.grid, s);
             case 2: return launch_left<float2, 32, 256, 16>(p, j.grid, s);
             case 3: return launch_left<float2, 16, 256, 32>(p, j.grid, s);
+            case 4: return launch_left_tc(p, j.grid, s);
             default: return launch_left<float2, 32, 256, 32>(p, j.grid, s);
         }
     } else {

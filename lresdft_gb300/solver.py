@@ -180,10 +180,10 @@ class LResGPU:
         return (dens.copy() if want_density else None), float(self._out[0]), float(self._out[1])
 
     def autotune(self, mu, e_lo, config=-1):
-        """Pick the tile configuration of the pole kernel (-1: time all four with full
+        """Pick the tile configuration of the pole kernel (-1: time all five with full
         passes at (mu, e_lo) and keep the fastest).  Returns (chosen, ms per config)."""
         chosen = C.c_int32()
-        ms = np.full(4, -1.0)
+        ms = np.full(5, -1.0)
         _lib.check(_lib.lib.lres_autotune(self._ctx, float(mu), float(e_lo), int(config), C.byref(chosen),
                                           _lib.ptrd(ms), None))
         return int(chosen.value), ms

@@ -157,3 +157,23 @@ def test_scf_energy_matches_reference(systems, name):
         assert r["converged"]
         assert abs(r["energy"] - g["scf_energy"]) / cr.n_elec < gate, (precision, r["energy"], g["scf_energy"])
         s.close()
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("config", [0, 1, 2, 3, 4])
+def test_every_tile_configuration_matches_reference(systems, name, config):
+    """Each compiled tile configuration of the pole kernel, forced: FP64 to 1e-10 in
+    density, mixed within the 2e-7 Ha/electron gate (configuration 4 of the mixed path runs
+    the chunk products on the tensor cores with a 3xTF32 split)."""
+    g, cr, b = systems[name]
+    v = g["v"].reshape(cr.shape)
+    for precision in ("fp64", "mixed"):
+        s = _solver(b, cr, g, precision)
+        s.autotune(0.0, -1.0, config=config)
+        s.set_potential(v)
+        dens, N, eb = s.pole_pass(float(g["cold_mu"]), float(g["cold_elo"]))
+        if precision == "fp64":
+            assert np.max(np.abs(dens - g["cold_dens"])) < 1e-10 and abs(eb - g["cold_eband"]) < 1e-9
+        else:
+            assert abs(eb - g["cold_eband"]) / cr.n_elec < 2e-7
+        s.close()
