@@ -115,7 +115,8 @@ def run_ours(args):
     if args.cells != 8:
         WORKLOAD.update(workload=f"{args.cells}^3 H2 crystal (profiling size), {cr.n_elec} electrons",
                         natoms=len(cr.pos), nwin=len(cr.pos), basis_functions=6 * len(cr.pos), grid=f"{cr.shape[0]}^3")
-    s = LResGPU(b, cr.pos, R_w=8.0, M=64, precision=args.precision, tile_config="auto")
+    s = LResGPU(b, cr.pos, R_w=8.0, M=64, precision=args.precision,
+                tile_config="auto" if args.tile_config is None else args.tile_config)
     go = GridOps(s)
     vion = go.ion_potential()
     d0 = np.full(cr.shape, cr.n_elec / (cr.ng * cr.dV))
@@ -225,7 +226,8 @@ def run_ours(args):
                          "gather": round(float(np.mean(gather_ms)), 3),
                          "transform": round(float(np.mean(transform_ms)), 3)},
         "setup_s": round(setup_s, 2), "accuracy": err,
-        "tile_config": {"chosen": s.tile_config, "pole_kernel_ms_per_config": [round(float(x), 2) for x in s.tune_ms]},
+        "tile_config": {"chosen": s.tile_config,
+                        "pole_kernel_ms_per_config": [round(float(x), 2) for x in getattr(s, "tune_ms", [])]},
     }
 
     # FP64 path on the same potential (the target ratio is mixed vs FP64)
@@ -344,6 +346,7 @@ def main():
                     help="skip the FP64 SCF window (about a minute at 1024 electrons)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cells", type=int, default=8, help="crystal of cells^3 H2 (8 = the benchmark workload)")
+    ap.add_argument("--tile-config", type=int, default=None, help="force a pole-kernel tile configuration")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
