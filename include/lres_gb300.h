@@ -105,12 +105,24 @@ int lres_set_hamiltonian_csr(lres_ctx* ctx, const int64_t* Hp, const int64_t* Hi
  * and returns LRES_ENUMERIC (bit 1) or LRES_EINVAL (bit 2) when out[2] != 0. */
 int lres_pass(lres_ctx* ctx, double mu, double e_lo, double* dens, int dens_on_device, double* out, void* stream);
 
-/* Tile configuration of the fused pole kernel: force_config in [0, 4] selects one
+/* The pass of lres_pass without any host synchronisation or host memory: pole nodes and
+ * weights are computed on the device, d_out[0..1] (device) receives N(mu) and E_band, the
+ * density stays in the context (lres_density_ptr).  Enqueues kernels and memsets only, so
+ * lres_set_potential(v on device) + lres_pass_async can be captured in a CUDA graph and
+ * replayed (after one ordinary call has set the kernel attributes).  Check the kernel
+ * status afterwards with lres_status. */
+int lres_pass_async(lres_ctx* ctx, double mu, double e_lo, double* d_out, void* stream);
+/* Status bits of the most recent pass (see lres_pass out[2]); synchronises the stream. */
+int lres_status(lres_ctx* ctx, int32_t* status, void* stream);
+/* Device address of the context's density array (ng doubles, valid until destroy). */
+int lres_density_ptr(lres_ctx* ctx, const double** d_dens);
+
+/* Tile configuration of the fused pole kernel: force_config in [0, 5] selects one
  * (LRES_MIXED configuration 4 runs the chunk products on the tensor cores, tcgen05 with a
  * 3xTF32 split; it is timed but kept only when forced, its error being ~5x that of the FP32
  * configurations); -1 times every configuration with full passes at (mu, e_lo) on the
- * current Hamiltonian and keeps the fastest eligible one for this context.  *chosen (may be NULL) receives the choice, ms_per_config[5]
- * (may be NULL) the measured kernel times. */
+ * current Hamiltonian and keeps the fastest eligible one for this context.  *chosen (may be
+ * NULL) receives the choice, ms_per_config[6] (may be NULL) the measured kernel times. */
 int lres_autotune(lres_ctx* ctx, double mu, double e_lo, int32_t force_config, int32_t* chosen,
                   double* ms_per_config, void* stream);
 

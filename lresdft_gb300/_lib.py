@@ -17,7 +17,7 @@ LRES_FP64, LRES_MIXED = 0, 1
 ERRORS = {-22: "EINVAL", -12: "ENOMEM", -5: "ECUDA", -33: "ENUMERIC", -71: "ESTATE"}
 
 EXPORTS = ("lres_version", "lres_last_error", "lres_ctx_create", "lres_ctx_destroy", "lres_set_potential",
-           "lres_set_hamiltonian_csr", "lres_pass", "lres_autotune", "lres_timings", "lres_window_sums", "lres_inertia", "lres_min_eig",
+           "lres_set_hamiltonian_csr", "lres_pass", "lres_pass_async", "lres_status", "lres_density_ptr", "lres_autotune", "lres_timings", "lres_window_sums", "lres_inertia", "lres_min_eig",
            "lres_voronoi_owner", "lres_lda_xc", "lres_hartree", "lres_ion_potential", "lres_inertia_noalloc")
 
 
@@ -59,6 +59,9 @@ def _load():
         "lres_set_potential": (i32, [vp, vp, i32, vp]),
         "lres_set_hamiltonian_csr": (i32, [vp, P64, P64, PD, vp]),
         "lres_pass": (i32, [vp, dbl, dbl, vp, i32, PD, vp]),
+        "lres_pass_async": (i32, [vp, dbl, dbl, vp, vp]),
+        "lres_status": (i32, [vp, C.POINTER(C.c_int32), vp]),
+        "lres_density_ptr": (i32, [vp, C.POINTER(C.c_void_p)]),
         "lres_autotune": (i32, [vp, dbl, dbl, C.c_int32, C.POINTER(C.c_int32), PD, vp]),
         "lres_timings": (i32, [vp, PD, i32]),
         "lres_window_sums": (i32, [vp, PD, PD]),

@@ -150,9 +150,10 @@ int ldl_launch(lres_ctx* c, LdlJob::Kind kind, int nitems, const int2* items, co
     j.mmax = mmax;
     const size_t el = kind == LdlJob::C128 ? 16 : 8;
     const int slots = kind == LdlJob::R64 ? c->nsm : 4 * c->nsm;   // complex: up to 4 CTAs per SM
-    j.ws_stride = (long long)(c->ws_bytes / el / slots);
+    // slots start 16-byte aligned (bulk copies), and hold (n_pad + m + 1) x n_pad complex
+    j.ws_stride = (long long)(c->ws_bytes / el / slots) / 16 * 16;
     const long long nmaxp = (c->nmax + 31) / 32 * 32;   // padded window dimension (complex kernel)
-    const long long need = kind == LdlJob::R64 ? (long long)ldp * c->nmax : (nmaxp + mmax) * nmaxp;
+    const long long need = kind == LdlJob::R64 ? (long long)ldp * c->nmax : (nmaxp + mmax + 1) * nmaxp;
     if (need > j.ws_stride) {
         lres_set_error("workspace too small");
         return LRES_EINVAL;
@@ -178,6 +179,34 @@ __global__ void identity_kernel(const int* n_w, const long long* off, double* I,
     for (int i = threadIdx.x; i < n; i += blockDim.x) D[i + (long long)i * n] = 1.0;
 }
 
+// Pole nodes and weights on the device (a capturable pass takes mu, e_lo by value):
+// z_k = c + R e^{i pi (2k+1)/M}, w_k = R e^{i pi (2k+1)/M} / M  (lrft/core.py:130-139)
+__global__ void poles_kernel(int P, int M, double mu, double e_lo, int fp32, void* shifts, double2* wq, double2* wzq) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= P) return;
+    const double cc = 0.5 * (mu + e_lo), R = 0.5 * (mu - e_lo);
+    double sn, cs;
+    sincospi((double)(2 * k + 1) / (double)M, &sn, &cs);
+    const double zr = cc + R * cs, zi = R * sn;
+    const double wr = R * cs / M, wi = R * sn / M;
+    if (fp32) reinterpret_cast<float2*>(shifts)[k] = make_float2((float)zr, (float)zi);
+    else reinterpret_cast<double2*>(shifts)[k] = make_double2(zr, zi);
+    wq[k] = make_double2(wr, wi);
+    wzq[k] = make_double2(wr * zr - wi * zi, wr * zi + wi * zr);
+}
+
+// N and E_band from the per-window sums, fixed order (one thread).
+__global__ void window_total_kernel(int nwin, const double* nw, const double* ew, double* out) {
+    if (blockIdx.x || threadIdx.x) return;
+    double N = 0.0, E = 0.0;
+    for (int w = 0; w < nwin; ++w) {
+        N += nw[w];
+        E += ew[w];
+    }
+    out[0] = N;
+    out[1] = E;
+}
+
 int window_transform(lres_ctx* c, cudaStream_t s) {
     // H^_W = L^-1 H_W L^-T with LinvT = L^-T (upper triangular) stored column-major:
     // Y = H LinvT (k <= column), then the lower triangle of H^ = LinvT^T Y (k <= row),
@@ -191,6 +220,10 @@ int window_transform(lres_ctx* c, cudaStream_t s) {
 }
 
 int mark(lres_ctx* c, int which, int end, cudaStream_t s) {
+    // a stream being captured into a graph records no timing events
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    LRES_CUDA_TRY(cudaStreamIsCapturing(s, &cs));
+    if (cs != cudaStreamCaptureStatusNone) return LRES_OK;
     LRES_CUDA_TRY(cudaEventRecord(c->ev[2 * which + end], s));
     c->ev_used[which] = true;
     return LRES_OK;
@@ -569,7 +602,7 @@ extern "C" int lres_ctx_create(lres_ctx** out, const lres_system_desc* d, int pr
     // workspace: one slot per SM, large enough for (n + n) x n real or (n + m) x n complex
     const long long nmaxp = (c->nmax + 31) / 32 * 32;
     const long long ldmax = std::max<long long>(c->nmax + c->mmax, 2LL * c->nmax);
-    const size_t slot = std::max<size_t>((size_t)ldmax * c->nmax, (size_t)(nmaxp + c->mmax) * nmaxp) * 16;
+    const size_t slot = (std::max<size_t>((size_t)ldmax * c->nmax, (size_t)(nmaxp + c->mmax + 1) * nmaxp) + 16) * 16;
     c->ws_bytes = slot * 4 * c->nsm;
     TRY(dalloc((char**)&c->d_ws, c->ws_bytes));
 
@@ -694,23 +727,10 @@ extern "C" int lres_pass(lres_ctx* c, double mu, double e_lo, double* dens, int 
     }
     cudaStream_t s = (cudaStream_t)stream;
     const int P = c->npoles;
-    const double cc = 0.5 * (mu + e_lo), R = 0.5 * (mu - e_lo);
-    std::vector<double2> wq(P), wzq(P), z64(P);
-    std::vector<float2> z32(P);
-    for (int k = 0; k < P; ++k) {
-        // zeta_k = exp(i pi (2k+1)/M), z_k = c + R zeta_k, w_k = R zeta_k / M  (lrft/core.py:130-139)
-        const std::complex<double> zeta = std::exp(std::complex<double>(0.0, M_PI * (2 * k + 1) / c->M));
-        const std::complex<double> z = cc + R * zeta, w = R * zeta / (double)c->M, wz = w * z;
-        z64[k] = make_double2(z.real(), z.imag());
-        z32[k] = make_float2((float)z.real(), (float)z.imag());
-        wq[k] = make_double2(w.real(), w.imag());
-        wzq[k] = make_double2(wz.real(), wz.imag());
-    }
     const bool mixed = c->precision == LRES_MIXED;
-    if (mixed) LRES_CUDA_TRY(cudaMemcpyAsync(c->d_shifts, z32.data(), sizeof(float2) * P, cudaMemcpyHostToDevice, s));
-    else LRES_CUDA_TRY(cudaMemcpyAsync(c->d_shifts, z64.data(), sizeof(double2) * P, cudaMemcpyHostToDevice, s));
-    LRES_CUDA_TRY(cudaMemcpyAsync(c->d_wq, wq.data(), sizeof(double2) * P, cudaMemcpyHostToDevice, s));
-    LRES_CUDA_TRY(cudaMemcpyAsync(c->d_wzq, wzq.data(), sizeof(double2) * P, cudaMemcpyHostToDevice, s));
+    // nodes and weights on the device, the same kernel as the capturable pass (bitwise equal results)
+    poles_kernel<<<(P + 63) / 64, 64, 0, s>>>(P, c->M, mu, e_lo, mixed ? 1 : 0, c->d_shifts, c->d_wq, c->d_wzq);
+    LRES_CUDA_TRY(cudaGetLastError());
     LRES_CUDA_TRY(cudaMemsetAsync(c->d_status, 0, sizeof(int), s));
     LRES_CUDA_TRY(cudaMemsetAsync(c->d_counter, 0, sizeof(int), s));
     TRY(mark(c, 0, 0, s));
@@ -806,6 +826,58 @@ extern "C" int lres_timings(lres_ctx* c, double* ms, int n) {
         ms[i] = t;
     }
     for (int i = 6; i < n; ++i) ms[i] = -1.0;
+    return LRES_OK;
+}
+
+extern "C" int lres_pass_async(lres_ctx* c, double mu, double e_lo, double* d_out, void* stream) {
+    if (!c || !d_out) {
+        lres_set_error("null argument");
+        return LRES_EINVAL;
+    }
+    if (!c->have_h) {
+        lres_set_error("lres_pass_async before a Hamiltonian was set");
+        return LRES_ESTATE;
+    }
+    if (!(mu > e_lo) || !std::isfinite(mu) || !std::isfinite(e_lo)) {
+        lres_set_error("need finite e_lo < mu (got mu=%g, e_lo=%g)", mu, e_lo);
+        return LRES_EINVAL;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    const bool mixed = c->precision == LRES_MIXED;
+    const int P = c->npoles;
+    poles_kernel<<<(P + 63) / 64, 64, 0, s>>>(P, c->M, mu, e_lo, mixed ? 1 : 0, c->d_shifts, c->d_wq, c->d_wzq);
+    LRES_CUDA_TRY(cudaGetLastError());
+    LRES_CUDA_TRY(cudaMemsetAsync(c->d_status, 0, sizeof(int), s));
+    if (mixed)
+        TRY(ldl_launch(c, LdlJob::C64, c->nitems, c->d_items, c->d_Hhat32, nullptr, c->d_Fhat32, c->d_m, c->d_offF,
+                       c->d_shifts, c->d_q, nullptr, c->nmax + c->mmax, c->mmax, s));
+    else
+        TRY(ldl_launch(c, LdlJob::C128, c->nitems, c->d_items, c->d_HW, c->d_SW, c->d_F, c->d_m, c->d_offF,
+                       c->d_shifts, c->d_q, nullptr, c->nmax + c->mmax, c->mmax, s));
+    TRY(pole_sums(c->nwin, c->d_offQ, c->d_m, c->d_Oflat, mixed, c->d_q, c->npts, P, c->d_wq, c->d_wzq, c->dV,
+                  c->d_dens, c->d_nw, c->d_ew, s));
+    window_total_kernel<<<1, 1, 0, s>>>(c->nwin, c->d_nw, c->d_ew, d_out);
+    LRES_CUDA_TRY(cudaGetLastError());
+    return LRES_OK;
+}
+
+extern "C" int lres_status(lres_ctx* c, int32_t* status, void* stream) {
+    if (!c || !status) {
+        lres_set_error("null argument");
+        return LRES_EINVAL;
+    }
+    int st = 0;
+    TRY(read_status(c, (cudaStream_t)stream, &st));
+    *status = st;
+    return LRES_OK;
+}
+
+extern "C" int lres_density_ptr(lres_ctx* c, const double** d_dens) {
+    if (!c || !d_dens) {
+        lres_set_error("null argument");
+        return LRES_EINVAL;
+    }
+    *d_dens = c->d_dens;
     return LRES_OK;
 }
 

@@ -39,7 +39,8 @@ struct LdlJob {
 //   0: NB 32 (c64) / 16 (c128), 256 threads, k-chunk 32     1: 128 threads
 //   2: k-chunk 16                                           3: NB 16 (c64) / 8 (c128)
 //   4: c64: chunk products on the tensor cores (tcgen05, 3xTF32); c128: NB 8, 128 threads
-constexpr int kLeftConfigs = 5;
+//   5: operands of every chunk brought in by bulk asynchronous copies, 128 threads
+constexpr int kLeftConfigs = 6;
 
 int run_ldl(const LdlJob& j, cudaStream_t s);
 size_t ldl_smem_bytes(int elem_bytes, int nb, int ldp, int mmax);

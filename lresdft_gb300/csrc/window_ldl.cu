@@ -72,6 +72,32 @@ struct LdlParams {
     int nmax, mmax;
 };
 
+// Dynamic shared memory attribute and occupancy of a kernel, set/queried only when the
+// request grows, so that launches enqueued during CUDA-graph capture issue no attribute
+// calls (the first, eager launch of each instantiation does).
+template <auto Kern>
+static int prepare_kernel(int threads, size_t smem, int* per_sm) {
+    static size_t set_smem = 0;          // one cache per kernel instantiation
+    static int cached_per_sm = 0;
+    if (smem > set_smem) {
+        LRES_CUDA_TRY(cudaFuncSetAttribute(Kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        LRES_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cached_per_sm, Kern, threads, smem));
+        set_smem = smem;
+    }
+    *per_sm = cached_per_sm;
+    return LRES_OK;
+}
+
+static int device_sms() {
+    static int nsm = 0;
+    if (!nsm) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    }
+    return nsm;
+}
+
 template <class T, int NB, int TR, int TC, int NT>
 __global__ void __launch_bounds__(NT) ldl_aug_kernel(LdlParams<T> p) {
     using E = El<T>;
@@ -830,14 +856,267 @@ __global__ void __launch_bounds__(128, 1) ldl_left_tc_kernel(LdlParams<float2> p
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem));
 }
 
+// ---------------------------------------------------------------------------
+// Bulk-copy variant of the left-looking kernel (tile configuration 5).  The row operand
+// (128 rows x KC columns of G) and the panel operand (NB rows x KC columns) of every chunk
+// are brought into shared memory by the bulk-copy engine (cp.async.bulk, one contiguous
+// copy per column, completion counted in bytes on an mbarrier), double-buffered, so that
+// many kilobytes are in flight per CTA instead of two loads per thread.  The accumulators
+// stay in registers (blocked: each chunk is summed from zero and subtracted).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void mbar_init(uint32_t a, int count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect(uint32_t a, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
+    asm volatile("cp.async.bulk.shared::cta.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(dst), "l"(src), "r"(bytes), "r"(mbar) : "memory");
+}
+// bounded wait; returns false if the phase did not complete
+__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t phase) {
+    uint32_t done = 0;
+    for (int spin = 0; spin < (1 << 24) && !done; ++spin)
+        asm volatile("{ .reg .pred q; mbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\n"
+                     "selp.u32 %0, 1, 0, q; }" : "=r"(done) : "r"(a), "r"(phase) : "memory");
+    return done != 0;
+}
+
+template <class T, int NB, int KC>
+__global__ void __launch_bounds__(128, 2) ldl_left_bulk_kernel(LdlParams<T> p) {
+    using E = El<T>;
+    using R = typename E::R;
+    constexpr int NT = 128;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    T* As = reinterpret_cast<T*>(smem_raw);          // [2][KC][NT]: As[kk*NT + r] = G[i0 + r, k0 + kk]
+    T* Bs = As + 2 * KC * NT;                        // [2][KC][NB]: Bs[kk*NB + c] = G[j0 + c, k0 + kk]
+    T* Dg = Bs + 2 * KC * NB;                        // [32][NB+1]
+    T* WL = Dg + 32 * (NB + 1);
+    T* Dsh = WL + NB * NB;
+    T* Dinv = Dsh + NB;
+    T* Dsq = Dinv + NB;
+    T* qsh = Dsq + NB;                               // mmax
+    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ int item_sh, bail_sh;
+    const int tid = threadIdx.x;
+    T* G = p.ws + (size_t)blockIdx.x * p.ws_stride;
+    const uint32_t mb0 = (uint32_t)__cvta_generic_to_shared(&mbar[0]);
+    const uint32_t mb1 = (uint32_t)__cvta_generic_to_shared(&mbar[1]);
+    if (tid == 0) {
+        mbar_init(mb0, 1);
+        mbar_init(mb1, 1);
+        bail_sh = 0;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    uint32_t ph0 = 0, ph1 = 0;
+
+    for (;;) {
+        if (tid == 0) item_sh = atomicAdd(p.counter, 1);
+        __syncthreads();
+        const int it = item_sh;
+        if (it >= p.nitems || bail_sh) break;
+        const int w = p.items[it].x, k = p.items[it].y;
+        const int n = p.n_w[w];
+        const int m = p.F ? p.m_w[w] : 0;
+        const int np = (n + NB - 1) / NB * NB;
+        const int rows = np + m;
+        const long long ld = rows + (rows & 1);          // even: 16-byte aligned columns
+        if (n > p.nmax || m > p.mmax) {
+            if (tid == 0) atomicOr(p.status, ST_BAD_SHAPE);
+            __syncthreads();
+            continue;
+        }
+        const T z = p.shifts[k];
+        const R* C = p.C ? p.C + p.offC[w] : nullptr;
+        const R* B = p.B ? p.B + p.offC[w] : nullptr;
+        const R* F = p.F ? p.F + p.offF[w] : nullptr;
+        for (int r = tid; r < m; r += NT) qsh[r] = E::zero();
+        __syncthreads();
+
+        for (int j0 = 0; j0 < np && !bail_sh; j0 += NB) {
+            const int na = rows - j0;
+            for (int b0 = 0; b0 < na; b0 += NT) {
+                const int ir = b0 + tid;
+                const int i = j0 + ir;
+                const int i0 = j0 + b0;                   // first row of the batch (even)
+                const bool active = ir < na;
+                const int nrow = min(NT, na - b0);
+                const uint32_t abytes = (uint32_t)(((nrow + 1) & ~1) * sizeof(T));
+                T acc[NB];
+                if (active && i < n) {
+                    const R* cp = C ? C + i + (long long)j0 * n : nullptr;
+                    const R* bp = B ? B + i + (long long)j0 * n : nullptr;
+#pragma unroll
+                    for (int c = 0; c < NB; ++c) {
+                        const int col = j0 + c;
+                        T a = E::zero();
+                        if (col <= i) {
+                            const R bb = bp ? bp[(long long)c * n] : (i == col ? R(1) : R(0));
+                            const R cc = cp ? cp[(long long)c * n] : R(0);
+                            a = E::shift_minus(z, bb, cc);
+                        }
+                        acc[c] = a;
+                    }
+                } else if (active && i < np) {
+#pragma unroll
+                    for (int c = 0; c < NB; ++c) acc[c] = (j0 + c == i) ? E::from(R(1)) : E::zero();
+                } else if (active) {
+                    const R* fp = F + (i - np) + (long long)j0 * m;
+#pragma unroll
+                    for (int c = 0; c < NB; ++c) acc[c] = (j0 + c < n) ? E::from(fp[(long long)c * m]) : E::zero();
+                } else {
+#pragma unroll
+                    for (int c = 0; c < NB; ++c) acc[c] = E::zero();
+                }
+                const int nch = (j0 + KC - 1) / KC;
+                // issue chunk ci into buffer ci & 1 (one thread; one copy per column)
+                auto issue = [&](int ci) {
+                    const int k0 = ci * KC, kc = min(KC, j0 - k0);
+                    const int buf = ci & 1;
+                    const uint32_t mb = buf ? mb1 : mb0;
+                    T* a_dst = As + buf * KC * NT;
+                    T* b_dst = Bs + buf * KC * NB;
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    mbar_expect(mb, (uint32_t)kc * (abytes + NB * sizeof(T)));
+                    for (int kk = 0; kk < kc; ++kk) {
+                        const T* col = G + (long long)(k0 + kk) * ld;
+                        bulk_g2s((uint32_t)__cvta_generic_to_shared(a_dst + kk * NT), col + i0, abytes, mb);
+                        bulk_g2s((uint32_t)__cvta_generic_to_shared(b_dst + kk * NB), col + j0,
+                                 NB * (uint32_t)sizeof(T), mb);
+                    }
+                };
+                if (nch > 0) {
+                    __syncthreads();                      // buffers free (previous users done)
+                    if (tid == 0) issue(0);
+                }
+                for (int ci = 0; ci < nch; ++ci) {
+                    const int k0 = ci * KC, kc = min(KC, j0 - k0);
+                    if (tid == 0 && ci + 1 < nch) issue(ci + 1);
+                    const int buf = ci & 1;
+                    const bool ok = mbar_wait(buf ? mb1 : mb0, buf ? ph1 : ph0);
+                    if (buf) ph1 ^= 1u; else ph0 ^= 1u;
+                    if (!ok) {
+                        atomicOr(p.status, ST_TIMEOUT);
+                        atomicOr(&bail_sh, 1);
+                    }
+                    if (active && ok) {
+                        const T* a = As + buf * KC * NT + tid;
+                        const T* bb = Bs + buf * KC * NB;
+                        T tmp[NB];
+#pragma unroll
+                        for (int c = 0; c < NB; ++c) tmp[c] = E::zero();
+                        for (int kk = 0; kk < kc; kk += 2) {
+                            const T g0 = a[kk * NT], g1 = a[(kk + 1) * NT];
+                            const T* b = bb + kk * NB;
+#pragma unroll
+                            for (int c = 0; c < NB; ++c) {
+                                T t = tmp[c];
+                                t = E::fma(g0, b[c], t);
+                                t = E::fma(g1, b[NB + c], t);
+                                tmp[c] = t;
+                            }
+                        }
+#pragma unroll
+                        for (int c = 0; c < NB; ++c) acc[c] = E::sub(acc[c], tmp[c]);
+                    }
+                    __syncthreads();                      // buffer ci & 1 consumed by everyone
+                    if (bail_sh) break;
+                }
+                if (bail_sh) break;
+                if (b0 == 0) {
+                    if (tid < 32) {
+#pragma unroll
+                        for (int c = 0; c < NB; ++c) Dg[tid * (NB + 1) + c] = acc[c];
+                    }
+                    __syncthreads();
+                    if (tid < 32) {
+                        const int lane = tid;
+                        T* myrow = Dg + lane * (NB + 1);
+                        for (int kk = 0; kk < NB; ++kk) {
+                            __syncwarp();
+                            const T d = Dg[kk * (NB + 1) + kk];
+                            const T dinv = E::inv(d);
+                            const bool mine = lane > kk && lane < NB;
+                            T l = E::zero();
+                            if (mine) {
+                                l = E::mul(myrow[kk], dinv);
+                                myrow[kk] = l;
+                            }
+                            if (lane == kk) {
+                                Dsh[kk] = d;
+                                Dinv[kk] = dinv;
+                                Dsq[kk] = E::csqrt(d);
+                                const double m2 = (double)E::mag2(d);
+                                if (!(m2 > 0.0) || !isfinite(m2)) atomicOr(p.status, ST_ZERO_PIVOT);
+                            }
+                            __syncwarp();
+                            if (mine) {
+                                const T ldv = E::mul(l, d);
+                                for (int c = kk + 1; c <= lane; ++c)
+                                    myrow[c] = E::fms(ldv, Dg[c * (NB + 1) + kk], myrow[c]);
+                            }
+                        }
+                        __syncwarp();
+                        for (int kk = 0; kk < NB; ++kk)
+                            if (lane > kk && lane < NB) WL[kk * NB + lane] = E::mul(Dsh[kk], myrow[kk]);
+                    }
+                    __syncthreads();
+                    if (tid < 32) {
+#pragma unroll
+                        for (int c = 0; c < NB; ++c) acc[c] = Dg[tid * (NB + 1) + c];
+                    }
+                }
+                if (active && ir >= NB) {
+#pragma unroll
+                    for (int kk = 0; kk < NB; ++kk) {
+                        const T l = E::mul(acc[kk], Dinv[kk]);
+#pragma unroll
+                        for (int kk2 = kk + 1; kk2 < NB; ++kk2) acc[kk2] = E::fms(l, WL[kk * NB + kk2], acc[kk2]);
+                        acc[kk] = l;
+                    }
+                    if (i >= np) {
+                        T qv = qsh[i - np];
+#pragma unroll
+                        for (int kk = 0; kk < NB; ++kk) qv = E::fma(E::mul(acc[kk], acc[kk]), Dsh[kk], qv);
+                        qsh[i - np] = qv;
+                    }
+                    if (j0 + NB < np) {
+                        T* gout = G + i + (long long)j0 * ld;
+#pragma unroll
+                        for (int kk = 0; kk < NB; ++kk) gout[(long long)kk * ld] = E::mul(acc[kk], Dsq[kk]);
+                    }
+                }
+            }
+            __syncthreads();                              // G columns of this panel complete
+        }
+        if (p.q && !bail_sh) {
+            T* qo = p.q + (long long)k * p.qstride + p.offQ[w];
+            for (int r = tid; r < m; r += NT) qo[r] = qsh[r];
+        }
+        __syncthreads();
+    }
+}
+
+template <class T, int NB, int KC>
+static int launch_left_bulk(const LdlParams<T>& p, int grid, cudaStream_t s) {
+    const size_t smem = sizeof(T) * ((size_t)2 * KC * 128 + 2 * KC * NB + 32 * (NB + 1) + NB * NB + 3 * NB + p.mmax);
+    auto kern = ldl_left_bulk_kernel<T, NB, KC>;
+    int per_sm = 0;
+    if (int rc = prepare_kernel<ldl_left_bulk_kernel<T, NB, KC>>(128, smem, &per_sm)) return rc;
+    grid = std::min(grid, std::max(1, per_sm) * device_sms());
+    kern<<<grid, 128, smem, s>>>(p);
+    LRES_CUDA_TRY(cudaGetLastError());
+    return LRES_OK;
+}
+
 static int launch_left_tc(const LdlParams<float2>& p, int grid, cudaStream_t s) {
     const size_t smem = 2 * (size_t)tc::A_BYTES + 2 * (size_t)tc::B_BYTES +
                         sizeof(float2) * ((size_t)32 * 33 + 32 * 32 + 3 * 32 + p.mmax);
-    LRES_CUDA_TRY(cudaFuncSetAttribute(ldl_left_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int dev = 0, nsm = 0;
-    LRES_CUDA_TRY(cudaGetDevice(&dev));
-    LRES_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    grid = std::min(grid, nsm);                         // one CTA (one TMEM allocation) per SM
+    int per_sm = 0;
+    if (int rc = prepare_kernel<ldl_left_tc_kernel>(128, smem, &per_sm)) return rc;
+    grid = std::min(grid, device_sms());                // one CTA (one TMEM allocation) per SM
     ldl_left_tc_kernel<<<grid, 128, smem, s>>>(p);
     LRES_CUDA_TRY(cudaGetLastError());
     return LRES_OK;
@@ -847,13 +1126,10 @@ template <class T, int NB, int NT, int KC>
 static int launch_left(const LdlParams<T>& p, int grid, cudaStream_t s) {
     const size_t smem = sizeof(T) * ((size_t)2 * KC * NB + 32 * (NB + 1) + NB * NB + 3 * NB + p.mmax + (size_t)NB * NT);
     auto kern = ldl_left_kernel<T, NB, NT, KC>;
-    LRES_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     // persistent grid: as many CTAs as fit on the device, at most one workspace slot each
-    int dev = 0, nsm = 0, per_sm = 0;
-    LRES_CUDA_TRY(cudaGetDevice(&dev));
-    LRES_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    LRES_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem));
-    grid = std::min(grid, std::max(1, per_sm) * nsm);
+    int per_sm = 0;
+    if (int rc = prepare_kernel<ldl_left_kernel<T, NB, NT, KC>>(NT, smem, &per_sm)) return rc;
+    grid = std::min(grid, std::max(1, per_sm) * device_sms());
     kern<<<grid, NT, smem, s>>>(p);
     LRES_CUDA_TRY(cudaGetLastError());
     return LRES_OK;
@@ -866,9 +1142,9 @@ static int launch_left(const LdlParams<T>& p, int grid, cudaStream_t s) {
 template <class T, int NB, int TR, int TC, int NT>
 static int launch_ldl(const LdlParams<T>& p, int grid, cudaStream_t s) {
     const size_t smem = sizeof(T) * ((size_t)NB * p.ldp + NB * NB + 3 * NB + p.mmax);
-    auto kern = ldl_aug_kernel<T, NB, TR, TC, NT>;
-    LRES_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<grid, NT, smem, s>>>(p);
+    int per_sm = 0;
+    if (int rc = prepare_kernel<ldl_aug_kernel<T, NB, TR, TC, NT>>(NT, smem, &per_sm)) return rc;
+    ldl_aug_kernel<T, NB, TR, TC, NT><<<grid, NT, smem, s>>>(p);
     LRES_CUDA_TRY(cudaGetLastError());
     return LRES_OK;
 }
@@ -916,6 +1192,7 @@ int run_ldl(const LdlJob& j, cudaStream_t s) {
             case 2: return launch_left<double2, 16, 256, 16>(p, j.grid, s);
             case 3: return launch_left<double2, 8, 256, 32>(p, j.grid, s);
             case 4: return launch_left<double2, 8, 128, 32>(p, j.grid, s);
+            case 5: return launch_left_bulk<double2, 16, 16>(p, j.grid, s);
             default: return launch_left<double2, 16, 256, 32>(p, j.grid, s);
         }
     } else if (j.kind == LdlJob::C64) {
@@ -931,6 +1208,7 @@ int run_ldl(const LdlJob& j, cudaStream_t s) {
             case 2: return launch_left<float2, 32, 256, 16>(p, j.grid, s);
             case 3: return launch_left<float2, 16, 256, 32>(p, j.grid, s);
             case 4: return launch_left_tc(p, j.grid, s);
+            case 5: return launch_left_bulk<float2, 32, 32>(p, j.grid, s);
             default: return launch_left<float2, 32, 256, 32>(p, j.grid, s);
         }
     } else {

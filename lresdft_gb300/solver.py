@@ -154,9 +154,9 @@ class LResGPU:
         else:
             self.set_hamiltonian(self.b.H(v))
 
-    def set_potential_device(self, v_ptr):
-        """H(v) from a device array of ng doubles (stream-ordered, no host copy)."""
-        _lib.check(_lib.lib.lres_set_potential(self._ctx, v_ptr, 1, None))
+    def set_potential_device(self, v_ptr, stream=None):
+        """H(v) from a device array of ng doubles (stream-ordered, no host copy; capturable)."""
+        _lib.check(_lib.lib.lres_set_potential(self._ctx, v_ptr, 1, stream))
 
     def pole_pass_device(self, mu, e_lo, dens_ptr=None):
         """Pole pass leaving the density on the device (copied to dens_ptr if given);
@@ -164,6 +164,21 @@ class LResGPU:
         self.passes += 1
         _lib.check(_lib.lib.lres_pass(self._ctx, float(mu), float(e_lo), dens_ptr, 1, _lib.ptrd(self._out), None))
         return float(self._out[0]), float(self._out[1])
+
+    def pass_async(self, mu, e_lo, d_out_ptr, stream=None):
+        """Capturable pass: no host synchronisation; N, E_band land in d_out_ptr[0..1]."""
+        self.passes += 1
+        _lib.check(_lib.lib.lres_pass_async(self._ctx, float(mu), float(e_lo), d_out_ptr, stream))
+
+    def status(self):
+        st = C.c_int32()
+        _lib.check(_lib.lib.lres_status(self._ctx, C.byref(st), None))
+        return int(st.value)
+
+    def density_device_ptr(self):
+        p = C.c_void_p()
+        _lib.check(_lib.lib.lres_density_ptr(self._ctx, C.byref(p)))
+        return p.value
 
     def set_hamiltonian(self, H):
         Hp, Hi, Hv = csr64(H)
@@ -180,10 +195,10 @@ class LResGPU:
         return (dens.copy() if want_density else None), float(self._out[0]), float(self._out[1])
 
     def autotune(self, mu, e_lo, config=-1):
-        """Pick the tile configuration of the pole kernel (-1: time all five with full
+        """Pick the tile configuration of the pole kernel (-1: time all six with full
         passes at (mu, e_lo) and keep the fastest).  Returns (chosen, ms per config)."""
         chosen = C.c_int32()
-        ms = np.full(5, -1.0)
+        ms = np.full(6, -1.0)
         _lib.check(_lib.lib.lres_autotune(self._ctx, float(mu), float(e_lo), int(config), C.byref(chosen),
                                           _lib.ptrd(ms), None))
         return int(chosen.value), ms
@@ -246,9 +261,11 @@ class LResGPU:
             x0, f0, d0, e0 = start
             cache[x0] = (d0, e0)
             hist.append((x0, f0))
+            # Newton step with the slope dN/dmu of the previous solve; stop if it lands within
+            # the tolerance, bracket on a sign change, else widen with secant steps
             slope = self._slope if self._slope and self._slope > 0 else max(N, 1.0)
             step = -f0 / slope
-            step = math.copysign(min(max(abs(step) * 1.2, 1e-7), 0.25), step)
+            step = math.copysign(min(max(abs(step), 1e-7), 0.1), step)
             a, fa = x0, f0
             b = None
             for _ in range(40):
@@ -256,12 +273,15 @@ class LResGPU:
                 if x1 <= lo_bound:
                     x1 = 0.5 * (a + lo_bound)
                 f1 = f(x1)
-                if (f1 > 0) != (fa > 0) or f1 == 0:
+                if abs(f1) <= ftol:
+                    self._note_slope(hist, x1)
+                    return x1, cache[x1][0], cache[x1][1]
+                if (f1 > 0) != (fa > 0):
                     b, fb = x1, f1
                     break
-                # secant extrapolation from the last two points, at least doubling the step
+                # secant extrapolation from the last two points, at least 1.5x further
                 sec = -f1 * (x1 - a) / (f1 - fa) if f1 != fa else 2 * step
-                step = math.copysign(min(max(abs(sec) * 1.2, 2 * abs(step)), 1.0), step)
+                step = math.copysign(min(max(abs(sec) * 1.1, 1.5 * abs(step)), 1.0), step)
                 a, fa = x1, f1
             if b is None:
                 raise StaleMu("no sign change of the electron count near the warm-start mu")
@@ -281,16 +301,26 @@ class LResGPU:
                 fhi = f(hi)
             a, fa, b, fb = lo, flo, hi, fhi
         x = self._brent(f, a, fa, b, fb, ftol, xtol=getattr(self, "_xtol", 1e-12))
-        # local slope dN/dmu for the next warm start: the closest points on both sides
+        self._note_slope(hist, x)
+        dens, eb = cache[x]
+        return x, dens, eb
+
+    def _note_slope(self, hist, x):
+        """Local slope dN/dmu at the accepted root for the next warm start: the secant of
+        the closest evaluations on both sides (or the two closest ones)."""
         below = [h for h in hist if h[1] < 0]
         above = [h for h in hist if h[1] > 0]
         if below and above:
             lb = min(below, key=lambda h: abs(h[0] - x))
             ub = min(above, key=lambda h: abs(h[0] - x))
-            if ub[0] != lb[0]:
-                self._slope = (ub[1] - lb[1]) / (ub[0] - lb[0])
-        dens, eb = cache[x]
-        return x, dens, eb
+        elif len(hist) >= 2:
+            lb, ub = sorted(hist, key=lambda h: abs(h[0] - x))[:2]
+        else:
+            return
+        if ub[0] != lb[0]:
+            sl = (ub[1] - lb[1]) / (ub[0] - lb[0])
+            if sl > 0:
+                self._slope = sl
 
     @staticmethod
     def _brent(f, a, fa, b, fb, ftol, xtol=1e-12, maxit=100):

@@ -28,6 +28,18 @@ def systems():
     return out
 
 
+def _copy_device(ptr, host):
+    """Device-to-host copy of a raw device array of doubles (wrapped for torch through the
+    CUDA array interface)."""
+    import torch
+
+    class _Dev:
+        __cuda_array_interface__ = {"shape": (host.size,), "typestr": "<f8",
+                                    "data": (int(ptr), False), "version": 3}
+    torch.cuda.synchronize()
+    host[:] = torch.as_tensor(_Dev(), device="cuda").cpu().numpy()
+
+
 def _solver(b, cr, g, precision="fp64"):
     from lresdft_gb300 import LResGPU
     return LResGPU(b, cr.pos, R_w=float(g["R_w"]), M=int(g["M"]), precision=precision)
@@ -160,7 +172,7 @@ def test_scf_energy_matches_reference(systems, name):
 
 
 @pytest.mark.parametrize("name", CASES)
-@pytest.mark.parametrize("config", [0, 1, 2, 3, 4])
+@pytest.mark.parametrize("config", [0, 1, 2, 3, 4, 5])
 def test_every_tile_configuration_matches_reference(systems, name, config):
     """Each compiled tile configuration of the pole kernel, forced: FP64 to 1e-10 in
     density, mixed within the 2e-7 Ha/electron gate (configuration 4 of the mixed path runs
@@ -177,3 +189,36 @@ def test_every_tile_configuration_matches_reference(systems, name, config):
         else:
             assert abs(eb - g["cold_eband"]) / cr.n_elec < 2e-7
         s.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_pass_captured_in_cuda_graph(systems, precision):
+    """lres_set_potential (device v) + lres_pass_async captured once in a CUDA graph and
+    replayed: the same N, E_band and density as the synchronous lres_pass, bit for bit."""
+    import torch
+    g, cr, b = systems["cubic3"]
+    mu, e_lo = float(g["cold_mu"]), float(g["cold_elo"])
+    s = _solver(b, cr, g, precision)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    v = torch.from_numpy(g["v"].copy()).to(dev)
+    s.set_potential_device(v.data_ptr())
+    dens_ref, N_ref, E_ref = s.pole_pass(mu, e_lo)
+    out = torch.zeros(2, dtype=torch.float64, device=dev)
+    graph = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.graph(graph, stream=side):
+        st = torch.cuda.current_stream().cuda_stream
+        s.set_potential_device(v.data_ptr(), st)
+        s.pass_async(mu, e_lo, out.data_ptr(), st)
+    for _ in range(2):
+        out.zero_()
+        graph.replay()
+        torch.cuda.synchronize()
+        assert s.status() == 0
+        N, E = out.cpu().numpy()
+        assert N == N_ref and E == E_ref
+        host = np.empty(cr.ng)
+        _copy_device(s.density_device_ptr(), host)
+        assert np.array_equal(host, dens_ref)
+    s.close()
