@@ -168,6 +168,34 @@ int lres_voronoi_owner(const int64_t shape[3], const double cell[3], int64_t nce
 int lres_inertia_noalloc(int32_t nwin, const int32_t* n_w, const int64_t* offC, const double* H, const double* S,
                          double sigma, int32_t* below, int32_t nmax, void* stream);
 
+/* Replaces the dense window matrices directly (H and/or S may be NULL to keep the current
+ * one): float64 arrays in the window layout of the context — window w's column-major
+ * n_w x n_w block at offset offC[w] = sum_{u<w} n_u^2, windows in the order of Woff.  The
+ * LRES_MIXED path refactors S_W (standard form) when S is given.  The blocks stay in place
+ * until the next lres_set_potential / lres_set_hamiltonian_csr, which re-gather H_W only.
+ * The reference builds H_W, S_W only by gather (src/lrft_cpp.cpp:116-127); this entry makes
+ * the window matrices inputs of their own, as the adjoint below differentiates them. */
+int lres_set_windows(lres_ctx* ctx, const double* HW, const double* SW, int on_device, void* stream);
+
+/* Device addresses of the context's dense window matrices H_W and S_W (float64, window
+ * layout as lres_set_windows; valid until destroy, contents change with every update). */
+int lres_window_ptrs(lres_ctx* ctx, const double** d_HW, const double** d_SW);
+
+/* Adjoint of the band energy at fixed electron number (e_lo fixed), at (mu, e_lo) on the
+ * current window matrices.  The reference has no gradient code; its finite-M
+ * Hellmann-Feynman check (tests/test_lrft.py:59-79) is the template.  Runs one pole pass
+ * whose factors are kept (pole batches of whole windows, as many as free device memory
+ * admits), back-substitutes Z_k = (z_k S_W - H_W)^-1 F_W^T, accumulates Re sum_k c_k Z_k Z_k^T
+ * for c in {w, w z, w z^2} and returns, each optional:
+ *   dv[ng]           dE_band/dv(r) at fixed N (the grid local potential through
+ *                    H = T + X^T diag(v) X dV, lrft/lcao3d.py:98-100);
+ *   dHW, dSW[sizeC]  dE_band/dH_W and dE_band/dS_W at fixed N, window layout as
+ *                    lres_set_windows (each window's matrices taken as independent);
+ *   out[6]           N(mu), E_band(mu), dN/dmu, dE/dmu, kappa = (dE/dmu)/(dN/dmu), status.
+ * The pass also leaves the density in the context (lres_density_ptr).  Synchronises. */
+int lres_adjoint(lres_ctx* ctx, double mu, double e_lo, double* dv, int dv_on_device, double* dHW, double* dSW,
+                 int dW_on_device, double* out, void* stream);
+
 /* Grid kernels on device arrays of ng doubles (context supplies shape and cell). */
 int lres_lda_xc(lres_ctx* ctx, const double* dens, double* exc, double* vxc, void* stream);
 int lres_hartree(lres_ctx* ctx, const double* dens, double* vh, void* stream);

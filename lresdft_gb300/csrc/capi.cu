@@ -96,6 +96,21 @@ struct lres_ctx {
     void* d_q = nullptr;
     double *d_dens = nullptr, *d_nw = nullptr, *d_ew = nullptr, *d_v = nullptr;
     std::vector<double> nw_h, ew_h;
+    // host copies kept for the adjoint's inverse maps
+    std::vector<long long> soff_h;
+    std::vector<int> sgrid_h, wgrp_off_h, wgrp_h, wgrp_lo_h, gloc_h;
+    // adjoint (allocated on first use)
+    bool adj_ready = false;
+    double *d_adjA[3] = {nullptr, nullptr, nullptr}, *d_dHW = nullptr, *d_dSW = nullptr, *d_gH = nullptr;
+    double *d_adjdv = nullptr, *d_adju = nullptr;
+    double2* d_cw = nullptr;
+    int* d_order = nullptr;
+    long long *d_eoff = nullptr, *d_poff = nullptr;
+    int4* d_ent = nullptr;
+    int2* d_pent = nullptr;
+    void* d_adjws = nullptr;
+    size_t adjws_bytes = 0;
+    std::vector<double> adju_h;
     // grid
     FFT3* fft = nullptr;
     double2* d_fftwork = nullptr;
@@ -111,7 +126,8 @@ lres_ctx::~lres_ctx() {
                     bp.gptr, bp.bptr, bp.bcol, bp.brow, bp.boff, bp.btrans, bp.pair_blk, sp.soff, sp.sgrid,
                     sp.sval, sp.coff, sp.cslot, d_Sblk, d_Tblk, d_Hblk, d_SW, d_HW, d_F, d_LinvT, d_Y, d_Hhat,
                     d_Hhat32, d_Fhat32, d_LinvT_df, d_H_df, d_Y_df, d_items, d_items_win, d_items_sub, d_counter, d_status, d_npos, d_ws, d_shifts,
-                    d_wq, d_wzq, d_q, d_dens, d_nw, d_ew, d_v, d_fftwork};
+                    d_wq, d_wzq, d_q, d_dens, d_nw, d_ew, d_v, d_fftwork, d_adjA[0], d_adjA[1], d_adjA[2],
+                    d_dHW, d_dSW, d_gH, d_adjdv, d_adju, d_cw, d_order, d_eoff, d_poff, d_ent, d_pent, d_adjws};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (fft) fft3_destroy(fft);
@@ -241,6 +257,50 @@ int after_h_blocks(lres_ctx* c, cudaStream_t s) {
         TRY(mark(c, 4, 1, s));
     }
     c->have_h = true;
+    return LRES_OK;
+}
+
+// Standard form of the mixed path from the current S_W: L_c^-1 (stored as L^-T, FP64 and as
+// double-float pairs) and F^ = L_c^-1 F (FP32).  Allocates on the first call.
+int setup_standard_form(lres_ctx* c, cudaStream_t s) {
+    if (!c->d_LinvT) {
+        TRY(dalloc(&c->d_LinvT, c->sizeC));
+        TRY(dalloc(&c->d_LinvT_df, c->sizeC));
+        TRY(dalloc(&c->d_H_df, c->sizeC));
+        TRY(dalloc(&c->d_Y_df, c->sizeC));
+        TRY(dalloc(&c->d_Hhat32, c->sizeC));
+        TRY(dalloc(&c->d_Fhat32, c->sizeF));
+    }
+    double* I = nullptr;
+    double* Fhat = nullptr;
+    double* one = nullptr;
+    TRY(dalloc(&I, c->sizeC));
+    TRY(dalloc(&Fhat, c->sizeF));
+    TRY(dalloc(&one, 1));
+    const double h_one = 1.0;
+    LRES_CUDA_TRY(cudaMemcpyAsync(one, &h_one, sizeof(double), cudaMemcpyHostToDevice, s));
+    LRES_CUDA_TRY(cudaMemsetAsync(I, 0, sizeof(double) * c->sizeC, s));
+    identity_kernel<<<c->nwin, 128, 0, s>>>(c->d_n, c->d_offC, I, c->nwin);
+    LRES_CUDA_TRY(cudaGetLastError());
+    LRES_CUDA_TRY(cudaMemsetAsync(c->d_status, 0, sizeof(int), s));
+    // A = 1*S - 0 with identity rows: multipliers sqrt(D) D^-1 L^-1 e_r = (L_c^-1)_{:,r}
+    int rc = ldl_launch(c, LdlJob::R64, c->nwin, c->d_items_win, nullptr, c->d_SW, I, c->d_n, c->d_offC, one,
+                        nullptr, c->d_LinvT, 2 * c->nmax, c->nmax, s);
+    if (!rc)
+        rc = ldl_launch(c, LdlJob::R64, c->nwin, c->d_items_win, nullptr, c->d_SW, c->d_F, c->d_m, c->d_offF, one,
+                        nullptr, Fhat, c->nmax + c->mmax, c->mmax, s);
+    if (!rc) rc = convert_f64_f32(Fhat, c->d_Fhat32, c->sizeF, s);
+    if (!rc) rc = split_f64(c->d_LinvT, c->d_LinvT_df, c->sizeC, s);
+    int st = 0;
+    if (!rc) rc = read_status(c, s, &st);
+    cudaFree(I);
+    cudaFree(Fhat);
+    cudaFree(one);
+    if (rc) return rc;
+    if (st) {
+        lres_set_error("Cholesky of a window overlap S_W failed (status %d)", st);
+        return LRES_ENUMERIC;
+    }
     return LRES_OK;
 }
 
@@ -539,6 +599,13 @@ extern "C" int lres_ctx_create(lres_ctx** out, const lres_system_desc* d, int pr
         TRY(upload(&c->d_Oflat, Oflat, s));
     }
     TRY(pair_common_points(c->bp, c->sp, c->ngroups, pair_g, pair_h, s));
+    LRES_CUDA_TRY(cudaStreamSynchronize(s));   // the uploads above read the host vectors moved below
+    c->soff_h = std::move(soff);
+    c->sgrid_h = std::move(sgrid);
+    c->wgrp_off_h = std::move(wgrp_off);
+    c->wgrp_h = std::move(wgrp);
+    c->wgrp_lo_h = std::move(wgrp_lo);
+    c->gloc_h = std::move(gloc);
 
     // ---- dense window overlaps and owned-point blocks
     TRY(dalloc(&c->d_SW, c->sizeC));
@@ -606,45 +673,8 @@ extern "C" int lres_ctx_create(lres_ctx** out, const lres_system_desc* d, int pr
     c->ws_bytes = slot * 4 * c->nsm;
     TRY(dalloc((char**)&c->d_ws, c->ws_bytes));
 
-    // ---- standard form for the mixed path: L_c^-1 (as L^-T) and F^ = L_c^-1 F, FP64
-    if (precision == LRES_MIXED) {
-        TRY(dalloc(&c->d_LinvT, c->sizeC));
-        TRY(dalloc(&c->d_LinvT_df, c->sizeC));
-        TRY(dalloc(&c->d_H_df, c->sizeC));
-        TRY(dalloc(&c->d_Y_df, c->sizeC));
-        TRY(dalloc(&c->d_Hhat32, c->sizeC));
-        TRY(dalloc(&c->d_Fhat32, c->sizeF));
-        double* I = nullptr;
-        double* Fhat = nullptr;
-        double* one = nullptr;
-        TRY(dalloc(&I, c->sizeC));
-        TRY(dalloc(&Fhat, c->sizeF));
-        TRY(dalloc(&one, 1));
-        const double h_one = 1.0;
-        LRES_CUDA_TRY(cudaMemcpyAsync(one, &h_one, sizeof(double), cudaMemcpyHostToDevice, s));
-        LRES_CUDA_TRY(cudaMemsetAsync(I, 0, sizeof(double) * c->sizeC, s));
-        identity_kernel<<<c->nwin, 128, 0, s>>>(c->d_n, c->d_offC, I, c->nwin);
-        LRES_CUDA_TRY(cudaGetLastError());
-        LRES_CUDA_TRY(cudaMemsetAsync(c->d_status, 0, sizeof(int), s));
-        // A = 1*S - 0 with identity rows: multipliers sqrt(D) D^-1 L^-1 e_r = (L_c^-1)_{:,r}
-        int rc = ldl_launch(c.get(), LdlJob::R64, c->nwin, c->d_items_win, nullptr, c->d_SW, I, c->d_n, c->d_offC,
-                            one, nullptr, c->d_LinvT, 2 * c->nmax, c->nmax, s);
-        if (!rc)
-            rc = ldl_launch(c.get(), LdlJob::R64, c->nwin, c->d_items_win, nullptr, c->d_SW, c->d_F, c->d_m,
-                            c->d_offF, one, nullptr, Fhat, c->nmax + c->mmax, c->mmax, s);
-        if (!rc) rc = convert_f64_f32(Fhat, c->d_Fhat32, c->sizeF, s);
-        if (!rc) rc = split_f64(c->d_LinvT, c->d_LinvT_df, c->sizeC, s);
-        int st = 0;
-        if (!rc) rc = read_status(c.get(), s, &st);
-        cudaFree(I);
-        cudaFree(Fhat);
-        cudaFree(one);
-        if (rc) return rc;
-        if (st) {
-            lres_set_error("Cholesky of a window overlap S_W failed (status %d)", st);
-            return LRES_ENUMERIC;
-        }
-    }
+    // ---- standard form for the mixed path
+    if (precision == LRES_MIXED) TRY(setup_standard_form(c.get(), s));
 
     // ---- pass buffers
     TRY(dalloc((char**)&c->d_shifts, (size_t)c->npoles * 16));
@@ -1066,4 +1096,252 @@ extern "C" int lres_ion_potential(lres_ctx* c, int64_t natoms, const double* pos
     cudaFree(dz);
     cudaFree(dr);
     return r;
+}
+
+// ---------------------------------------------------------------------------
+// window matrices set directly, and the adjoint of the band energy at fixed N
+// ---------------------------------------------------------------------------
+
+extern "C" int lres_set_windows(lres_ctx* c, const double* HW, const double* SW, int on_device, void* stream) {
+    if (!c || (!HW && !SW)) {
+        lres_set_error("null argument");
+        return LRES_EINVAL;
+    }
+    if (!HW && !c->have_h) {
+        lres_set_error("lres_set_windows without H_W before a Hamiltonian was set");
+        return LRES_ESTATE;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    if (HW) LRES_CUDA_TRY(cudaMemcpyAsync(c->d_HW, HW, sizeof(double) * c->sizeC, kind, s));
+    if (SW) {
+        LRES_CUDA_TRY(cudaMemcpyAsync(c->d_SW, SW, sizeof(double) * c->sizeC, kind, s));
+        if (c->precision == LRES_MIXED) TRY(setup_standard_form(c, s));
+    }
+    if (c->precision == LRES_MIXED) TRY(window_transform(c, s));
+    c->have_h = true;
+    if (!on_device) LRES_CUDA_TRY(cudaStreamSynchronize(s));
+    return LRES_OK;
+}
+
+extern "C" int lres_window_ptrs(lres_ctx* c, const double** d_HW, const double** d_SW) {
+    if (!c || !d_HW || !d_SW) {
+        lres_set_error("null argument");
+        return LRES_EINVAL;
+    }
+    *d_HW = c->d_HW;
+    *d_SW = c->d_SW;
+    return LRES_OK;
+}
+
+namespace {
+
+// Inverse maps of the adjoint (once per context): for every stored atom-pair block the
+// windows holding both atoms with the atoms' local offsets (windows ascending), and for
+// every grid point the atoms whose support covers it with their support slots.
+int adj_prepare(lres_ctx* c, cudaStream_t s) {
+    if (c->adj_ready) return LRES_OK;
+    const int nblk = c->bp.nblk;
+    std::vector<long long> eoff(nblk + 1, 0);
+    for (int pass = 0; pass < 2; ++pass) {
+        std::vector<long long> cur;
+        std::vector<int4> ent;
+        if (pass) {
+            for (int b = 0; b < nblk; ++b) eoff[b + 1] += eoff[b];
+            cur.assign(eoff.begin(), eoff.end() - 1);
+            ent.resize(eoff[nblk]);
+        }
+        for (int w = 0; w < c->nwin; ++w)
+            for (int gi = c->wgrp_off_h[w]; gi < c->wgrp_off_h[w + 1]; ++gi) {
+                const int g = c->wgrp_h[gi], lg = c->wgrp_lo_h[gi];
+                for (int b = c->bptr_h[g]; b < c->bptr_h[g + 1]; ++b) {
+                    const int lh = c->gloc_h[(size_t)w * c->ngroups + c->bcol_h[b]];
+                    if (lh < 0) continue;
+                    if (pass) ent[cur[b]++] = make_int4(w, lg, lh, 0);
+                    else ++eoff[b + 1];
+                }
+            }
+        if (pass) {
+            TRY(upload(&c->d_eoff, eoff, s));
+            TRY(upload(&c->d_ent, ent, s));
+            LRES_CUDA_TRY(cudaStreamSynchronize(s));
+        }
+    }
+    std::vector<long long> poff(c->ng + 1, 0);
+    for (long long sl = 0; sl < (long long)c->sgrid_h.size(); ++sl) ++poff[c->sgrid_h[sl] + 1];
+    for (long long r = 0; r < c->ng; ++r) poff[r + 1] += poff[r];
+    std::vector<int2> pent(poff[c->ng]);
+    {
+        std::vector<long long> cur(poff.begin(), poff.end() - 1);
+        for (int g = 0; g < c->ngroups; ++g)
+            for (long long sl = c->soff_h[g]; sl < c->soff_h[g + 1]; ++sl)
+                pent[cur[c->sgrid_h[sl]]++] = make_int2(g, (int)sl);
+    }
+    TRY(upload(&c->d_poff, poff, s));
+    TRY(upload(&c->d_pent, pent, s));
+    TRY(upload(&c->d_order, c->order, s));
+    for (double*& a : c->d_adjA) TRY(dalloc(&a, c->sizeC));
+    TRY(dalloc(&c->d_dHW, c->sizeC));
+    TRY(dalloc(&c->d_dSW, c->sizeC));
+    TRY(dalloc(&c->d_gH, c->bp.nval));
+    TRY(dalloc(&c->d_adjdv, c->ng));
+    TRY(dalloc(&c->d_adju, 3 * (size_t)c->nwin));
+    TRY(dalloc(&c->d_cw, 3 * (size_t)c->npoles));
+    c->adju_h.resize(3 * (size_t)c->nwin);
+    LRES_CUDA_TRY(cudaStreamSynchronize(s));
+    c->adj_ready = true;
+    return LRES_OK;
+}
+
+}  // namespace
+
+extern "C" int lres_adjoint(lres_ctx* c, double mu, double e_lo, double* dv, int dv_on_device, double* dHW,
+                            double* dSW, int dW_on_device, double* out, void* stream) {
+    if (!c || !out) {
+        lres_set_error("null argument");
+        return LRES_EINVAL;
+    }
+    if (!c->have_h) {
+        lres_set_error("lres_adjoint before a Hamiltonian was set");
+        return LRES_ESTATE;
+    }
+    if (!(mu > e_lo) || !std::isfinite(mu) || !std::isfinite(e_lo)) {
+        lres_set_error("need finite e_lo < mu (got mu=%g, e_lo=%g)", mu, e_lo);
+        return LRES_EINVAL;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    TRY(adj_prepare(c, s));
+    const bool mixed = c->precision == LRES_MIXED;
+    const int P = c->npoles;
+    const size_t el = mixed ? 8 : 16;
+    const int nbk = mixed ? kKeepNB64 : kKeepNB128;
+    const long long npmax = (c->nmax + nbk - 1) / nbk * nbk;
+    const long long stride = ((npmax + c->mmax + 1) * npmax + 15) / 16 * 16;   // elements per item slot
+    const size_t item_bytes = (size_t)stride * el;
+    // items per batch: whole windows (all poles), as many as the free device memory admits
+    size_t freeb = 0, totalb = 0;
+    LRES_CUDA_TRY(cudaMemGetInfo(&freeb, &totalb));
+    size_t have = c->adjws_bytes + freeb;
+    const size_t reserve = (size_t)4 << 30;
+    size_t budget = have > reserve ? std::min(have - reserve, have / 4 * 3) : 0;
+    long long win_per_batch = (long long)(budget / (item_bytes * P));
+    if (win_per_batch < 1) {
+        lres_set_error("adjoint: one window's %d pole factors (%zu bytes) do not fit in free device memory", P,
+                       item_bytes * P);
+        return LRES_ENOMEM;
+    }
+    win_per_batch = std::min<long long>(win_per_batch, c->nwin);
+    const size_t need = item_bytes * P * (size_t)win_per_batch;
+    if (c->adjws_bytes < need) {
+        if (c->d_adjws) cudaFree(c->d_adjws);
+        c->d_adjws = nullptr;
+        c->adjws_bytes = 0;
+        TRY(dalloc((char**)&c->d_adjws, need));
+        c->adjws_bytes = need;
+    }
+    poles_kernel<<<(P + 63) / 64, 64, 0, s>>>(P, c->M, mu, e_lo, mixed ? 1 : 0, c->d_shifts, c->d_wq, c->d_wzq);
+    LRES_CUDA_TRY(cudaGetLastError());
+    TRY(adj_weights(P, c->M, mu, e_lo, c->d_cw, s));
+    LRES_CUDA_TRY(cudaMemsetAsync(c->d_status, 0, sizeof(int), s));
+    for (long long w0 = 0; w0 < c->nwin; w0 += win_per_batch) {
+        const int nwb = (int)std::min<long long>(win_per_batch, c->nwin - w0);
+        const int2* items = c->d_items + w0 * P;       // windows in work-queue order, poles inner
+        const int nit = nwb * P;
+        LdlJob j{};
+        j.kind = mixed ? LdlJob::C64 : LdlJob::C128;
+        j.nitems = nit;
+        j.items = items;
+        j.counter = c->d_counter;
+        j.n_w = c->d_n;
+        j.m_w = c->d_m;
+        j.offC = c->d_offC;
+        j.offF = c->d_offF;
+        j.offQ = c->d_offQ;
+        j.C = mixed ? (const void*)c->d_Hhat32 : (const void*)c->d_HW;
+        j.B = mixed ? nullptr : (const void*)c->d_SW;
+        j.F = mixed ? (const void*)c->d_Fhat32 : (const void*)c->d_F;
+        j.shifts = c->d_shifts;
+        j.q = c->d_q;
+        j.qstride = c->npts;
+        j.npos = c->d_npos;
+        j.status = c->d_status;
+        j.ws = c->d_adjws;
+        j.ws_stride = stride;
+        j.ldp = c->nmax + c->mmax;
+        j.nmax = c->nmax;
+        j.mmax = c->mmax;
+        j.grid = nit;
+        j.smem_budget = c->smem_budget;
+        j.config = 0;
+        j.keep = 1;
+        LRES_CUDA_TRY(cudaMemsetAsync(c->d_counter, 0, sizeof(int), s));
+        TRY(run_ldl(j, s));
+        TRY(adj_backsolve(mixed, items, nit, c->d_n, c->d_m, c->d_adjws, stride, c->d_status, s));
+        TRY(adj_accumulate(mixed, c->d_order + w0, nwb, P, c->nmax, c->d_n, c->d_m, c->d_offC, c->d_adjws, stride,
+                           c->d_cw, c->d_adjA[0], c->d_adjA[1], c->d_adjA[2], s));
+    }
+    TRY(pole_sums(c->nwin, c->d_offQ, c->d_m, c->d_Oflat, mixed, c->d_q, c->npts, P, c->d_wq, c->d_wzq, c->dV,
+                  c->d_dens, c->d_nw, c->d_ew, s));
+    TRY(adj_inner(c->nwin, c->d_n, c->d_offC, mixed ? nullptr : c->d_SW, c->d_adjA[0], c->d_adjA[1], c->d_adjA[2],
+                  c->d_adju, s));
+    LRES_CUDA_TRY(cudaMemcpyAsync(c->nw_h.data(), c->d_nw, sizeof(double) * c->nwin, cudaMemcpyDeviceToHost, s));
+    LRES_CUDA_TRY(cudaMemcpyAsync(c->ew_h.data(), c->d_ew, sizeof(double) * c->nwin, cudaMemcpyDeviceToHost, s));
+    LRES_CUDA_TRY(cudaMemcpyAsync(c->adju_h.data(), c->d_adju, sizeof(double) * 3 * c->nwin,
+                                  cudaMemcpyDeviceToHost, s));
+    int st = 0;
+    TRY(read_status(c, s, &st));
+    if (st) {
+        lres_set_error(st & ST_ZERO_PIVOT ? "zero or non-finite pivot in a window factorisation (adjoint)"
+                                          : "window kernel status %d (adjoint)", st);
+        return st & ST_ZERO_PIVOT ? LRES_ENUMERIC : LRES_EINVAL;
+    }
+    double N = 0.0, E = 0.0, U[3] = {0.0, 0.0, 0.0};
+    for (int w = 0; w < c->nwin; ++w) {
+        N += c->nw_h[w];
+        E += c->ew_h[w];
+        for (int k = 0; k < 3; ++k) U[k] += c->adju_h[(size_t)k * c->nwin + w];
+    }
+    for (double& u : U) u *= 4.0 * c->dV;
+    // z' = (1 + zeta)/2 = 1/2 + (z - cc)/(2R) and w' = w/(2R): every mu derivative is a real
+    // combination of the three accumulations and of N, E
+    const double cc = 0.5 * (mu + e_lo), R = 0.5 * (mu - e_lo);
+    const double a0 = 0.5 - cc / (2.0 * R), a1 = 1.0 / (2.0 * R);
+    const double dNdmu = N / (2.0 * R) - (a0 * U[0] + a1 * U[1]);
+    const double dEdmu = E / R + 0.5 * N - cc * N / (2.0 * R) - (a0 * U[1] + a1 * U[2]);
+    if (!(dNdmu != 0.0) || !std::isfinite(dNdmu) || !std::isfinite(dEdmu)) {
+        lres_set_error("adjoint: dN/dmu = %g is not usable", dNdmu);
+        return LRES_ENUMERIC;
+    }
+    const double kappa = dEdmu / dNdmu;
+    const double sc = 4.0 * c->dV;
+    if (mixed) {
+        // B_H = 4dV (A1 - kappa A0) into A0, B_S = -4dV (A2 - kappa A1) into A2, then L^-T B L^-1
+        TRY(adj_combine(c->sizeC, c->d_adjA[0], c->d_adjA[1], c->d_adjA[2], kappa, sc, -sc, c->d_adjA[0],
+                        c->d_adjA[2], s));
+        for (int which = 0; which < 2; ++which) {
+            const double* B = which ? c->d_adjA[2] : c->d_adjA[0];
+            double* D = which ? c->d_dSW : c->d_dHW;
+            TRY(batched_gemm(c->nwin, c->d_n, c->d_offC, c->nmax, false, c->d_LinvT, B, c->d_adjA[1], s));
+            TRY(batched_gemm(c->nwin, c->d_n, c->d_offC, c->nmax, false, c->d_adjA[1], c->d_LinvT, D, s, 0, true));
+        }
+    } else {
+        TRY(adj_combine(c->sizeC, c->d_adjA[0], c->d_adjA[1], c->d_adjA[2], kappa, sc, -sc, c->d_dHW, c->d_dSW,
+                        s));
+    }
+    TRY(adj_block_gather(c->bp, c->d_eoff, c->d_ent, c->d_n, c->d_offC, c->d_dHW, c->d_gH, s));
+    TRY(adj_point(c->ng, c->d_poff, c->d_pent, c->sp, c->bp, c->d_gH, c->dV, c->d_adjdv, s));
+    if (dv)
+        LRES_CUDA_TRY(cudaMemcpyAsync(dv, c->d_adjdv, sizeof(double) * c->ng,
+                                      dv_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+    const cudaMemcpyKind wk = dW_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (dHW) LRES_CUDA_TRY(cudaMemcpyAsync(dHW, c->d_dHW, sizeof(double) * c->sizeC, wk, s));
+    if (dSW) LRES_CUDA_TRY(cudaMemcpyAsync(dSW, c->d_dSW, sizeof(double) * c->sizeC, wk, s));
+    LRES_CUDA_TRY(cudaStreamSynchronize(s));
+    out[0] = N;
+    out[1] = E;
+    out[2] = dNdmu;
+    out[3] = dEdmu;
+    out[4] = kappa;
+    out[5] = (double)st;
+    return LRES_OK;
 }

@@ -258,8 +258,8 @@ int build_F(int nwin, const long long* Xp, const int* Xi, const double* Xv, cons
 // ---------------------------------------------------------------------------
 
 // KLIM = 0: full product.  KLIM = 1: B upper triangular (k <= column).  KLIM = 2: op(A)
-// lower triangular (k <= row) and only the lower triangle of C is needed.
-template <bool TA, int KLIM>
+// lower triangular (k <= row) and only the lower triangle of C is needed.  TB: C = op(A) B^T.
+template <bool TA, int KLIM, bool TB = false>
 __global__ void __launch_bounds__(256) gemm_f64_kernel(const int* n_w, const long long* off, const double* A,
                                                        const double* B, double* C) {
     constexpr int BM = 64, BN = 64, BK = 16;
@@ -286,9 +286,9 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(const int* n_w, const lon
             As[kk][i] = a;
         }
         for (int idx = tid; idx < BK * BN; idx += 256) {
-            const int j = idx / BK, kk = idx % BK;
+            const int j = TB ? idx % BN : idx / BK, kk = TB ? idx / BN : idx % BK;
             const int gj = n0 + j, gk = k0 + kk;
-            Bs[kk][j] = (gj < n && gk < n) ? Bw[gk + (long long)gj * n] : 0.0;
+            Bs[kk][j] = (gj < n && gk < n) ? (TB ? Bw[gj + (long long)gk * n] : Bw[gk + (long long)gj * n]) : 0.0;
         }
         __syncthreads();
 #pragma unroll
@@ -315,10 +315,16 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(const int* n_w, const lon
 }
 
 int batched_gemm(int nwin, const int* n_w, const long long* offA, int nmax, bool transA, const double* A,
-                 const double* B, double* C, cudaStream_t s, int klim) {
+                 const double* B, double* C, cudaStream_t s, int klim, bool transB) {
     if (!nwin) return LRES_OK;
     dim3 grid((nmax + 63) / 64, (nmax + 63) / 64, nwin);
-    if (transA) {
+    if (transB) {
+        if (transA || klim) {
+            lres_set_error("unsupported FP64 GEMM variant");
+            return LRES_EINVAL;
+        }
+        gemm_f64_kernel<false, 0, true><<<grid, 256, 0, s>>>(n_w, offA, A, B, C);
+    } else if (transA) {
         if (klim == 2) gemm_f64_kernel<true, 2><<<grid, 256, 0, s>>>(n_w, offA, A, B, C);
         else gemm_f64_kernel<true, 0><<<grid, 256, 0, s>>>(n_w, offA, A, B, C);
     } else {

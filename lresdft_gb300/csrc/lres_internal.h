@@ -33,7 +33,11 @@ struct LdlJob {
     int grid = 0;
     size_t smem_budget = 0;
     int config = 0;                 // complex kernels: tile configuration (see lres_tune)
+    int keep = 0;                   // complex kernels: keep every item's factor (slot = item index)
 };
+
+// Panel width of the factor kept for the adjoint (the window is padded to a multiple).
+constexpr int kKeepNB64 = 32, kKeepNB128 = 16;
 
 // Tile configurations of the complex pole kernel, index = LdlJob::config:
 //   0: NB 32 (c64) / 16 (c128), 256 threads, k-chunk 32     1: 128 threads
@@ -85,7 +89,7 @@ int build_F(int nwin, const long long* Xp, const int* Xi, const double* Xv, cons
             const int* gptr, const int* gloc, int ngroups, const long long* Ooff, const long long* Oflat,
             const long long* offF, const int* m_w, int mmax, double* F, cudaStream_t s);
 int batched_gemm(int nwin, const int* n_w, const long long* offA, int nmax, bool transA, const double* A,
-                 const double* B, double* C, cudaStream_t s, int klim = 0);
+                 const double* B, double* C, cudaStream_t s, int klim = 0, bool transB = false);
 int convert_f64_f32(const double* a, float* b, long long n, cudaStream_t s);
 int split_f64(const double* a, float2* b, long long n, cudaStream_t s);
 int batched_gemm_df64(int nwin, const int* n_w, const long long* off, int nmax, bool transA, int klim,
@@ -93,6 +97,22 @@ int batched_gemm_df64(int nwin, const int* n_w, const long long* off, int nmax, 
 int pole_sums(int nwin, const long long* offQ, const int* m_w, const long long* Oflat, bool fp32,
               const void* q, long long qstride, int npoles, const double2* wq, const double2* wzq, double dV,
               double* dens, double* n_w, double* e_w, cudaStream_t s);
+
+// Adjoint of the window solve (adjoint.cu)
+int adj_backsolve(bool fp32, const int2* items, int nitems, const int* n_w, const int* m_w, void* ws,
+                  long long ws_stride, int* status, cudaStream_t s);
+int adj_accumulate(bool fp32, const int* wins, int nwin_batch, int P, int nmax, const int* n_w, const int* m_w,
+                   const long long* offC, const void* ws, long long ws_stride, const double2* cw, double* A0,
+                   double* A1, double* A2, cudaStream_t s);
+int adj_weights(int P, int M, double mu, double e_lo, double2* cw, cudaStream_t s);
+int adj_inner(int nwin, const int* n_w, const long long* offC, const double* S, const double* A0, const double* A1,
+              const double* A2, double* u, cudaStream_t s);
+int adj_combine(long long nval, const double* A0, const double* A1, const double* A2, double kappa, double a,
+                double b, double* X, double* Y, cudaStream_t s);
+int adj_block_gather(const BlockPattern& bp, const long long* eoff, const int4* ent, const int* n_w,
+                     const long long* offC, const double* dHW, double* gH, cudaStream_t s);
+int adj_point(long long ng, const long long* poff, const int2* pent, const Supports& sp, const BlockPattern& bp,
+              const double* gH, double dV, double* dv, cudaStream_t s);
 
 struct FFT3;
 int fft3_create(FFT3** out, const int64_t shape[3]);

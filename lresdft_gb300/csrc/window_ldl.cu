@@ -70,6 +70,8 @@ struct LdlParams {
     long long ws_stride;
     int ldp;                    // shared panel leading dimension (>= max n + m)
     int nmax, mmax;
+    int keep;                   // left-looking kernel: one workspace slot per item, the complete
+                                // factor G (diagonal blocks and last panel included) is kept
 };
 
 // Dynamic shared memory attribute and occupancy of a kernel, set/queried only when the
@@ -374,13 +376,14 @@ __global__ void __launch_bounds__(NT, 512 / NT) ldl_left_kernel(LdlParams<T> p) 
     T* accS = qsh + p.mmax;                          // [NB][NT]: the row's running panel values
     __shared__ int item_sh;
     const int tid = threadIdx.x;
-    T* G = p.ws + (size_t)blockIdx.x * p.ws_stride;
+    T* const Gcta = p.ws + (size_t)blockIdx.x * p.ws_stride;
 
     for (;;) {
         if (tid == 0) item_sh = atomicAdd(p.counter, 1);
         __syncthreads();
         const int it = item_sh;
         if (it >= p.nitems) return;
+        T* const G = p.keep ? p.ws + (size_t)it * p.ws_stride : Gcta;
         const int w = p.items[it].x, k = p.items[it].y;
         const int n = p.n_w[w];
         const int m = p.F ? p.m_w[w] : 0;
@@ -527,6 +530,11 @@ __global__ void __launch_bounds__(NT, 512 / NT) ldl_left_kernel(LdlParams<T> p) 
                         __syncwarp();
                         for (int kk = 0; kk < NB; ++kk)
                             if (lane > kk && lane < NB) WL[kk * NB + lane] = E::mul(Dsh[kk], myrow[kk]);
+                        if (p.keep && lane < NB) {     // the block's G = L sqrt(D), lower part
+                            T* gd = G + (j0 + lane) + (long long)j0 * ld;
+                            for (int c = 0; c <= lane; ++c)
+                                gd[(long long)c * ld] = c == lane ? Dsq[c] : E::mul(myrow[c], Dsq[c]);
+                        }
                     }
                     __syncthreads();
                     // warp 0 reloads its parked rows (rows below the block still need the solve)
@@ -550,7 +558,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) ldl_left_kernel(LdlParams<T> p) 
                         for (int kk = 0; kk < NB; ++kk) qv = E::fma(E::mul(acc[kk], acc[kk]), Dsh[kk], qv);
                         qsh[i - np] = qv;
                     }
-                    if (j0 + NB < np) {
+                    if (j0 + NB < np || p.keep) {
                         T* gout = G + i + (long long)j0 * ld;
 #pragma unroll
                         for (int kk = 0; kk < NB; ++kk) gout[(long long)kk * ld] = E::mul(acc[kk], Dsq[kk]);
@@ -1187,6 +1195,8 @@ int run_ldl(const LdlJob& j, cudaStream_t s) {
         p.shifts = (const double2*)j.shifts; p.q = (double2*)j.q; p.qstride = j.qstride;
         p.mult = nullptr; p.npos = j.npos; p.status = j.status;
         p.ws = (double2*)j.ws; p.ws_stride = j.ws_stride; p.ldp = j.ldp; p.nmax = j.nmax; p.mmax = j.mmax;
+        p.keep = j.keep;
+        if (j.keep) return launch_left<double2, kKeepNB128, 256, 32>(p, j.grid, s);
         switch (j.config) {
             case 1: return launch_left<double2, 16, 128, 32>(p, j.grid, s);
             case 2: return launch_left<double2, 16, 256, 16>(p, j.grid, s);
@@ -1203,6 +1213,8 @@ int run_ldl(const LdlJob& j, cudaStream_t s) {
         p.shifts = (const float2*)j.shifts; p.q = (float2*)j.q; p.qstride = j.qstride;
         p.mult = nullptr; p.npos = j.npos; p.status = j.status;
         p.ws = (float2*)j.ws; p.ws_stride = j.ws_stride; p.ldp = j.ldp; p.nmax = j.nmax; p.mmax = j.mmax;
+        p.keep = j.keep;
+        if (j.keep) return launch_left<float2, kKeepNB64, 256, 32>(p, j.grid, s);
         switch (j.config) {
             case 1: return launch_left<float2, 32, 128, 32>(p, j.grid, s);
             case 2: return launch_left<float2, 32, 256, 16>(p, j.grid, s);

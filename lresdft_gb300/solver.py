@@ -180,6 +180,91 @@ class LResGPU:
         _lib.check(_lib.lib.lres_density_ptr(self._ctx, C.byref(p)))
         return p.value
 
+    # ------------------------------------------------------------------ adjoint
+    @property
+    def window_offsets(self):
+        """Offsets of each window's column-major n_W x n_W block in the flat window layout
+        of set_windows / adjoint (windows in the order of ``windows``)."""
+        return np.concatenate([[0], np.cumsum(self.nW.astype(np.int64) ** 2)])
+
+    def window_blocks(self, flat):
+        """Per-window n_W x n_W matrices of a flat window-layout array (views)."""
+        off = self.window_offsets
+        return [flat[off[w]:off[w + 1]].reshape(n, n, order="F") for w, n in enumerate(self.nW)]
+
+    def flatten_windows(self, mats):
+        """Flat window-layout array of per-window matrices."""
+        return np.concatenate([np.asarray(a, np.float64).ravel(order="F") for a in mats])
+
+    def set_windows(self, HW=None, SW=None):
+        """Replace the dense window matrices (flat window layout, host arrays); None keeps one."""
+        h = None if HW is None else _lib.f64(HW)
+        sw = None if SW is None else _lib.f64(SW)
+        _lib.check(_lib.lib.lres_set_windows(self._ctx, None if h is None else h.ctypes.data,
+                                             None if sw is None else sw.ctypes.data, 0, None))
+
+    def window_ptrs(self):
+        """Device addresses of the context's H_W and S_W arrays (flat window layout)."""
+        h, sw = C.c_void_p(), C.c_void_p()
+        _lib.check(_lib.lib.lres_window_ptrs(self._ctx, C.byref(h), C.byref(sw)))
+        return h.value, sw.value
+
+    def set_windows_device(self, HW_ptr=None, SW_ptr=None, stream=None):
+        _lib.check(_lib.lib.lres_set_windows(self._ctx, HW_ptr, SW_ptr, 1, stream))
+
+    def adjoint(self, mu=None, e_lo=None, windows=False):
+        """Gradient of the band energy at fixed N (e_lo fixed) at (mu, e_lo), by default the
+        state of the last density call, on the current Hamiltonian.  Returns a dict with
+        N, E, dN/dmu, dE/dmu, kappa, dv (grid shape) and, with windows=True, the flat
+        window-layout arrays dHW and dSW."""
+        mu = self.mu if mu is None else mu
+        e_lo = self.e_lo if e_lo is None else e_lo
+        if mu is None or e_lo is None:
+            raise RuntimeError("adjoint needs (mu, e_lo): call density() first or pass them")
+        cr = self.b.cr
+        dv = np.empty(cr.ng)
+        size = int(self.window_offsets[-1])
+        dHW = np.empty(size) if windows else None
+        dSW = np.empty(size) if windows else None
+        out = np.zeros(6)
+        _lib.check(_lib.lib.lres_adjoint(self._ctx, float(mu), float(e_lo), dv.ctypes.data, 0,
+                                         None if dHW is None else dHW.ctypes.data,
+                                         None if dSW is None else dSW.ctypes.data, 0, _lib.ptrd(out), None))
+        res = {"N": out[0], "E": out[1], "dNdmu": out[2], "dEdmu": out[3], "kappa": out[4],
+               "dv": dv.reshape(cr.shape), "mu": float(mu), "e_lo": float(e_lo)}
+        if windows:
+            res["dHW"], res["dSW"] = dHW, dSW
+        return res
+
+    def adjoint_device(self, mu, e_lo, dv_ptr=None, dHW_ptr=None, dSW_ptr=None, stream=None):
+        """lres_adjoint into device arrays; returns (N, E, dN/dmu, dE/dmu, kappa)."""
+        out = np.zeros(6)
+        _lib.check(_lib.lib.lres_adjoint(self._ctx, float(mu), float(e_lo), dv_ptr, 1, dHW_ptr, dSW_ptr, 1,
+                                         _lib.ptrd(out), stream))
+        return tuple(float(x) for x in out[:5])
+
+    def solve_mu_fixed_n(self, N=None, mu0=None, tol=1e-10, maxiter=40):
+        """mu with N(mu) = N on the current Hamiltonian, e_lo fixed, by secant steps on full
+        passes until |N(mu) - N| <= tol (absolute).  Returns (mu, N(mu), E_band(mu))."""
+        N = self.b.cr.n_elec if N is None else N
+        mu = self.mu if mu0 is None else mu0
+        if mu is None or self.e_lo is None:
+            raise RuntimeError("solve_mu_fixed_n needs a previous density() call (mu, e_lo)")
+        _, n0, e0 = self.pole_pass(mu, self.e_lo, want_density=False)
+        if abs(n0 - N) <= tol:
+            return mu, n0, e0
+        slope = self._slope if self._slope else 10.0
+        mu1 = mu - (n0 - N) / slope
+        best = (abs(n0 - N), mu, n0, e0)
+        for _ in range(maxiter):
+            _, n1, e1 = self.pole_pass(mu1, self.e_lo, want_density=False)
+            if abs(n1 - N) < best[0]:
+                best = (abs(n1 - N), mu1, n1, e1)
+            if abs(n1 - N) <= tol or n1 == n0:
+                break
+            mu, n0, mu1 = mu1, n1, mu1 - (n1 - N) * (mu1 - mu) / (n1 - n0)
+        return best[1], best[2], best[3]
+
     def set_hamiltonian(self, H):
         Hp, Hi, Hv = csr64(H)
         _lib.check(_lib.lib.lres_set_hamiltonian_csr(self._ctx, _lib.ptr64(Hp), _lib.ptr64(Hi), _lib.ptrd(Hv), None))
