@@ -97,6 +97,27 @@ def cpu_leg(b, v, s, mu, e_lo, workers=None):
     return r
 
 
+def adjoint_leg(s, s64, mu, e_lo):
+    """Band-energy adjoint at fixed N (dE/dv, dE/dH_W, dE/dS_W) on the benchmark potential:
+    wall time of one call through the C ABI (pole pass with kept factors, back-substitution,
+    accumulation, contraction to the grid; host copy of dv) for the mixed and the FP64 path,
+    and the mixed gradient's error against the FP64 one."""
+    out = {}
+    s.adjoint(mu, e_lo)                         # first call: inverse maps and buffers
+    t = time.perf_counter()
+    am = s.adjoint(mu, e_lo)
+    out["mixed_s"] = round(time.perf_counter() - t, 3)
+    t = time.perf_counter()
+    a64 = s64.adjoint(mu, e_lo)
+    out["fp64_s_first_call"] = round(time.perf_counter() - t, 3)
+    out["mixed_speedup"] = round(out["fp64_s_first_call"] / out["mixed_s"], 2)
+    dv, dv64 = am["dv"].ravel(), a64["dv"].ravel()
+    out["mixed_dv_err_rel"] = float(np.max(np.abs(dv - dv64)) / np.max(np.abs(dv64)))
+    out["mixed_kappa_err"] = abs(am["kappa"] - a64["kappa"])
+    out["dv_integral_over_N"] = float(np.sum(dv64) / a64["N"])
+    return out
+
+
 def run_ours(args):
     import torch
     from lresdft_gb300 import LResGPU
@@ -288,6 +309,8 @@ def run_ours(args):
                         "mixed_speedup": round(ms64 / ms_step, 2),
                         "mixed_eband_err_per_e": abs(E32 - E64) / cr.n_elec,
                         "mixed_count_err": abs(N32 - N64)}
+        if args.adjoint:
+            line["adjoint"] = adjoint_leg(s, s64, mu, e_lo)
         s64.close()
 
     # SCF seconds per iteration: the same fixed iteration window from the same start for the
@@ -384,6 +407,8 @@ def main():
     ap.add_argument("--no-fp64-scf", dest="fp64_scf", action="store_false",
                     help="skip the FP64 SCF window (about a minute at 1024 electrons)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-adjoint", dest="adjoint", action="store_false",
+                    help="skip the band-energy adjoint leg (mixed and FP64)")
     ap.add_argument("--cells", type=int, default=8, help="crystal of cells^3 H2 (8 = the benchmark workload)")
     ap.add_argument("--tile-config", type=int, default=None, help="force a pole-kernel tile configuration")
     args = ap.parse_args()

@@ -286,9 +286,10 @@ int setup_standard_form(lres_ctx* c, cudaStream_t s) {
     // A = 1*S - 0 with identity rows: multipliers sqrt(D) D^-1 L^-1 e_r = (L_c^-1)_{:,r}
     int rc = ldl_launch(c, LdlJob::R64, c->nwin, c->d_items_win, nullptr, c->d_SW, I, c->d_n, c->d_offC, one,
                         nullptr, c->d_LinvT, 2 * c->nmax, c->nmax, s);
+    // F^ = F L^-T (owned-point rows in the standard form), any number of rows
     if (!rc)
-        rc = ldl_launch(c, LdlJob::R64, c->nwin, c->d_items_win, nullptr, c->d_SW, c->d_F, c->d_m, c->d_offF, one,
-                        nullptr, Fhat, c->nmax + c->mmax, c->mmax, s);
+        rc = batched_gemm_rect_upper(c->nwin, c->d_n, c->d_m, c->d_offF, c->d_offC, c->nmax, c->mmax, c->d_F,
+                                     c->d_LinvT, Fhat, s);
     if (!rc) rc = convert_f64_f32(Fhat, c->d_Fhat32, c->sizeF, s);
     if (!rc) rc = split_f64(c->d_LinvT, c->d_LinvT_df, c->sizeC, s);
     int st = 0;

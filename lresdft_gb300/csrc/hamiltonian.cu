@@ -314,6 +314,70 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(const int* n_w, const lon
         }
 }
 
+// C_w = A_w U_w with A_w m_w x n_w (column-major, leading dimension m_w, offsets offA) and
+// U_w n_w x n_w upper triangular (column-major, offsets offU): the owned-point rows in the
+// standard form, F^ = F L^-T.
+__global__ void __launch_bounds__(256) gemm_rect_upper_kernel(const int* n_w, const int* m_w, const long long* offA,
+                                                              const long long* offU, const double* A,
+                                                              const double* U, double* C) {
+    constexpr int BM = 64, BN = 64, BK = 16;
+    const int w = blockIdx.z;
+    const int n = n_w[w], m = m_w[w];
+    const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+    if (m0 >= m || n0 >= n) return;
+    const int kend = min(n, n0 + BN);
+    const double* Aw = A + offA[w];
+    const double* Uw = U + offU[w];
+    double* Cw = C + offA[w];
+    __shared__ double As[BK][BM + 1];
+    __shared__ double Bs[BK][BN + 1];
+    const int tid = threadIdx.x;
+    const int tx = tid % 16, ty = tid / 16;
+    double acc[4][4] = {};
+    for (int k0 = 0; k0 < kend; k0 += BK) {
+        for (int idx = tid; idx < BK * BM; idx += 256) {
+            const int kk = idx / BM, i = idx % BM;
+            const int gi = m0 + i, gk = k0 + kk;
+            As[kk][i] = (gi < m && gk < n) ? Aw[gi + (long long)gk * m] : 0.0;
+        }
+        for (int idx = tid; idx < BK * BN; idx += 256) {
+            const int j = idx / BK, kk = idx % BK;
+            const int gj = n0 + j, gk = k0 + kk;
+            Bs[kk][j] = (gj < n && gk <= gj) ? Uw[gk + (long long)gj * n] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < BK; ++kk) {
+            double a[4], b[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) a[u] = As[kk][tx + 16 * u];
+#pragma unroll
+            for (int v = 0; v < 4; ++v) b[v] = Bs[kk][ty + 16 * v];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) acc[u][v] = fma(a[u], b[v], acc[u][v]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const int gi = m0 + tx + 16 * u, gj = n0 + ty + 16 * v;
+            if (gi < m && gj < n) Cw[gi + (long long)gj * m] = acc[u][v];
+        }
+}
+
+int batched_gemm_rect_upper(int nwin, const int* n_w, const int* m_w, const long long* offA, const long long* offU,
+                            int nmax, int mmax, const double* A, const double* U, double* C, cudaStream_t s) {
+    if (!nwin || !mmax) return LRES_OK;
+    dim3 grid((mmax + 63) / 64, (nmax + 63) / 64, nwin);
+    gemm_rect_upper_kernel<<<grid, 256, 0, s>>>(n_w, m_w, offA, offU, A, U, C);
+    LRES_CUDA_TRY(cudaGetLastError());
+    return LRES_OK;
+}
+
 int batched_gemm(int nwin, const int* n_w, const long long* offA, int nmax, bool transA, const double* A,
                  const double* B, double* C, cudaStream_t s, int klim, bool transB) {
     if (!nwin) return LRES_OK;
