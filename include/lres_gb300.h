@@ -196,6 +196,19 @@ int lres_window_ptrs(lres_ctx* ctx, const double** d_HW, const double** d_SW);
 int lres_adjoint(lres_ctx* ctx, double mu, double e_lo, double* dv, int dv_on_device, double* dHW, double* dSW,
                  int dW_on_device, double* out, void* stream);
 
+/* Trace rows — no counterpart in the reference.  N(mu), E_band and the adjoint depend on
+ * the owned-point rows F_W = X[own(B), W] only through F_W^T F_W, so on fine grids
+ * (|own(B)| >> n_W) a factor R_W with R_W^T R_W = F_W^T F_W and at most n_W rows gives the
+ * same sums with far fewer rows.  lres_owned_gram writes K_W = F_W^T F_W (window layout,
+ * n_W x n_W column-major at offC[w]; host or device).  lres_set_trace_rows installs
+ * r_w[w] rows per window, R = the r_w x n_W blocks (column-major, leading dimension r_w[w])
+ * concatenated in window order (host); NULL r_w removes them.  While installed, lres_pass
+ * with dens == NULL and lres_adjoint run over the trace rows (no density is produced and
+ * the context's density array is left as it was); passes that return a density use the
+ * owned points. */
+int lres_owned_gram(lres_ctx* ctx, double* K, int on_device, void* stream);
+int lres_set_trace_rows(lres_ctx* ctx, const int32_t* r_w, const double* R, void* stream);
+
 /* Grid kernels on device arrays of ng doubles (context supplies shape and cell). */
 int lres_lda_xc(lres_ctx* ctx, const double* dens, double* exc, double* vxc, void* stream);
 int lres_hartree(lres_ctx* ctx, const double* dens, double* vh, void* stream);

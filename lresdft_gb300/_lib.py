@@ -19,7 +19,7 @@ ERRORS = {-22: "EINVAL", -12: "ENOMEM", -5: "ECUDA", -33: "ENUMERIC", -71: "ESTA
 EXPORTS = ("lres_version", "lres_last_error", "lres_ctx_create", "lres_ctx_destroy", "lres_set_potential",
            "lres_set_hamiltonian_csr", "lres_pass", "lres_pass_async", "lres_status", "lres_density_ptr", "lres_autotune", "lres_timings", "lres_window_sums", "lres_inertia", "lres_min_eig",
            "lres_voronoi_owner", "lres_lda_xc", "lres_hartree", "lres_ion_potential", "lres_inertia_noalloc",
-           "lres_set_windows", "lres_window_ptrs", "lres_adjoint")
+           "lres_set_windows", "lres_window_ptrs", "lres_adjoint", "lres_owned_gram", "lres_set_trace_rows")
 
 
 class LResError(RuntimeError):
@@ -76,6 +76,8 @@ def _load():
         "lres_set_windows": (i32, [vp, vp, vp, i32, vp]),
         "lres_window_ptrs": (i32, [vp, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
         "lres_adjoint": (i32, [vp, dbl, dbl, vp, i32, vp, vp, i32, PD, vp]),
+        "lres_owned_gram": (i32, [vp, vp, i32, vp]),
+        "lres_set_trace_rows": (i32, [vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

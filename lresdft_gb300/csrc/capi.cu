@@ -96,6 +96,16 @@ struct lres_ctx {
     void* d_q = nullptr;
     double *d_dens = nullptr, *d_nw = nullptr, *d_ew = nullptr, *d_v = nullptr;
     std::vector<double> nw_h, ew_h;
+    // trace rows: r_w x n_w factors R_W with R_W^T R_W = F_W^T F_W, used by passes that need
+    // N and E_band only (no density) and by the adjoint
+    bool have_trace = false;
+    int mmaxT = 0;
+    long long nptsT = 0, sizeFT = 0;
+    int *d_mT = nullptr;
+    long long *d_offFT = nullptr, *d_offQT = nullptr;
+    double* d_FT = nullptr;
+    float* d_FhatT32 = nullptr;
+    void* d_qT = nullptr;
     // host copies kept for the adjoint's inverse maps
     std::vector<long long> soff_h;
     std::vector<int> sgrid_h, wgrp_off_h, wgrp_h, wgrp_lo_h, gloc_h;
@@ -127,7 +137,8 @@ lres_ctx::~lres_ctx() {
                     sp.sval, sp.coff, sp.cslot, d_Sblk, d_Tblk, d_Hblk, d_SW, d_HW, d_F, d_LinvT, d_Y, d_Hhat,
                     d_Hhat32, d_Fhat32, d_LinvT_df, d_H_df, d_Y_df, d_items, d_items_win, d_items_sub, d_counter, d_status, d_npos, d_ws, d_shifts,
                     d_wq, d_wzq, d_q, d_dens, d_nw, d_ew, d_v, d_fftwork, d_adjA[0], d_adjA[1], d_adjA[2],
-                    d_dHW, d_dSW, d_gH, d_adjdv, d_adju, d_cw, d_order, d_eoff, d_poff, d_ent, d_pent, d_adjws};
+                    d_dHW, d_dSW, d_gH, d_adjdv, d_adju, d_cw, d_order, d_eoff, d_poff, d_ent, d_pent, d_adjws,
+                    d_mT, d_offFT, d_offQT, d_FT, d_FhatT32, d_qT};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (fft) fft3_destroy(fft);
@@ -140,7 +151,7 @@ namespace {
 // Runs the fused LDL^T kernel over `items` (device) with the given operands.
 int ldl_launch(lres_ctx* c, LdlJob::Kind kind, int nitems, const int2* items, const void* C, const void* B,
                const void* F, const int* m_w, const long long* offF, const void* shifts, void* q, double* mult,
-               int ldp, int mmax, cudaStream_t s) {
+               int ldp, int mmax, cudaStream_t s, const long long* offQ = nullptr, long long qstride = -1) {
     LdlJob j{};
     j.kind = kind;
     j.nitems = nitems;
@@ -150,13 +161,13 @@ int ldl_launch(lres_ctx* c, LdlJob::Kind kind, int nitems, const int2* items, co
     j.m_w = m_w;
     j.offC = c->d_offC;
     j.offF = offF;
-    j.offQ = c->d_offQ;
+    j.offQ = offQ ? offQ : c->d_offQ;
     j.C = C;
     j.B = B;
     j.F = F;
     j.shifts = shifts;
     j.q = q;
-    j.qstride = c->npts;
+    j.qstride = qstride >= 0 ? qstride : c->npts;
     j.mult = mult;
     j.npos = c->d_npos;
     j.status = c->d_status;
@@ -179,6 +190,26 @@ int ldl_launch(lres_ctx* c, LdlJob::Kind kind, int nitems, const int2* items, co
     j.config = c->config;
     LRES_CUDA_TRY(cudaMemsetAsync(c->d_counter, 0, sizeof(int), s));
     return run_ldl(j, s);
+}
+
+// The owned-row set of a pass: the grid's owned points (density) or the trace rows.
+struct Rows {
+    const int* m;
+    const long long *offF, *offQ, *Oflat;
+    const void* F;            // FP64 rows (LRES_FP64) or standard-form FP32 rows (LRES_MIXED)
+    void* q;
+    long long npts;
+    int mmax;
+    double* dens;
+};
+
+Rows select_rows(lres_ctx* c, bool trace) {
+    const bool mixed = c->precision == LRES_MIXED;
+    if (trace)
+        return Rows{c->d_mT, c->d_offFT, c->d_offQT, nullptr,
+                    mixed ? (const void*)c->d_FhatT32 : (const void*)c->d_FT, c->d_qT, c->nptsT, c->mmaxT, nullptr};
+    return Rows{c->d_m, c->d_offF, c->d_offQ, c->d_Oflat,
+                mixed ? (const void*)c->d_Fhat32 : (const void*)c->d_F, c->d_q, c->npts, c->mmax, c->d_dens};
 }
 
 int read_status(lres_ctx* c, cudaStream_t s, int* st) {
@@ -260,6 +291,20 @@ int after_h_blocks(lres_ctx* c, cudaStream_t s) {
     return LRES_OK;
 }
 
+// Trace rows in the standard form: R^ = R L^-T, FP32.
+int trace_standard_form(lres_ctx* c, cudaStream_t s) {
+    double* tmp = nullptr;
+    TRY(dalloc(&tmp, c->sizeFT));
+    int rc = batched_gemm_rect_upper(c->nwin, c->d_n, c->d_mT, c->d_offFT, c->d_offC, c->nmax, c->mmaxT, c->d_FT,
+                                     c->d_LinvT, tmp, s);
+    if (!rc) rc = convert_f64_f32(tmp, c->d_FhatT32, c->sizeFT, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    cudaFree(tmp);
+    if (rc) return rc;
+    LRES_CUDA_TRY(e);
+    return LRES_OK;
+}
+
 // Standard form of the mixed path from the current S_W: L_c^-1 (stored as L^-T, FP64 and as
 // double-float pairs) and F^ = L_c^-1 F (FP32).  Allocates on the first call.
 int setup_standard_form(lres_ctx* c, cudaStream_t s) {
@@ -291,6 +336,7 @@ int setup_standard_form(lres_ctx* c, cudaStream_t s) {
         rc = batched_gemm_rect_upper(c->nwin, c->d_n, c->d_m, c->d_offF, c->d_offC, c->nmax, c->mmax, c->d_F,
                                      c->d_LinvT, Fhat, s);
     if (!rc) rc = convert_f64_f32(Fhat, c->d_Fhat32, c->sizeF, s);
+    if (!rc && c->have_trace) rc = trace_standard_form(c, s);
     if (!rc) rc = split_f64(c->d_LinvT, c->d_LinvT_df, c->sizeC, s);
     int st = 0;
     if (!rc) rc = read_status(c, s, &st);
@@ -764,17 +810,19 @@ extern "C" int lres_pass(lres_ctx* c, double mu, double e_lo, double* dens, int 
     LRES_CUDA_TRY(cudaGetLastError());
     LRES_CUDA_TRY(cudaMemsetAsync(c->d_status, 0, sizeof(int), s));
     LRES_CUDA_TRY(cudaMemsetAsync(c->d_counter, 0, sizeof(int), s));
+    // no density requested and trace rows installed: the pass over the trace rows
+    const Rows rw = select_rows(c, !dens && c->have_trace);
     TRY(mark(c, 0, 0, s));
     if (mixed)
-        TRY(ldl_launch(c, LdlJob::C64, c->nitems, c->d_items, c->d_Hhat32, nullptr, c->d_Fhat32, c->d_m, c->d_offF,
-                       c->d_shifts, c->d_q, nullptr, c->nmax + c->mmax, c->mmax, s));
+        TRY(ldl_launch(c, LdlJob::C64, c->nitems, c->d_items, c->d_Hhat32, nullptr, rw.F, rw.m, rw.offF,
+                       c->d_shifts, rw.q, nullptr, c->nmax + rw.mmax, rw.mmax, s, rw.offQ, rw.npts));
     else
-        TRY(ldl_launch(c, LdlJob::C128, c->nitems, c->d_items, c->d_HW, c->d_SW, c->d_F, c->d_m, c->d_offF,
-                       c->d_shifts, c->d_q, nullptr, c->nmax + c->mmax, c->mmax, s));
+        TRY(ldl_launch(c, LdlJob::C128, c->nitems, c->d_items, c->d_HW, c->d_SW, rw.F, rw.m, rw.offF,
+                       c->d_shifts, rw.q, nullptr, c->nmax + rw.mmax, rw.mmax, s, rw.offQ, rw.npts));
     TRY(mark(c, 0, 1, s));
     TRY(mark(c, 1, 0, s));
-    TRY(pole_sums(c->nwin, c->d_offQ, c->d_m, c->d_Oflat, mixed, c->d_q, c->npts, P, c->d_wq, c->d_wzq, c->dV,
-                  c->d_dens, c->d_nw, c->d_ew, s));
+    TRY(pole_sums(c->nwin, rw.offQ, rw.m, rw.Oflat, mixed, rw.q, rw.npts, P, c->d_wq, c->d_wzq, c->dV, rw.dens,
+                  c->d_nw, c->d_ew, s));
     TRY(mark(c, 1, 1, s));
     LRES_CUDA_TRY(cudaMemcpyAsync(c->nw_h.data(), c->d_nw, sizeof(double) * c->nwin, cudaMemcpyDeviceToHost, s));
     LRES_CUDA_TRY(cudaMemcpyAsync(c->ew_h.data(), c->d_ew, sizeof(double) * c->nwin, cudaMemcpyDeviceToHost, s));
@@ -1217,7 +1265,8 @@ extern "C" int lres_adjoint(lres_ctx* c, double mu, double e_lo, double* dv, int
     const size_t el = mixed ? 8 : 16;
     const int nbk = mixed ? kKeepNB64 : kKeepNB128;
     const long long npmax = (c->nmax + nbk - 1) / nbk * nbk;
-    const long long stride = ((npmax + c->mmax + 1) * npmax + 15) / 16 * 16;   // elements per item slot
+    const int mrows = c->have_trace ? c->mmaxT : c->mmax;
+    const long long stride = ((npmax + mrows + 1) * npmax + 15) / 16 * 16;   // elements per item slot
     const size_t item_bytes = (size_t)stride * el;
     // items per batch: whole windows (all poles), as many as the free device memory admits
     size_t freeb = 0, totalb = 0;
@@ -1240,6 +1289,7 @@ extern "C" int lres_adjoint(lres_ctx* c, double mu, double e_lo, double* dv, int
         TRY(dalloc((char**)&c->d_adjws, need));
         c->adjws_bytes = need;
     }
+    const Rows rw = select_rows(c, c->have_trace);
     poles_kernel<<<(P + 63) / 64, 64, 0, s>>>(P, c->M, mu, e_lo, mixed ? 1 : 0, c->d_shifts, c->d_wq, c->d_wzq);
     LRES_CUDA_TRY(cudaGetLastError());
     TRY(adj_weights(P, c->M, mu, e_lo, c->d_cw, s));
@@ -1254,35 +1304,35 @@ extern "C" int lres_adjoint(lres_ctx* c, double mu, double e_lo, double* dv, int
         j.items = items;
         j.counter = c->d_counter;
         j.n_w = c->d_n;
-        j.m_w = c->d_m;
+        j.m_w = rw.m;
         j.offC = c->d_offC;
-        j.offF = c->d_offF;
-        j.offQ = c->d_offQ;
+        j.offF = rw.offF;
+        j.offQ = rw.offQ;
         j.C = mixed ? (const void*)c->d_Hhat32 : (const void*)c->d_HW;
         j.B = mixed ? nullptr : (const void*)c->d_SW;
-        j.F = mixed ? (const void*)c->d_Fhat32 : (const void*)c->d_F;
+        j.F = rw.F;
         j.shifts = c->d_shifts;
-        j.q = c->d_q;
-        j.qstride = c->npts;
+        j.q = rw.q;
+        j.qstride = rw.npts;
         j.npos = c->d_npos;
         j.status = c->d_status;
         j.ws = c->d_adjws;
         j.ws_stride = stride;
-        j.ldp = c->nmax + c->mmax;
+        j.ldp = c->nmax + rw.mmax;
         j.nmax = c->nmax;
-        j.mmax = c->mmax;
+        j.mmax = rw.mmax;
         j.grid = nit;
         j.smem_budget = c->smem_budget;
         j.config = 0;
         j.keep = 1;
         LRES_CUDA_TRY(cudaMemsetAsync(c->d_counter, 0, sizeof(int), s));
         TRY(run_ldl(j, s));
-        TRY(adj_backsolve(mixed, items, nit, c->d_n, c->d_m, c->d_adjws, stride, c->d_status, s));
-        TRY(adj_accumulate(mixed, c->d_order + w0, nwb, P, c->nmax, c->d_n, c->d_m, c->d_offC, c->d_adjws, stride,
+        TRY(adj_backsolve(mixed, items, nit, c->d_n, rw.m, c->d_adjws, stride, c->d_status, s));
+        TRY(adj_accumulate(mixed, c->d_order + w0, nwb, P, c->nmax, c->d_n, rw.m, c->d_offC, c->d_adjws, stride,
                            c->d_cw, c->d_adjA[0], c->d_adjA[1], c->d_adjA[2], s));
     }
-    TRY(pole_sums(c->nwin, c->d_offQ, c->d_m, c->d_Oflat, mixed, c->d_q, c->npts, P, c->d_wq, c->d_wzq, c->dV,
-                  c->d_dens, c->d_nw, c->d_ew, s));
+    TRY(pole_sums(c->nwin, rw.offQ, rw.m, rw.Oflat, mixed, rw.q, rw.npts, P, c->d_wq, c->d_wzq, c->dV, rw.dens,
+                  c->d_nw, c->d_ew, s));
     TRY(adj_inner(c->nwin, c->d_n, c->d_offC, mixed ? nullptr : c->d_SW, c->d_adjA[0], c->d_adjA[1], c->d_adjA[2],
                   c->d_adju, s));
     LRES_CUDA_TRY(cudaMemcpyAsync(c->nw_h.data(), c->d_nw, sizeof(double) * c->nwin, cudaMemcpyDeviceToHost, s));
@@ -1344,5 +1394,85 @@ extern "C" int lres_adjoint(lres_ctx* c, double mu, double e_lo, double* dv, int
     out[3] = dEdmu;
     out[4] = kappa;
     out[5] = (double)st;
+    return LRES_OK;
+}
+
+// ---------------------------------------------------------------------------
+// trace rows: N and E_band (and the adjoint) depend on the owned-point rows F_W only
+// through F_W^T F_W, so any R_W with R_W^T R_W = F_W^T F_W (rank <= n_W rows) gives the
+// same sums with fewer rows when the grid is fine
+// ---------------------------------------------------------------------------
+
+extern "C" int lres_owned_gram(lres_ctx* c, double* K, int on_device, void* stream) {
+    if (!c || !K) {
+        lres_set_error("null argument");
+        return LRES_EINVAL;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    double* dK = K;
+    if (!on_device) TRY(dalloc(&dK, c->sizeC));
+    int rc = batched_gram(c->nwin, c->d_n, c->d_m, c->d_offF, c->d_offC, c->nmax, c->d_F, dK, s);
+    if (!rc && !on_device) {
+        cudaError_t e = cudaMemcpyAsync(K, dK, sizeof(double) * c->sizeC, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            lres_set_error("lres_owned_gram: %s", cudaGetErrorString(e));
+            rc = LRES_ECUDA;
+        }
+    }
+    if (!on_device) cudaFree(dK);
+    return rc;
+}
+
+extern "C" int lres_set_trace_rows(lres_ctx* c, const int32_t* r_w, const double* R, void* stream) {
+    if (!c) {
+        lres_set_error("null argument");
+        return LRES_EINVAL;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    LRES_CUDA_TRY(cudaStreamSynchronize(s));
+    for (void* p : {(void*)c->d_mT, (void*)c->d_offFT, (void*)c->d_offQT, (void*)c->d_FT, (void*)c->d_FhatT32,
+                    c->d_qT})
+        if (p) cudaFree(p);
+    c->d_mT = nullptr;
+    c->d_offFT = c->d_offQT = nullptr;
+    c->d_FT = nullptr;
+    c->d_FhatT32 = nullptr;
+    c->d_qT = nullptr;
+    c->have_trace = false;
+    if (!r_w) return LRES_OK;                 // removed
+    if (!R) {
+        lres_set_error("null argument");
+        return LRES_EINVAL;
+    }
+    std::vector<int> m(c->nwin);
+    std::vector<long long> offF(c->nwin + 1, 0), offQ(c->nwin + 1, 0);
+    int mmax = 0;
+    for (int w = 0; w < c->nwin; ++w) {
+        if (r_w[w] < 0 || r_w[w] > c->mmax) {
+            lres_set_error("trace rows of window %d: %d (0..%d allowed)", w, r_w[w], c->mmax);
+            return LRES_EINVAL;
+        }
+        m[w] = r_w[w];
+        mmax = std::max(mmax, m[w]);
+        offF[w + 1] = offF[w] + (long long)m[w] * c->n_w[w];
+        offQ[w + 1] = offQ[w] + m[w];
+    }
+    c->mmaxT = mmax;
+    c->sizeFT = offF[c->nwin];
+    c->nptsT = offQ[c->nwin];
+    std::vector<double> Rh(R, R + c->sizeFT);
+    TRY(upload(&c->d_mT, m, s));
+    TRY(upload(&c->d_offFT, offF, s));
+    TRY(upload(&c->d_offQT, offQ, s));
+    TRY(upload(&c->d_FT, Rh, s));
+    const bool mixed = c->precision == LRES_MIXED;
+    TRY(dalloc((char**)&c->d_qT, (size_t)c->npoles * std::max<long long>(c->nptsT, 1) * (mixed ? 8 : 16)));
+    c->have_trace = true;
+    if (mixed) {
+        TRY(dalloc(&c->d_FhatT32, c->sizeFT));
+        TRY(trace_standard_form(c, s));
+    }
+    LRES_CUDA_TRY(cudaStreamSynchronize(s));
     return LRES_OK;
 }

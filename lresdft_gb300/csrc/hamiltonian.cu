@@ -369,6 +369,65 @@ __global__ void __launch_bounds__(256) gemm_rect_upper_kernel(const int* n_w, co
         }
 }
 
+// K_w = F_w^T F_w (n_w x n_w, column-major at offK) from the owned-point rows F_w (m_w x n_w,
+// leading dimension m_w at offF); lower-triangle tiles computed, mirrored.
+__global__ void __launch_bounds__(256) gram_kernel(const int* n_w, const int* m_w, const long long* offF,
+                                                   const long long* offK, const double* F, double* K) {
+    constexpr int BM = 64, BK = 16;
+    const int w = blockIdx.z;
+    const int n = n_w[w], m = m_w[w];
+    const int a0 = blockIdx.x * BM, b0 = blockIdx.y * BM;
+    if (a0 >= n || b0 >= n || a0 < b0) return;
+    const double* Fw = F + offF[w];
+    double* Kw = K + offK[w];
+    __shared__ double As[BK][BM + 1];
+    __shared__ double Bs[BK][BM + 1];
+    const int tid = threadIdx.x;
+    const int tx = tid % 16, ty = tid / 16;
+    double acc[4][4] = {};
+    for (int r0 = 0; r0 < m; r0 += BK) {
+        for (int idx = tid; idx < BK * BM; idx += 256) {
+            const int kk = idx % BK, i = idx / BK;         // rows contiguous
+            const int r = r0 + kk;
+            As[kk][i] = (r < m && a0 + i < n) ? Fw[r + (long long)(a0 + i) * m] : 0.0;
+            Bs[kk][i] = (r < m && b0 + i < n) ? Fw[r + (long long)(b0 + i) * m] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < BK; ++kk) {
+            double a[4], b[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) a[u] = As[kk][tx + 16 * u];
+#pragma unroll
+            for (int v = 0; v < 4; ++v) b[v] = Bs[kk][ty + 16 * v];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) acc[u][v] = fma(a[u], b[v], acc[u][v]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const int a = a0 + tx + 16 * u, b = b0 + ty + 16 * v;
+            if (a < n && b < n) {
+                Kw[a + (long long)b * n] = acc[u][v];
+                Kw[b + (long long)a * n] = acc[u][v];
+            }
+        }
+}
+
+int batched_gram(int nwin, const int* n_w, const int* m_w, const long long* offF, const long long* offK, int nmax,
+                 const double* F, double* K, cudaStream_t s) {
+    if (!nwin) return LRES_OK;
+    dim3 grid((nmax + 63) / 64, (nmax + 63) / 64, nwin);
+    gram_kernel<<<grid, 256, 0, s>>>(n_w, m_w, offF, offK, F, K);
+    LRES_CUDA_TRY(cudaGetLastError());
+    return LRES_OK;
+}
+
 int batched_gemm_rect_upper(int nwin, const int* n_w, const int* m_w, const long long* offA, const long long* offU,
                             int nmax, int mmax, const double* A, const double* U, double* C, cudaStream_t s) {
     if (!nwin || !mmax) return LRES_OK;
@@ -436,7 +495,7 @@ __global__ void __launch_bounds__(256) pole_sum_kernel(const long long* offQ, co
             ae += b.x * qx - b.y * qy;
         }
         const double nr = 4.0 * an, er = 4.0 * ae;
-        dens[Oflat[base + r]] = nr;
+        if (dens) dens[Oflat[base + r]] = nr;
         sn += nr;
         se += er;
     }

@@ -90,6 +90,8 @@ int build_F(int nwin, const long long* Xp, const int* Xi, const double* Xv, cons
             const long long* offF, const int* m_w, int mmax, double* F, cudaStream_t s);
 int batched_gemm(int nwin, const int* n_w, const long long* offA, int nmax, bool transA, const double* A,
                  const double* B, double* C, cudaStream_t s, int klim = 0, bool transB = false);
+int batched_gram(int nwin, const int* n_w, const int* m_w, const long long* offF, const long long* offK, int nmax,
+                 const double* F, double* K, cudaStream_t s);
 int batched_gemm_rect_upper(int nwin, const int* n_w, const int* m_w, const long long* offA, const long long* offU,
                             int nmax, int mmax, const double* A, const double* U, double* C, cudaStream_t s);
 int convert_f64_f32(const double* a, float* b, long long n, cudaStream_t s);

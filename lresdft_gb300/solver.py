@@ -80,7 +80,7 @@ class LResGPU:
     count and energies)."""
 
     def __init__(self, basis, cells, R_w=12.1, M=64, margin=0.3, nthreads=1, lag_mu=False, reuse_vectors=True,
-                 precision="fp64", tile_config=None):
+                 precision="fp64", tile_config=None, trace_rows="auto"):
         if M % 2:
             raise ValueError("M must be even")
         self.b, self.M, self.margin = basis, M, margin
@@ -132,6 +132,13 @@ class LResGPU:
             self.autotune(0.0, -1.0, config=tile_config)
         self._out = np.zeros(3)
         self.dens_buf = np.zeros(cr.ng)
+        # trace rows (passes that need N and E only): installed when the owned points
+        # outnumber the window functions clearly (fine grids)
+        self._trace = False
+        self.trace_rows = None
+        m_w = np.diff(self.Ooff)
+        if trace_rows is True or (trace_rows == "auto" and m_w.mean() > 1.5 * self.nW.mean()):
+            self.install_trace_rows()
 
     def close(self):
         if getattr(self, "_ctx", None):
@@ -243,6 +250,36 @@ class LResGPU:
                                          _lib.ptrd(out), stream))
         return tuple(float(x) for x in out[:5])
 
+    def owned_gram(self):
+        """K_W = F_W^T F_W of every window (flat window layout), F_W = X[own(B), W]."""
+        K = np.empty(int(self.window_offsets[-1]))
+        _lib.check(_lib.lib.lres_owned_gram(self._ctx, K.ctypes.data, 0, None))
+        return K
+
+    def install_trace_rows(self, rtol=1e-14):
+        """Factor R_W = Lambda^1/2 V^T of K_W = V Lambda V^T (eigenvalues above rtol * max kept)
+        for every window and install it as the trace rows: passes without a density and the
+        adjoint then run over r_W <= n_W rows instead of |own(B)|."""
+        K = self.owned_gram()
+        rows, blocks = [], []
+        for Kw in self.window_blocks(K):
+            lam, V = np.linalg.eigh(Kw)
+            top = lam[-1] if lam.size else 0.0
+            keep = lam > rtol * top if top > 0 else np.zeros(lam.size, bool)
+            R = np.sqrt(lam[keep])[:, None] * V[:, keep].T
+            rows.append(R.shape[0])
+            blocks.append(R.ravel(order="F"))
+        r_w = np.asarray(rows, np.int32)
+        flat = np.ascontiguousarray(np.concatenate(blocks))
+        _lib.check(_lib.lib.lres_set_trace_rows(self._ctx, r_w.ctypes.data, flat.ctypes.data, None))
+        self._trace = True
+        self.trace_rows = r_w
+
+    def remove_trace_rows(self):
+        _lib.check(_lib.lib.lres_set_trace_rows(self._ctx, None, None, None))
+        self._trace = False
+        self.trace_rows = None
+
     def solve_mu_fixed_n(self, N=None, mu0=None, tol=1e-10, maxiter=40):
         """mu with N(mu) = N on the current Hamiltonian, e_lo fixed, by secant steps on full
         passes until |N(mu) - N| <= tol (absolute).  Returns (mu, N(mu), E_band(mu))."""
@@ -336,7 +373,7 @@ class LResGPU:
         hist = []
 
         def f(x):
-            dens, n, eb = self.pole_pass(x, e_lo)
+            dens, n, eb = self.pole_pass(x, e_lo, want_density=not self._trace)
             cache[x] = (dens, eb)
             hist.append((x, n - N))
             return n - N
@@ -477,14 +514,16 @@ class LResGPU:
         if self.mu is not None:
             mu, e_lo = self.mu, self.e_lo
             if self._edge_ok(mu, e_lo):
-                dens, n, eb = self.pole_pass(mu, e_lo)
+                dens, n, eb = self.pole_pass(mu, e_lo, want_density=not self._trace)
                 cnt = n - N
                 if self.lag_mu and abs(cnt) < 0.25:
                     self.mu = mu
+                    dens, eb = self._with_density(mu, e_lo, dens, eb)
                     return dens.reshape(cr.shape), eb, mu
                 if abs(cnt) > tol:
                     mu, dens, eb = self._solve_mu(e_lo, N, ftol, start=(mu, cnt, dens, eb))
                 self.mu = self._mu_last = mu
+                dens, eb = self._with_density(mu, e_lo, dens, eb)
                 return dens.reshape(cr.shape), eb, mu
         # cold path: new filter edge from the smallest window eigenvalue (inertia bisection,
         # bracketed around the previous one when there is one)
@@ -499,7 +538,7 @@ class LResGPU:
         if self._mu_last is not None and self._mu_last > lo:
             # the root of the (monotone) count is unique: start from the previous mu
             try:
-                dens, n, eb = self.pole_pass(self._mu_last, e_lo)
+                dens, n, eb = self.pole_pass(self._mu_last, e_lo, want_density=not self._trace)
                 mu, dens, eb = self._solve_mu(e_lo, N, ftol, start=(self._mu_last, n - N, dens, eb))
                 found = True
             except StaleMu:
@@ -508,4 +547,12 @@ class LResGPU:
             mu, dens, eb = self._solve_mu(e_lo, N, ftol, lo_start=lo)
         self.mu, self.e_lo = mu, e_lo
         self._mu_last = mu
+        dens, eb = self._with_density(mu, e_lo, dens, eb)
         return dens.reshape(cr.shape), eb, mu
+
+    def _with_density(self, mu, e_lo, dens, eb):
+        """The accepted pass's density, or (after trace-row passes) one density pass at mu."""
+        if dens is not None:
+            return dens, eb
+        dens, _, eb = self.pole_pass(mu, e_lo)
+        return dens, eb
