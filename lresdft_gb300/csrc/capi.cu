@@ -171,20 +171,25 @@ int ldl_launch(lres_ctx* c, LdlJob::Kind kind, int nitems, const int2* items, co
     j.mult = mult;
     j.npos = c->d_npos;
     j.status = c->d_status;
-    j.ws = c->d_ws;
     j.ldp = ldp;
     j.nmax = c->nmax;
     j.mmax = mmax;
     const size_t el = kind == LdlJob::C128 ? 16 : 8;
-    const int slots = kind == LdlJob::R64 ? c->nsm : 4 * c->nsm;   // complex: up to 4 CTAs per SM
-    // slots start 16-byte aligned (bulk copies), and hold (n_pad + m + 1) x n_pad complex
-    j.ws_stride = (long long)(c->ws_bytes / el / slots) / 16 * 16;
+    // one workspace slot per resident CTA (complex: up to 4 per SM), never more than items;
+    // slots start 16-byte aligned (bulk copies) and hold (n_pad + m + 1) x n_pad complex
+    const int slots = std::max(1, std::min(nitems, kind == LdlJob::R64 ? c->nsm : 4 * c->nsm));
     const long long nmaxp = (c->nmax + 31) / 32 * 32;   // padded window dimension (complex kernel)
     const long long need = kind == LdlJob::R64 ? (long long)ldp * c->nmax : (nmaxp + mmax + 1) * nmaxp;
-    if (need > j.ws_stride) {
-        lres_set_error("workspace too small");
-        return LRES_EINVAL;
+    j.ws_stride = (need + 15) / 16 * 16;
+    const size_t bytes = (size_t)j.ws_stride * el * slots;
+    if (bytes > c->ws_bytes) {            // grows on demand (an eager call precedes any capture)
+        if (c->d_ws) cudaFree(c->d_ws);
+        c->d_ws = nullptr;
+        c->ws_bytes = 0;
+        TRY(dalloc((char**)&c->d_ws, bytes));
+        c->ws_bytes = bytes;
     }
+    j.ws = c->d_ws;
     j.grid = slots;
     j.smem_budget = c->smem_budget;
     j.config = c->config;
@@ -713,12 +718,7 @@ extern "C" int lres_ctx_create(lres_ctx** out, const lres_system_desc* d, int pr
     LRES_CUDA_TRY(cudaMemsetAsync(c->d_status, 0, sizeof(int), s));
     TRY(dalloc(&c->d_npos, std::max(c->nitems, c->nwin)));
 
-    // workspace: one slot per SM, large enough for (n + n) x n real or (n + m) x n complex
-    const long long nmaxp = (c->nmax + 31) / 32 * 32;
-    const long long ldmax = std::max<long long>(c->nmax + c->mmax, 2LL * c->nmax);
-    const size_t slot = (std::max<size_t>((size_t)ldmax * c->nmax, (size_t)(nmaxp + c->mmax + 1) * nmaxp) + 16) * 16;
-    c->ws_bytes = slot * 4 * c->nsm;
-    TRY(dalloc((char**)&c->d_ws, c->ws_bytes));
+    // workspace of the window kernels: allocated by the first launch that needs it
 
     // ---- standard form for the mixed path
     if (precision == LRES_MIXED) TRY(setup_standard_form(c.get(), s));

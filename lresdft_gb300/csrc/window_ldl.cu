@@ -372,8 +372,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) ldl_left_kernel(LdlParams<T> p) 
     T* Dsh = WL + NB * NB;
     T* Dinv = Dsh + NB;
     T* Dsq = Dinv + NB;
-    T* qsh = Dsq + NB;                               // mmax
-    T* accS = qsh + p.mmax;                          // [NB][NT]: the row's running panel values
+    T* accS = Dsq + NB;                              // [NB][NT]: the row's running panel values
     __shared__ int item_sh;
     const int tid = threadIdx.x;
     T* const Gcta = p.ws + (size_t)blockIdx.x * p.ws_stride;
@@ -401,7 +400,10 @@ __global__ void __launch_bounds__(NT, 512 / NT) ldl_left_kernel(LdlParams<T> p) 
         const R* C = p.C ? p.C + p.offC[w] : nullptr;
         const R* B = p.B ? p.B + p.offC[w] : nullptr;
         const R* F = p.F ? p.F + p.offF[w] : nullptr;
-        for (int r = tid; r < m; r += NT) qsh[r] = E::zero();
+        // quadratic forms accumulate in place in the output (any number of owned rows)
+        T* const qg = p.q ? p.q + (long long)k * p.qstride + p.offQ[w] : nullptr;
+        if (qg)
+            for (int r = tid; r < m; r += NT) qg[r] = E::zero();
         __syncthreads();
 
         for (int j0 = 0; j0 < np; j0 += NB) {
@@ -552,11 +554,11 @@ __global__ void __launch_bounds__(NT, 512 / NT) ldl_left_kernel(LdlParams<T> p) 
                         for (int kk2 = kk + 1; kk2 < NB; ++kk2) acc[kk2] = E::fms(l, WL[kk * NB + kk2], acc[kk2]);
                         acc[kk] = l;
                     }
-                    if (i >= np) {
-                        T qv = qsh[i - np];
+                    if (i >= np && qg) {
+                        T qv = qg[i - np];
 #pragma unroll
                         for (int kk = 0; kk < NB; ++kk) qv = E::fma(E::mul(acc[kk], acc[kk]), Dsh[kk], qv);
-                        qsh[i - np] = qv;
+                        qg[i - np] = qv;
                     }
                     if (j0 + NB < np || p.keep) {
                         T* gout = G + i + (long long)j0 * ld;
@@ -566,10 +568,6 @@ __global__ void __launch_bounds__(NT, 512 / NT) ldl_left_kernel(LdlParams<T> p) 
                 }
             }
             __syncthreads();                          // finished G columns visible to the next panel
-        }
-        if (p.q) {
-            T* qo = p.q + (long long)k * p.qstride + p.offQ[w];
-            for (int r = tid; r < m; r += NT) qo[r] = qsh[r];
         }
         __syncthreads();
     }
@@ -649,7 +647,6 @@ __global__ void __launch_bounds__(128, 1) ldl_left_tc_kernel(LdlParams<float2> p
     T* Dsh = WL + NB * NB;
     T* Dinv = Dsh + NB;
     T* Dsq = Dinv + NB;
-    T* qsh = Dsq + NB;                                  // mmax
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_slot;
     __shared__ int item_sh, bail_sh;
@@ -693,7 +690,10 @@ __global__ void __launch_bounds__(128, 1) ldl_left_tc_kernel(LdlParams<float2> p
         const T z = p.shifts[k];
         const float* C = p.C ? p.C + p.offC[w] : nullptr;
         const float* F = p.F ? p.F + p.offF[w] : nullptr;
-        for (int r = tid; r < m; r += NT) qsh[r] = E::zero();
+        // quadratic forms accumulate in place in the output (any number of owned rows)
+        T* const qg = p.q ? p.q + (long long)k * p.qstride + p.offQ[w] : nullptr;
+        if (qg)
+            for (int r = tid; r < m; r += NT) qg[r] = E::zero();
         __syncthreads();
 
         for (int j0 = 0; j0 < np && !bail_sh; j0 += NB) {
@@ -837,11 +837,11 @@ __global__ void __launch_bounds__(128, 1) ldl_left_tc_kernel(LdlParams<float2> p
                         for (int kk2 = kk + 1; kk2 < NB; ++kk2) acc[kk2] = E::fms(l, WL[kk * NB + kk2], acc[kk2]);
                         acc[kk] = l;
                     }
-                    if (i >= np) {
-                        T qv = qsh[i - np];
+                    if (i >= np && qg) {
+                        T qv = qg[i - np];
 #pragma unroll
                         for (int kk = 0; kk < NB; ++kk) qv = E::fma(E::mul(acc[kk], acc[kk]), Dsh[kk], qv);
-                        qsh[i - np] = qv;
+                        qg[i - np] = qv;
                     }
                     if (j0 + NB < np) {
                         T* gout = G + i + (long long)j0 * ld;
@@ -851,10 +851,6 @@ __global__ void __launch_bounds__(128, 1) ldl_left_tc_kernel(LdlParams<float2> p
                 }
             }
             __syncthreads();
-        }
-        if (p.q && !bail_sh) {
-            T* qo = p.q + (long long)k * p.qstride + p.offQ[w];
-            for (int r = tid; r < m; r += NT) qo[r] = qsh[r];
         }
         __syncthreads();
     }
@@ -904,7 +900,6 @@ __global__ void __launch_bounds__(128, 2) ldl_left_bulk_kernel(LdlParams<T> p) {
     T* Dsh = WL + NB * NB;
     T* Dinv = Dsh + NB;
     T* Dsq = Dinv + NB;
-    T* qsh = Dsq + NB;                               // mmax
     __shared__ __align__(8) uint64_t mbar[2];
     __shared__ int item_sh, bail_sh;
     const int tid = threadIdx.x;
@@ -940,7 +935,10 @@ __global__ void __launch_bounds__(128, 2) ldl_left_bulk_kernel(LdlParams<T> p) {
         const R* C = p.C ? p.C + p.offC[w] : nullptr;
         const R* B = p.B ? p.B + p.offC[w] : nullptr;
         const R* F = p.F ? p.F + p.offF[w] : nullptr;
-        for (int r = tid; r < m; r += NT) qsh[r] = E::zero();
+        // quadratic forms accumulate in place in the output (any number of owned rows)
+        T* const qg = p.q ? p.q + (long long)k * p.qstride + p.offQ[w] : nullptr;
+        if (qg)
+            for (int r = tid; r < m; r += NT) qg[r] = E::zero();
         __syncthreads();
 
         for (int j0 = 0; j0 < np && !bail_sh; j0 += NB) {
@@ -1084,11 +1082,11 @@ __global__ void __launch_bounds__(128, 2) ldl_left_bulk_kernel(LdlParams<T> p) {
                         for (int kk2 = kk + 1; kk2 < NB; ++kk2) acc[kk2] = E::fms(l, WL[kk * NB + kk2], acc[kk2]);
                         acc[kk] = l;
                     }
-                    if (i >= np) {
-                        T qv = qsh[i - np];
+                    if (i >= np && qg) {
+                        T qv = qg[i - np];
 #pragma unroll
                         for (int kk = 0; kk < NB; ++kk) qv = E::fma(E::mul(acc[kk], acc[kk]), Dsh[kk], qv);
-                        qsh[i - np] = qv;
+                        qg[i - np] = qv;
                     }
                     if (j0 + NB < np) {
                         T* gout = G + i + (long long)j0 * ld;
@@ -1099,17 +1097,13 @@ __global__ void __launch_bounds__(128, 2) ldl_left_bulk_kernel(LdlParams<T> p) {
             }
             __syncthreads();                              // G columns of this panel complete
         }
-        if (p.q && !bail_sh) {
-            T* qo = p.q + (long long)k * p.qstride + p.offQ[w];
-            for (int r = tid; r < m; r += NT) qo[r] = qsh[r];
-        }
         __syncthreads();
     }
 }
 
 template <class T, int NB, int KC>
 static int launch_left_bulk(const LdlParams<T>& p, int grid, cudaStream_t s) {
-    const size_t smem = sizeof(T) * ((size_t)2 * KC * 128 + 2 * KC * NB + 32 * (NB + 1) + NB * NB + 3 * NB + p.mmax);
+    const size_t smem = sizeof(T) * ((size_t)2 * KC * 128 + 2 * KC * NB + 32 * (NB + 1) + NB * NB + 3 * NB);
     auto kern = ldl_left_bulk_kernel<T, NB, KC>;
     int per_sm = 0;
     if (int rc = prepare_kernel<ldl_left_bulk_kernel<T, NB, KC>>(128, smem, &per_sm)) return rc;
@@ -1121,7 +1115,7 @@ static int launch_left_bulk(const LdlParams<T>& p, int grid, cudaStream_t s) {
 
 static int launch_left_tc(const LdlParams<float2>& p, int grid, cudaStream_t s) {
     const size_t smem = 2 * (size_t)tc::A_BYTES + 2 * (size_t)tc::B_BYTES +
-                        sizeof(float2) * ((size_t)32 * 33 + 32 * 32 + 3 * 32 + p.mmax);
+                        sizeof(float2) * ((size_t)32 * 33 + 32 * 32 + 3 * 32);
     int per_sm = 0;
     if (int rc = prepare_kernel<ldl_left_tc_kernel>(128, smem, &per_sm)) return rc;
     grid = std::min(grid, device_sms());                // one CTA (one TMEM allocation) per SM
@@ -1132,7 +1126,7 @@ static int launch_left_tc(const LdlParams<float2>& p, int grid, cudaStream_t s) 
 
 template <class T, int NB, int NT, int KC>
 static int launch_left(const LdlParams<T>& p, int grid, cudaStream_t s) {
-    const size_t smem = sizeof(T) * ((size_t)2 * KC * NB + 32 * (NB + 1) + NB * NB + 3 * NB + p.mmax + (size_t)NB * NT);
+    const size_t smem = sizeof(T) * ((size_t)2 * KC * NB + 32 * (NB + 1) + NB * NB + 3 * NB + (size_t)NB * NT);
     auto kern = ldl_left_kernel<T, NB, NT, KC>;
     // persistent grid: as many CTAs as fit on the device, at most one workspace slot each
     int per_sm = 0;

@@ -80,7 +80,7 @@ class LResGPU:
     count and energies)."""
 
     def __init__(self, basis, cells, R_w=12.1, M=64, margin=0.3, nthreads=1, lag_mu=False, reuse_vectors=True,
-                 precision="fp64", tile_config=None, trace_rows="auto"):
+                 precision="fp64", tile_config=None, trace_rows="auto", merge_windows="auto"):
         if M % 2:
             raise ValueError("M must be even")
         self.b, self.M, self.margin = basis, M, margin
@@ -94,6 +94,30 @@ class LResGPU:
         self.Woff = np.concatenate([[0], np.cumsum(self.nW)]).astype(np.int64)
         self.Oflat = np.concatenate(self.own).astype(np.int64)
         self.Ooff = np.concatenate([[0], np.cumsum([len(o) for o in self.own])]).astype(np.int64)
+        # the windows the GPU solves: windows with identical function sets (R_w reaching
+        # across the cell) merged into one with the union of their owned points, since
+        # N, E_band and the density are sums over owned points of the same resolvent
+        cw, cown = self.windows, self.own
+        self._ctx_of = np.arange(len(self.windows))     # solved window of every window
+        if merge_windows:
+            first, groups = {}, []
+            for B, W in enumerate(self.windows):
+                key = W.tobytes()
+                if key not in first:
+                    first[key] = len(groups)
+                    groups.append([])
+                groups[first[key]].append(B)
+            if len(groups) < len(self.windows):
+                for k, gr in enumerate(groups):
+                    self._ctx_of[gr] = k
+                cw = [self.windows[gr[0]] for gr in groups]
+                cown = [np.sort(np.concatenate([self.own[B] for B in gr])) for gr in groups]
+        self.ctx_windows, self.ctx_own = cw, cown
+        self.ctx_nW = np.array([len(W) for W in cw])
+        cWflat = np.concatenate(cw).astype(np.int64)
+        cWoff = np.concatenate([[0], np.cumsum(self.ctx_nW)]).astype(np.int64)
+        cOflat = np.concatenate(cown).astype(np.int64)
+        cOoff = np.concatenate([[0], np.cumsum([len(o) for o in cown])]).astype(np.int64)
         self.gptr = _groups(basis)
         self.mu = self.e_lo = None
         self.passes = 0
@@ -116,14 +140,14 @@ class LResGPU:
             d.Tp, d.Ti, d.Tv = _lib.ptr64(T[0]), _lib.ptr64(T[1]), _lib.ptrd(T[2])
         d.ngroups = len(self.gptr) - 1
         d.gptr = _lib.ptr64(self.gptr)
-        d.nwin = len(self.windows)
-        d.Wflat, d.Woff = _lib.ptr64(self.Wflat), _lib.ptr64(self.Woff)
-        d.Oflat, d.Ooff = _lib.ptr64(self.Oflat), _lib.ptr64(self.Ooff)
+        d.nwin = len(cw)
+        d.Wflat, d.Woff = _lib.ptr64(cWflat), _lib.ptr64(cWoff)
+        d.Oflat, d.Ooff = _lib.ptr64(cOflat), _lib.ptr64(cOoff)
         ctx = C.c_void_p()
         prec = {"fp64": _lib.LRES_FP64, "mixed": _lib.LRES_MIXED}[precision]
         _lib.check(_lib.lib.lres_ctx_create(C.byref(ctx), C.byref(d), prec, M, None))
         self._ctx = ctx
-        self._keep = (X, S, T)      # host arrays referenced by the descriptor during creation
+        self._keep = (X, S, T, cWflat, cWoff, cOflat, cOoff)   # referenced by the descriptor
         # tile configuration of the pole kernel: an index, or "auto" to time all of them on
         # the first Hamiltonian (see autotune); None keeps the library default
         self.tile_config = tile_config
@@ -136,8 +160,8 @@ class LResGPU:
         # outnumber the window functions clearly (fine grids)
         self._trace = False
         self.trace_rows = None
-        m_w = np.diff(self.Ooff)
-        if trace_rows is True or (trace_rows == "auto" and m_w.mean() > 1.5 * self.nW.mean()):
+        m_w = np.diff(cOoff)
+        if trace_rows is True or (trace_rows == "auto" and m_w.mean() > 1.5 * self.ctx_nW.mean()):
             self.install_trace_rows()
 
     def close(self):
@@ -191,13 +215,14 @@ class LResGPU:
     @property
     def window_offsets(self):
         """Offsets of each window's column-major n_W x n_W block in the flat window layout
-        of set_windows / adjoint (windows in the order of ``windows``)."""
-        return np.concatenate([[0], np.cumsum(self.nW.astype(np.int64) ** 2)])
+        of set_windows / adjoint: the windows the GPU solves (``ctx_windows``, which are
+        ``windows`` unless identical windows were merged)."""
+        return np.concatenate([[0], np.cumsum(self.ctx_nW.astype(np.int64) ** 2)])
 
     def window_blocks(self, flat):
         """Per-window n_W x n_W matrices of a flat window-layout array (views)."""
         off = self.window_offsets
-        return [flat[off[w]:off[w + 1]].reshape(n, n, order="F") for w, n in enumerate(self.nW)]
+        return [flat[off[w]:off[w + 1]].reshape(n, n, order="F") for w, n in enumerate(self.ctx_nW)]
 
     def flatten_windows(self, mats):
         """Flat window-layout array of per-window matrices."""
@@ -280,27 +305,45 @@ class LResGPU:
         self._trace = False
         self.trace_rows = None
 
-    def solve_mu_fixed_n(self, N=None, mu0=None, tol=1e-10, maxiter=40):
-        """mu with N(mu) = N on the current Hamiltonian, e_lo fixed, by secant steps on full
-        passes until |N(mu) - N| <= tol (absolute).  Returns (mu, N(mu), E_band(mu))."""
+    def solve_mu_fixed_n(self, N=None, mu0=None, tol=1e-10, maxiter=60):
+        """mu with |N(mu) - N| <= tol (absolute) on the current Hamiltonian, e_lo fixed: a
+        bracket grown from mu0 (default: the current mu) by steps of the stored slope, then
+        Brent's method, on passes without density.  Returns (mu, N(mu), E_band(mu))."""
         N = self.b.cr.n_elec if N is None else N
         mu = self.mu if mu0 is None else mu0
         if mu is None or self.e_lo is None:
-            raise RuntimeError("solve_mu_fixed_n needs a previous density() call (mu, e_lo)")
-        _, n0, e0 = self.pole_pass(mu, self.e_lo, want_density=False)
-        if abs(n0 - N) <= tol:
-            return mu, n0, e0
-        slope = self._slope if self._slope else 10.0
-        mu1 = mu - (n0 - N) / slope
-        best = (abs(n0 - N), mu, n0, e0)
+            raise RuntimeError("solve_mu_fixed_n needs (mu, e_lo): call density() first or set them")
+        lo_bound = self.e_lo + 1e-6
+        mu = max(mu, lo_bound + 1e-6)
+        cache = {}
+
+        def f(x):
+            _, n, e = self.pole_pass(x, self.e_lo, want_density=False)
+            cache[x] = (n, e)
+            return n - N
+
+        f0 = f(mu)
+        if abs(f0) <= tol:
+            return mu, cache[mu][0], cache[mu][1]
+        slope = self._slope if self._slope and self._slope > 0 else max(N, 1.0)
+        step = min(max(abs(f0) / slope, 1e-6), 0.1)
+        a, fa = mu, f0
         for _ in range(maxiter):
-            _, n1, e1 = self.pole_pass(mu1, self.e_lo, want_density=False)
-            if abs(n1 - N) < best[0]:
-                best = (abs(n1 - N), mu1, n1, e1)
-            if abs(n1 - N) <= tol or n1 == n0:
+            x = a - step if fa > 0 else a + step
+            if x <= lo_bound:
+                x = 0.5 * (a + lo_bound)
+            fx = f(x)
+            if abs(fx) <= tol:
+                return x, cache[x][0], cache[x][1]
+            if (fx > 0) != (fa > 0):
+                b, fb = x, fx
                 break
-            mu, n0, mu1 = mu1, n1, mu1 - (n1 - N) * (mu1 - mu) / (n1 - n0)
-        return best[1], best[2], best[3]
+            a, fa = x, fx
+            step *= 2.0
+        else:
+            raise RuntimeError("solve_mu_fixed_n: no sign change of N(mu) - N")
+        x = self._brent(f, a, fa, b, fb, tol, xtol=1e-15, maxit=maxiter)
+        return x, cache[x][0], cache[x][1]
 
     def set_hamiltonian(self, H):
         Hp, Hi, Hv = csr64(H)
@@ -333,8 +376,8 @@ class LResGPU:
         return dict(zip(("pole_kernel", "pole_sums", "assemble_h", "gather", "transform", "inertia"), ms))
 
     def window_sums(self):
-        nw = np.empty(len(self.windows))
-        ew = np.empty(len(self.windows))
+        nw = np.empty(len(self.ctx_windows))
+        ew = np.empty(len(self.ctx_windows))
         _lib.check(_lib.lib.lres_window_sums(self._ctx, _lib.ptrd(nw), _lib.ptrd(ew)))
         return nw, ew
 
@@ -342,10 +385,12 @@ class LResGPU:
         """Number of window eigenvalues below sigma (total, or per window)."""
         self.inertia_calls += 1
         tot = C.c_int64()
-        below = np.empty(len(self.windows), np.int32) if per_window else None
+        below = np.empty(len(self.ctx_windows), np.int32) if per_window else None
         bp = below.ctypes.data_as(C.POINTER(C.c_int32)) if per_window else None
         _lib.check(_lib.lib.lres_inertia(self._ctx, float(sigma), bp, C.byref(tot), None))
-        return below if per_window else int(tot.value)
+        # per window of ``windows`` (merged windows share their count); the total counts
+        # each solved window once
+        return below[self._ctx_of] if per_window else int(tot.value)
 
     def min_eig(self, lo, hi, tol=1e-12):
         out = C.c_double()
@@ -514,7 +559,8 @@ class LResGPU:
         if self.mu is not None:
             mu, e_lo = self.mu, self.e_lo
             if self._edge_ok(mu, e_lo):
-                dens, n, eb = self.pole_pass(mu, e_lo, want_density=not self._trace)
+                # with density: when mu is kept (the common warm case) this is the only pass
+                dens, n, eb = self.pole_pass(mu, e_lo)
                 cnt = n - N
                 if self.lag_mu and abs(cnt) < 0.25:
                     self.mu = mu

@@ -58,6 +58,7 @@ def test_adjoint_matches_oracle(cubic3, precision):
     s = _solver(b, cr, g, precision)
     v = g["v"].reshape(cr.shape)
     mu, e_lo, M = float(g["cold_mu"]), float(g["cold_elo"]), int(g["M"])
+    assert len(s.ctx_nW) == len(s.nW)           # no identical windows on this cell
     s.set_potential(v)
     a = s.adjoint(mu, e_lo, windows=True)
     o = _oracle(b, cr, s, v, mu, e_lo, M)
@@ -97,7 +98,7 @@ def _sym_dirs(s, n, seed):
     out = []
     for _ in range(n):
         mats = []
-        for nw in s.nW:
+        for nw in s.ctx_nW:
             x = rng.normal(size=(nw, nw))
             mats.append(x + x.T)
         flat = s.flatten_windows(mats)

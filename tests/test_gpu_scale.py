@@ -1,0 +1,131 @@
+"""Adjoint at the scale of the 6x6x6 adjoint workload: H2 crystal of 432 electrons, a = 4.5
+bohr, bond 1.4, centres jittered U(+-0.1) with random axes (seed 0), grid spacing 0.25 bohr
+(108^3 points), R_w = 8, M = 64.  Opt-in (about ten GPU-minutes): LRES_SCALE_TESTS=1.
+
+* FP64 adjoint against central finite differences (step 1e-5) along 20 seeded directions each:
+  smooth unit-RMS potential fields with mu re-solved at fixed N (secant passes over the trace
+  rows to 1e-10 electrons, first-order remainder removed with kappa), and random symmetric
+  perturbations of all window Hamiltonians / overlaps, unit Frobenius norm in every window, at
+  the unperturbed mu, where dE|_N = dE|_mu - kappa dN|_mu is exact to second order.  Gate: 1e-6
+  relative (norm over the 20 directions).  With directions of unit norm over all 432 windows
+  together the S_W derivatives are ~20x smaller and the FP64 rounding of E_band (~1e-13 Ha over
+  h = 1e-5) limits the agreement to ~3e-6.
+* Mixed against FP64 gradients (dv, dH_W, dS_W, kappa).
+* R_w = 30 (every window the whole cell, merged into one window of 2592 functions with all
+  1.26 M grid points as owned rows, solved over its trace rows): the FP64 window gradient
+  equals the dense-KS density-matrix gradient (oracle, scipy generalised eigh), 1e-9."""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = [pytest.mark.gpu,
+              pytest.mark.skipif(not os.environ.get("LRES_SCALE_TESTS"), reason="opt-in: LRES_SCALE_TESTS=1")]
+
+H_FD = 1e-5
+NDIR = 20
+
+
+@pytest.fixture(scope="module")
+def big():
+    from lresdft_gb300 import LResGPU, system
+    from lresdft_gb300.scf import GridOps
+    cr = system.jittered_h2((6, 6, 6), a=4.5, bond=1.4, pts_per_cell=18, jitter=0.1, seed=0)
+    b = system.LCAOBasis(cr)
+    s = LResGPU(b, cr.pos, R_w=8.0, M=64, precision="fp64", tile_config=3)
+    go = GridOps(s)
+    d0 = np.full(cr.shape, cr.n_elec / (cr.ng * cr.dV))
+    exc, vxc, vh = go.lda_hartree(d0)
+    v = go.ion_potential() + vh + vxc
+    return cr, b, s, v
+
+
+def _rel(a, b):
+    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+
+def test_scale_fd_and_mixed(big):
+    from lresdft_gb300 import LResGPU
+    cr, b, s, v = big
+    assert s.trace_rows is not None
+    N0 = float(cr.n_elec)
+    s.density(v)
+    mu0, _, _ = s.solve_mu_fixed_n(tol=1e-10)
+    s.mu = mu0
+    e_lo = s.e_lo
+    base = s.adjoint(mu0, e_lo, windows=True)
+    kap = base["kappa"]
+    # mixed against FP64 at the same (mu, e_lo)
+    sm = LResGPU(b, cr.pos, R_w=8.0, M=64, precision="mixed")
+    sm.set_potential(v)
+    am = sm.adjoint(mu0, e_lo, windows=True)
+    mixed = {"dv": _rel(am["dv"], base["dv"]), "dHW": _rel(am["dHW"], base["dHW"]),
+             "dSW": _rel(am["dSW"], base["dSW"]), "kappa": abs(am["kappa"] - kap) / abs(kap)}
+    print("mixed vs fp64", mixed)
+    sm.close()
+    assert max(mixed.values()) < 1e-4
+    from lresdft_gb300.autograd import window_matrices
+    HW0, SW0 = [t.cpu().numpy() for t in window_matrices(s)]
+    rng = np.random.default_rng(4)
+    I, J, K = np.meshgrid(*[np.arange(m) for m in cr.shape], indexing="ij")
+    errs = {}
+    for kind in ("v", "H", "S"):
+        fd, an = [], []
+        for _ in range(NDIR):
+            e = []
+            if kind == "v":
+                d = np.zeros(cr.shape)
+                for _ in range(4):
+                    kv = rng.integers(-2, 3, 3)
+                    d += rng.normal() * np.cos(2 * np.pi * (kv[0] * I + kv[1] * J + kv[2] * K) / cr.shape[0]
+                                               + rng.uniform(0, 2 * np.pi))
+                d += 0.3 * rng.normal(size=cr.shape)
+                d /= np.sqrt(np.mean(d ** 2))
+                for sg in (1, -1):
+                    s.set_potential(v + sg * H_FD * d)
+                    mu, N, E = s.solve_mu_fixed_n(mu0=mu0, tol=1e-10)
+                    e.append(E - kap * (N - N0))
+                an.append(float(np.dot(base["dv"].ravel(), d.ravel())))
+            else:
+                mats = []
+                for nw in s.ctx_nW:
+                    x = rng.normal(size=(nw, nw))
+                    x = x + x.T
+                    mats.append(x / np.linalg.norm(x))    # unit Frobenius norm in every window
+                d = s.flatten_windows(mats)
+                for sg in (1, -1):
+                    if kind == "H":
+                        s.set_windows(HW=HW0 + sg * H_FD * d)
+                    else:
+                        s.set_windows(HW=HW0, SW=SW0 + sg * H_FD * d)
+                    _, N, E = s.pole_pass(mu0, e_lo, want_density=False)
+                    e.append(E - kap * N)
+                an.append(float(np.dot(base["dHW" if kind == "H" else "dSW"], d)))
+            fd.append((e[0] - e[1]) / (2 * H_FD))
+        s.set_windows(HW=HW0, SW=SW0)
+        fd, an = np.array(fd), np.array(an)
+        errs[kind] = float(np.linalg.norm(fd - an) / np.linalg.norm(an))
+    print("finite differences, relative error over", NDIR, "directions:", errs)
+    assert max(errs.values()) < 1e-6, errs
+
+
+def test_scale_whole_cell_equals_dense_ks(big):
+    from lresdft_gb300 import LResGPU
+    from oracle.lrft_adjoint import dense_ks_gradient
+    cr, b, s8, v = big
+    s = LResGPU(b, cr.pos, R_w=30.0, M=64, precision="fp64", tile_config=3)
+    assert len(s.ctx_windows) == 1 and s.ctx_nW[0] == b.nb and s.trace_rows is not None
+    s.set_potential(v)
+    lam_min = s.min_eig(-1.0, 0.0, tol=1e-10)
+    s.e_lo = lam_min - 0.3
+    s.mu = s8.mu if s8.mu is not None else lam_min + 0.4
+    mu, N, E = s.solve_mu_fixed_n(tol=1e-9)
+    a = s.adjoint(mu, s.e_lo, windows=True)
+    H = b.H(v.ravel())
+    G, kap = dense_ks_gradient(H, b.S, cr.n_elec, cr.dV, mu, s.e_lo, 64)
+    gw = s.window_blocks(a["dHW"])[0]
+    dv_ks = cr.dV * np.asarray(b.Xr.multiply(b.Xr @ G).sum(axis=1)).ravel()
+    errs = (abs(a["kappa"] - kap) / abs(kap), _rel(gw, G), _rel(a["dv"].ravel(), dv_ks))
+    print("R_w = 30 vs dense KS: kappa, dH, dv", errs, "N", N)
+    assert max(errs) < 1e-9, errs
+    s.close()

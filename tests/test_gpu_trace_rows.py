@@ -39,7 +39,7 @@ def test_trace_rows_give_same_sums_and_gradient(cubic3, precision):
     v = g["v"].reshape(cr.shape)
     full = _solver(b, cr, R_w, M, precision, False)
     tr = _solver(b, cr, R_w, M, precision, True)
-    assert tr.trace_rows is not None and np.all(tr.trace_rows <= tr.nW)
+    assert tr.trace_rows is not None and np.all(tr.trace_rows <= tr.ctx_nW)
     for s in (full, tr):
         s.set_potential(v)
     _, N0, E0 = full.pole_pass(mu, e_lo, want_density=False)
