@@ -20,6 +20,7 @@ template <> struct El<double> {
     __device__ __forceinline__ static double fma(double a, double b, double c) { return ::fma(a, b, c); }
     __device__ __forceinline__ static double fms(double a, double b, double c) { return ::fma(-a, b, c); }   // c - a*b
     __device__ __forceinline__ static double sub(double a, double b) { return a - b; }
+    __device__ __forceinline__ static double add(double a, double b) { return a + b; }
     __device__ __forceinline__ static double inv(double a) { return 1.0 / a; }
     __device__ __forceinline__ static double scale(double a, double s) { return a * s; }
     __device__ __forceinline__ static double re(double a) { return a; }
@@ -47,6 +48,7 @@ template <> struct El<double2> {
         return c;
     }
     __device__ __forceinline__ static double2 sub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+    __device__ __forceinline__ static double2 add(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
     __device__ __forceinline__ static double2 inv(double2 a) {
         // 1/a with one rescaling to keep |a|^2 in range
         double s = fmax(fabs(a.x), fabs(a.y));
@@ -93,6 +95,7 @@ template <> struct El<float2> {
         return c;
     }
     __device__ __forceinline__ static float2 sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+    __device__ __forceinline__ static float2 add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
     __device__ __forceinline__ static float2 inv(float2 a) {
         float s = fmaxf(fabsf(a.x), fabsf(a.y));
         float ax = a.x / s, ay = a.y / s;

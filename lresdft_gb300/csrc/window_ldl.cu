@@ -555,10 +555,12 @@ __global__ void __launch_bounds__(NT, 512 / NT) ldl_left_kernel(LdlParams<T> p) 
                         acc[kk] = l;
                     }
                     if (i >= np && qg) {
-                        T qv = qg[i - np];
+                        // the panel's NB terms of the quadratic form summed from zero, then added
+                        // (blocked summation: one FP32 chain over all n terms loses ~10x accuracy)
+                        T part = E::zero();
 #pragma unroll
-                        for (int kk = 0; kk < NB; ++kk) qv = E::fma(E::mul(acc[kk], acc[kk]), Dsh[kk], qv);
-                        qg[i - np] = qv;
+                        for (int kk = 0; kk < NB; ++kk) part = E::fma(E::mul(acc[kk], acc[kk]), Dsh[kk], part);
+                        qg[i - np] = E::add(qg[i - np], part);
                     }
                     if (j0 + NB < np || p.keep) {
                         T* gout = G + i + (long long)j0 * ld;
@@ -838,10 +840,12 @@ __global__ void __launch_bounds__(128, 1) ldl_left_tc_kernel(LdlParams<float2> p
                         acc[kk] = l;
                     }
                     if (i >= np && qg) {
-                        T qv = qg[i - np];
+                        // the panel's NB terms of the quadratic form summed from zero, then added
+                        // (blocked summation: one FP32 chain over all n terms loses ~10x accuracy)
+                        T part = E::zero();
 #pragma unroll
-                        for (int kk = 0; kk < NB; ++kk) qv = E::fma(E::mul(acc[kk], acc[kk]), Dsh[kk], qv);
-                        qg[i - np] = qv;
+                        for (int kk = 0; kk < NB; ++kk) part = E::fma(E::mul(acc[kk], acc[kk]), Dsh[kk], part);
+                        qg[i - np] = E::add(qg[i - np], part);
                     }
                     if (j0 + NB < np) {
                         T* gout = G + i + (long long)j0 * ld;
@@ -1083,10 +1087,12 @@ __global__ void __launch_bounds__(128, 2) ldl_left_bulk_kernel(LdlParams<T> p) {
                         acc[kk] = l;
                     }
                     if (i >= np && qg) {
-                        T qv = qg[i - np];
+                        // the panel's NB terms of the quadratic form summed from zero, then added
+                        // (blocked summation: one FP32 chain over all n terms loses ~10x accuracy)
+                        T part = E::zero();
 #pragma unroll
-                        for (int kk = 0; kk < NB; ++kk) qv = E::fma(E::mul(acc[kk], acc[kk]), Dsh[kk], qv);
-                        qg[i - np] = qv;
+                        for (int kk = 0; kk < NB; ++kk) part = E::fma(E::mul(acc[kk], acc[kk]), Dsh[kk], part);
+                        qg[i - np] = E::add(qg[i - np], part);
                     }
                     if (j0 + NB < np) {
                         T* gout = G + i + (long long)j0 * ld;

@@ -1,6 +1,7 @@
 """Adjoint at the scale of the 6x6x6 adjoint workload: H2 crystal of 432 electrons, a = 4.5
 bohr, bond 1.4, centres jittered U(+-0.1) with random axes (seed 0), grid spacing 0.25 bohr
-(108^3 points), R_w = 8, M = 64.  Opt-in (about ten GPU-minutes): LRES_SCALE_TESTS=1.
+(108^3 points), R_w = 8, M = 64.  Opt-in (LRES_SCALE_TESTS=1); also the 1024-electron amorphous cell at M = 32, 64, 128 and
+the 2000-electron crystals at M = 128, mixed against complex128.
 
 * FP64 adjoint against central finite differences (step 1e-5) along 20 seeded directions each:
   smooth unit-RMS potential fields with mu re-solved at fixed N (secant passes over the trace
@@ -129,3 +130,58 @@ def test_scale_whole_cell_equals_dense_ks(big):
     print("R_w = 30 vs dense KS: kappa, dH, dv", errs, "N", N)
     assert max(errs) < 1e-9, errs
     s.close()
+
+
+def _pass_pair(b, cells, R_w, M, v, fp64=True):
+    """Mixed density call for (mu, e_lo), then one FP64 and one mixed pass there; returns the
+    mixed errors against FP64 and the pass times."""
+    import time
+    from lresdft_gb300 import LResGPU
+    cr = b.cr
+    sm = LResGPU(b, cells, R_w=R_w, M=M, precision="mixed", tile_config=1)
+    sm.density(v)
+    mu, e_lo = sm.mu, sm.e_lo
+    t = time.perf_counter()
+    dm, Nm, Em = sm.pole_pass(mu, e_lo)
+    out = {"nW": (int(sm.nW.min()), int(sm.nW.max())), "mixed_pass_s": time.perf_counter() - t, "mu": mu}
+    sm.close()
+    if fp64:
+        s64 = LResGPU(b, cells, R_w=R_w, M=M, precision="fp64", tile_config=3)
+        s64.set_potential(v)
+        t = time.perf_counter()
+        d64, N64, E64 = s64.pole_pass(mu, e_lo)
+        out["fp64_pass_s"] = time.perf_counter() - t
+        s64.close()
+        out["eband_err_per_e"] = abs(Em - E64) / cr.n_elec
+        out["count_err"] = abs(Nm - N64)
+        out["dens_l2_per_e"] = float(np.sqrt(np.sum((dm - d64) ** 2) * cr.dV) / cr.n_elec)
+    return out
+
+
+@pytest.mark.parametrize("M", [32, 64, 128])
+def test_scale_amorphous_1024(M):
+    """512 H2 by random sequential addition (d_min 3 bohr, 36^3 bohr box, 0.6 bohr grid), one
+    window per atom, R_w = 8: uneven windows, mixed against complex128 at M = 32, 64, 128."""
+    from lresdft_gb300 import system
+    from oracle.lrft_oracle import guess_potential
+    cr, centres = system.amorphous_h2(nmol=512, box=36.0, dmin=3.0, seed=7)
+    b = system.LCAOBasis(cr)
+    r = _pass_pair(b, cr.pos, 8.0, M, guess_potential(cr))
+    print("amorphous 1024 e, M =", M, r)
+    assert r["nW"][1] > 1.5 * r["nW"][0]
+    assert r["eband_err_per_e"] < 2e-7
+
+
+@pytest.mark.parametrize("a,R_w,fp64", [(4.5, 6.0, True), (4.5, 8.0, True), (4.5, 10.0, True),
+                                        (3.6, 6.0, True), (3.6, 8.0, False)])
+def test_scale_2000_electrons(a, R_w, fp64):
+    """10x10x10 H2 (2000 electrons, 80^3 grid), M = 128: mixed against complex128 (the largest
+    compressed windows, ~540 functions at a = 3.6, R_w = 8, are timed in mixed precision only)."""
+    from lresdft_gb300 import system
+    from oracle.lrft_oracle import guess_potential
+    cr = system.jittered_h2((10, 10, 10), a=a, bond=1.4, pts_per_cell=8, jitter=0.1, seed=0)
+    b = system.LCAOBasis(cr)
+    r = _pass_pair(b, cr.pos, R_w, 128, guess_potential(cr), fp64=fp64)
+    print("10x10x10 a =", a, "R_w =", R_w, r)
+    if fp64:
+        assert r["eband_err_per_e"] < 2e-7
