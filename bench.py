@@ -309,6 +309,19 @@ def run_ours(args):
                         "mixed_speedup": round(ms64 / ms_step, 2),
                         "mixed_eband_err_per_e": abs(E32 - E64) / cr.n_elec,
                         "mixed_count_err": abs(N32 - N64)}
+        # the tensor-core configuration (tcgen05, 3xTF32) on the same pass, against FP64
+        try:
+            s.autotune(mu, e_lo, config=4)
+            s.pole_pass(mu, e_lo)
+            _, Ntc, Etc = s.pole_pass(mu, e_lo)
+            line["tensor_core"] = {"tile_config": 4, "kernel_ms": round(s.timings()["pole_kernel"], 2),
+                                   "eband_err_per_e_vs_fp64": abs(Etc - E64) / cr.n_elec,
+                                   "count_err_vs_fp64": abs(Ntc - N64),
+                                   "note": "tcgen05.mma kind::tf32, 3xTF32 split; forced only (not auto-selected)"}
+        except Exception as exc:
+            line["tensor_core"] = {"error": str(exc)[:200]}
+        finally:
+            s.autotune(mu, e_lo, config=s.tile_config if isinstance(s.tile_config, int) else 1)
         if args.adjoint:
             line["adjoint"] = adjoint_leg(s, s64, mu, e_lo)
         s64.close()

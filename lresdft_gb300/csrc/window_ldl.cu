@@ -83,6 +83,9 @@ static int prepare_kernel(int threads, size_t smem, int* per_sm) {
     static int cached_per_sm = 0;
     if (smem > set_smem) {
         LRES_CUDA_TRY(cudaFuncSetAttribute(Kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        // prefer the largest shared-memory carveout, so that the occupancy below is the maximum
+        LRES_CUDA_TRY(cudaFuncSetAttribute(Kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                           (int)cudaSharedmemCarveoutMaxShared));
         LRES_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cached_per_sm, Kern, threads, smem));
         set_smem = smem;
     }
@@ -578,21 +581,29 @@ __global__ void __launch_bounds__(NT, 512 / NT) ldl_left_kernel(LdlParams<T> p) 
 // ---------------------------------------------------------------------------
 // Tensor-core variant of the left-looking kernel (complex FP32 path, tile configuration 4).
 //
-// The panel update of a 32-column chunk, tmp[r, c] = sum_k g[r, k] b[c, k] (complex), is a
-// real GEMM  [Re g | Im g] (128 x 64) . B' (64 x 64)  with B' built from the panel's G rows
+// The panel update of a 16-column chunk, tmp[r, c] = sum_k g[r, k] b[c, k] (complex), is a
+// real GEMM  [Re g | Im g] (128 x 32) . B' (64 x 32)^T  with B' built from the panel's G rows
 // ([b_re, -b_im ; b_im, b_re] per complex entry), run on the 5th-generation tensor cores:
-// operands in shared memory (K-major, no swizzle, 8 x 16-byte core matrices), accumulator
-// in tensor memory, tcgen05.mma issued by one thread, completion through an mbarrier.
-// FP32 accuracy from TF32 operands by the 3xTF32 split x = hi + lo (hi, lo rounded to
-// TF32): hi.hi + hi.lo + lo.hi, each chunk accumulated from zero in FP32 and subtracted
-// from the row's running value in registers (blocked summation, as the SIMT kernel).
-// 128 threads = 128 rows = 128 TMEM lanes; thread t reads its row with tcgen05.ld.
+// operands in shared memory (K-major, no swizzle, 8 x 16-byte core matrices), accumulator in
+// tensor memory, tcgen05.mma issued by one thread, completion through an mbarrier.  FP32
+// accuracy from TF32 operands by the 3xTF32 split x = hi + lo: hi.hi + hi.lo + lo.hi, each
+// chunk accumulated from zero in FP32 and subtracted from the row's running value in
+// registers (blocked summation, as the SIMT kernel).
+//
+// Pipeline: two shared-memory stages and two TMEM accumulators.  While the tensor core runs
+// the MMAs of chunk c+1, the threads read back chunk c and split/stage chunk c+2, whose
+// operands were loaded into registers two chunks earlier.  128 threads = 128 rows = 128 TMEM
+// lanes; two CTAs per SM, so that one CTA's panel factorisation overlaps the other's MMAs.
+// Every wait on an mbarrier is bounded: on a timeout the kernel sets ST_TIMEOUT, waits
+// (bounded) for the MMAs it has in flight, frees its tensor memory and returns.
 // ---------------------------------------------------------------------------
 namespace tc {
-constexpr int M = 128, N = 64, KR = 64;             // real GEMM per chunk
+constexpr int M = 128, N = 64, KR = 32, KCC = 16;   // real GEMM per chunk; complex columns per chunk
 constexpr int LBO = 128;                             // bytes between core matrices along K
 constexpr int SBO = (KR / 4) * 128;                  // bytes between 8-row groups
 constexpr int A_BYTES = M * KR * 4, B_BYTES = N * KR * 4;
+constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;   // Ahi, Alo, Bhi, Blo
+constexpr int TMEM_COLS = 128;                       // two 64-column accumulators
 __device__ __forceinline__ int off(int row, int k) { return (row >> 3) * SBO + (k >> 2) * LBO + (row & 7) * 16 + (k & 3) * 4; }
 __device__ __forceinline__ uint64_t desc(uint32_t saddr) {
     return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)((LBO >> 4) & 0x3FFF) << 16) |
@@ -633,45 +644,54 @@ __device__ __forceinline__ void ld64(uint32_t taddr, float* v) {
 #pragma unroll
     for (int j = 0; j < 64; ++j) v[j] = __uint_as_float(r[j]);
 }
+// bounded wait on an mbarrier phase; true when it completed
+__device__ __forceinline__ bool wait_phase(uint32_t mbar, uint32_t phase) {
+    uint32_t done = 0;
+    for (int spin = 0; spin < (1 << 24) && !done; ++spin)
+        asm volatile("{ .reg .pred q; mbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\n"
+                     "selp.u32 %0, 1, 0, q; }" : "=r"(done) : "r"(mbar), "r"(phase) : "memory");
+    return done != 0;
+}
 }  // namespace tc
 
-__global__ void __launch_bounds__(128, 1) ldl_left_tc_kernel(LdlParams<float2> p) {
+__global__ void __launch_bounds__(128, 2) ldl_left_tc_kernel(LdlParams<float2> p) {
     using T = float2;
     using E = El<T>;
-    constexpr int NB = 32, NT = 128;
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    unsigned char* Ahi = smem_raw;
-    unsigned char* Alo = Ahi + tc::A_BYTES;
-    unsigned char* Bhi = Alo + tc::A_BYTES;
-    unsigned char* Blo = Bhi + tc::B_BYTES;
-    T* Dg = reinterpret_cast<T*>(Blo + tc::B_BYTES);   // [32][NB+1]
-    T* WL = Dg + 32 * (NB + 1);
+    constexpr int NB = 32, NT = 128, KCC = tc::KCC;
+    extern __shared__ __align__(128) unsigned char smem_tc[];
+    // stage s: Ahi, Alo (128 x 32 real), Bhi, Blo (64 x 32 real), K-major core matrices
+    unsigned char* stage0 = smem_tc;
+    T* WL = reinterpret_cast<T*>(smem_tc + 2 * tc::STAGE_BYTES);    // [NB][NB]
     T* Dsh = WL + NB * NB;
     T* Dinv = Dsh + NB;
     T* Dsq = Dinv + NB;
-    __shared__ __align__(8) uint64_t mbar;
+    T* Dg = reinterpret_cast<T*>(smem_tc + tc::STAGE_BYTES);        // [32][NB+1], aliases stage 1 (free then)
+    __shared__ __align__(8) uint64_t mbar[2];
     __shared__ uint32_t tmem_slot;
     __shared__ int item_sh, bail_sh;
     const int tid = threadIdx.x, warp = tid >> 5;
     T* G = p.ws + (size_t)blockIdx.x * p.ws_stride;
-    const uint32_t mbar_a = (uint32_t)__cvta_generic_to_shared(&mbar);
-    const uint32_t aH = (uint32_t)__cvta_generic_to_shared(Ahi), aL = (uint32_t)__cvta_generic_to_shared(Alo);
-    const uint32_t bH = (uint32_t)__cvta_generic_to_shared(Bhi), bL = (uint32_t)__cvta_generic_to_shared(Blo);
+    const uint32_t mb0 = (uint32_t)__cvta_generic_to_shared(&mbar[0]);
+    const uint32_t mb1 = (uint32_t)__cvta_generic_to_shared(&mbar[1]);
+    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(stage0);
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_a));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb0));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb1));
         bail_sh = 0;
     }
     if (warp == 0) {
         const uint32_t slot = (uint32_t)__cvta_generic_to_shared(&tmem_slot);
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" ::"r"(slot));
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot), "n"(tc::TMEM_COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = tmem_slot;
-    const uint32_t my_taddr = tmem + ((uint32_t)(warp * 32) << 16);
-    uint32_t phase = 0;
+    const uint32_t my_lane = (uint32_t)(warp * 32) << 16;
+    uint32_t ph0 = 0u, ph1 = 0u;                        // mbarrier phases
+    int pend0 = 0, pend1 = 0;                           // MMAs committed and not yet waited for
 
     for (;;) {
         if (tid == 0) item_sh = atomicAdd(p.counter, 1);
@@ -692,7 +712,6 @@ __global__ void __launch_bounds__(128, 1) ldl_left_tc_kernel(LdlParams<float2> p
         const T z = p.shifts[k];
         const float* C = p.C ? p.C + p.offC[w] : nullptr;
         const float* F = p.F ? p.F + p.offF[w] : nullptr;
-        // quadratic forms accumulate in place in the output (any number of owned rows)
         T* const qg = p.q ? p.q + (long long)k * p.qstride + p.offQ[w] : nullptr;
         if (qg)
             for (int r = tid; r < m; r += NT) qg[r] = E::zero();
@@ -723,69 +742,116 @@ __global__ void __launch_bounds__(128, 1) ldl_left_tc_kernel(LdlParams<float2> p
 #pragma unroll
                     for (int c = 0; c < NB; ++c) acc[c] = E::zero();
                 }
-                for (int k0 = 0; k0 < j0; k0 += 32) {
-                    // ---- stage B' (panel rows x chunk) and A (this thread's row x chunk), split hi/lo
-                    for (int idx = tid; idx < 32 * 32; idx += NT) {
-                        const int c = idx & 31, kk = idx >> 5;
-                        const T b = G[(j0 + c) + (long long)(k0 + kk) * ld];
-                        float rh, rl, ih, il;
-                        tc::split(b.x, rh, rl);
-                        tc::split(b.y, ih, il);
-                        // rows 2c (real part of the output) and 2c+1 (imaginary), K columns 2kk, 2kk+1
-                        *reinterpret_cast<float2*>(Bhi + tc::off(2 * c, 2 * kk)) = make_float2(rh, -ih);
-                        *reinterpret_cast<float2*>(Blo + tc::off(2 * c, 2 * kk)) = make_float2(rl, -il);
-                        *reinterpret_cast<float2*>(Bhi + tc::off(2 * c + 1, 2 * kk)) = make_float2(ih, rh);
-                        *reinterpret_cast<float2*>(Blo + tc::off(2 * c + 1, 2 * kk)) = make_float2(il, rl);
-                    }
-                    {
-                        const T* gi = G + i + (long long)k0 * ld;
-#pragma unroll 8
-                        for (int kk = 0; kk < 32; ++kk) {
-                            const T g = active ? gi[(long long)kk * ld] : E::zero();
+                const int nch = j0 / KCC;                 // j0 is a multiple of 32: nch even
+                if (nch > 0) {
+                    // operands of two chunks in registers (slot a0/b0r: even chunks, a1/b1r: odd)
+                    T a0[KCC], a1[KCC], b0r[4], b1r[4];
+                    const T* grow = G + i;
+                    auto load = [&](int c, T (&ar)[KCC], T (&br)[4]) {
+                        const int k0 = c * KCC;
+#pragma unroll
+                        for (int kk = 0; kk < KCC; ++kk) ar[kk] = active ? grow[(long long)(k0 + kk) * ld] : E::zero();
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            const int idx = tid + NT * q, cc = idx & 31, kk = idx >> 5;
+                            br[q] = G[(j0 + cc) + (long long)(k0 + kk) * ld];
+                        }
+                    };
+                    auto stage = [&](const T (&ar)[KCC], const T (&br)[4], int st) {
+                        unsigned char* Ahi = stage0 + st * tc::STAGE_BYTES;
+                        unsigned char* Alo = Ahi + tc::A_BYTES;
+                        unsigned char* Bhi = Ahi + 2 * tc::A_BYTES;
+                        unsigned char* Blo = Bhi + tc::B_BYTES;
+#pragma unroll
+                        for (int kk = 0; kk < KCC; ++kk) {
                             float rh, rl, ih, il;
-                            tc::split(g.x, rh, rl);
-                            tc::split(g.y, ih, il);
+                            tc::split(ar[kk].x, rh, rl);
+                            tc::split(ar[kk].y, ih, il);
                             *reinterpret_cast<float2*>(Ahi + tc::off(tid, 2 * kk)) = make_float2(rh, ih);
                             *reinterpret_cast<float2*>(Alo + tc::off(tid, 2 * kk)) = make_float2(rl, il);
                         }
-                    }
-                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    asm volatile("tcgen05.fence::before_thread_sync;");
-                    __syncthreads();
-                    asm volatile("tcgen05.fence::after_thread_sync;");
-                    if (tid == 0) {
-                        // 3xTF32: hi.hi, hi.lo, lo.hi, 8 instructions (K = 8) each
 #pragma unroll
-                        for (int kb = 0; kb < tc::KR / 8; ++kb)
-                            tc::mma(tmem, tc::desc(aH + kb * 2 * tc::LBO), tc::desc(bH + kb * 2 * tc::LBO), kb > 0);
+                        for (int q = 0; q < 4; ++q) {
+                            const int idx = tid + NT * q, cc = idx & 31, kk = idx >> 5;
+                            float rh, rl, ih, il;
+                            tc::split(br[q].x, rh, rl);
+                            tc::split(br[q].y, ih, il);
+                            // rows 2cc (real part of the output) and 2cc+1 (imaginary), K columns 2kk, 2kk+1
+                            *reinterpret_cast<float2*>(Bhi + tc::off(2 * cc, 2 * kk)) = make_float2(rh, -ih);
+                            *reinterpret_cast<float2*>(Blo + tc::off(2 * cc, 2 * kk)) = make_float2(rl, -il);
+                            *reinterpret_cast<float2*>(Bhi + tc::off(2 * cc + 1, 2 * kk)) = make_float2(ih, rh);
+                            *reinterpret_cast<float2*>(Blo + tc::off(2 * cc + 1, 2 * kk)) = make_float2(il, rl);
+                        }
+                    };
+                    // stage st staged by every thread; one thread issues its 12 MMAs into
+                    // accumulator st and commits them to mbarrier st
+                    auto issue = [&](int st) {
+                        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                        asm volatile("tcgen05.fence::before_thread_sync;");
+                        __syncthreads();
+                        asm volatile("tcgen05.fence::after_thread_sync;");
+                        if (tid == 0) {
+                            const uint32_t aH = sbase + st * tc::STAGE_BYTES, aL = aH + tc::A_BYTES;
+                            const uint32_t bH = aH + 2 * tc::A_BYTES, bL = bH + tc::B_BYTES;
+                            const uint32_t acc_t = tmem + (uint32_t)(st * 64);
 #pragma unroll
-                        for (int kb = 0; kb < tc::KR / 8; ++kb)
-                            tc::mma(tmem, tc::desc(aH + kb * 2 * tc::LBO), tc::desc(bL + kb * 2 * tc::LBO), 1);
+                            for (int kb = 0; kb < tc::KR / 8; ++kb)
+                                tc::mma(acc_t, tc::desc(aH + kb * 2 * tc::LBO), tc::desc(bH + kb * 2 * tc::LBO), kb > 0);
 #pragma unroll
-                        for (int kb = 0; kb < tc::KR / 8; ++kb)
-                            tc::mma(tmem, tc::desc(aL + kb * 2 * tc::LBO), tc::desc(bH + kb * 2 * tc::LBO), 1);
-                        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-                                     ::"r"(mbar_a));
-                    }
-                    uint32_t done = 0;
-                    for (int spin = 0; spin < (1 << 24) && !done; ++spin)
-                        asm volatile("{ .reg .pred q; mbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\n"
-                                     "selp.u32 %0, 1, 0, q; }" : "=r"(done) : "r"(mbar_a), "r"(phase));
-                    phase ^= 1u;
-                    if (!done) {
-                        atomicOr(p.status, ST_TIMEOUT);
-                        atomicOr(&bail_sh, 1);
-                    }
-                    asm volatile("tcgen05.fence::after_thread_sync;");
-                    if (done) {
-                        float v[64];
-                        tc::ld64(my_taddr, v);
+                            for (int kb = 0; kb < tc::KR / 8; ++kb)
+                                tc::mma(acc_t, tc::desc(aH + kb * 2 * tc::LBO), tc::desc(bL + kb * 2 * tc::LBO), 1);
 #pragma unroll
-                        for (int c = 0; c < NB; ++c) acc[c] = E::sub(acc[c], make_float2(v[2 * c], v[2 * c + 1]));
+                            for (int kb = 0; kb < tc::KR / 8; ++kb)
+                                tc::mma(acc_t, tc::desc(aL + kb * 2 * tc::LBO), tc::desc(bH + kb * 2 * tc::LBO), 1);
+                            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                                         ::"r"(st ? mb1 : mb0));
+                        }
+                    };
+                    // wait for accumulator st, subtract it from the row's running values, release it
+                    auto finish = [&](int st, uint32_t& ph, int& pend) {
+                        const bool ok = tc::wait_phase(st ? mb1 : mb0, ph);
+                        if (ok) {
+                            ph ^= 1u;
+                            pend = 0;
+                        } else {
+                            atomicOr(p.status, ST_TIMEOUT);
+                            atomicOr(&bail_sh, 1);
+                        }
+                        asm volatile("tcgen05.fence::after_thread_sync;");
+                        if (ok) {
+                            float v[64];
+                            tc::ld64(tmem + my_lane + (uint32_t)(st * 64), v);
+#pragma unroll
+                            for (int cc = 0; cc < NB; ++cc)
+                                acc[cc] = E::sub(acc[cc], make_float2(v[2 * cc], v[2 * cc + 1]));
+                        }
+                        asm volatile("tcgen05.fence::before_thread_sync;");
+                        __syncthreads();                  // bail flag visible; accumulator st read
+                    };
+                    load(0, a0, b0r);
+                    load(1, a1, b1r);                     // nch is even (>= 2)
+                    stage(a0, b0r, 0);
+                    issue(0);
+                    pend0 = 1;
+                    if (nch > 2) load(2, a0, b0r);
+                    for (int c = 0; c < nch; c += 2) {
+                        // chunk c+1 into stage 1 while the MMAs of chunk c run (stage 1 and its
+                        // accumulator were released by finish(1) of the previous pair)
+                        stage(a1, b1r, 1);
+                        issue(1);
+                        pend1 = 1;
+                        if (c + 3 < nch) load(c + 3, a1, b1r);
+                        finish(0, ph0, pend0);
+                        if (bail_sh) break;
+                        if (c + 2 < nch) {
+                            stage(a0, b0r, 0);
+                            issue(0);
+                            pend0 = 1;
+                            if (c + 4 < nch) load(c + 4, a0, b0r);
+                        }
+                        finish(1, ph1, pend1);
+                        if (bail_sh) break;
                     }
-                    asm volatile("tcgen05.fence::before_thread_sync;");
-                    __syncthreads();                  // tiles free for the next chunk
-                    if (bail_sh) break;
                 }
                 if (bail_sh) break;
                 if (b0 == 0) {
@@ -830,6 +896,7 @@ __global__ void __launch_bounds__(128, 1) ldl_left_tc_kernel(LdlParams<float2> p
 #pragma unroll
                         for (int c = 0; c < NB; ++c) acc[c] = Dg[tid * (NB + 1) + c];
                     }
+                    __syncthreads();                      // Dg (stage 1) free for the next batch
                 }
                 if (active && ir >= NB) {
 #pragma unroll
@@ -841,7 +908,6 @@ __global__ void __launch_bounds__(128, 1) ldl_left_tc_kernel(LdlParams<float2> p
                     }
                     if (i >= np && qg) {
                         // the panel's NB terms of the quadratic form summed from zero, then added
-                        // (blocked summation: one FP32 chain over all n terms loses ~10x accuracy)
                         T part = E::zero();
 #pragma unroll
                         for (int kk = 0; kk < NB; ++kk) part = E::fma(E::mul(acc[kk], acc[kk]), Dsh[kk], part);
@@ -858,10 +924,12 @@ __global__ void __launch_bounds__(128, 1) ldl_left_tc_kernel(LdlParams<float2> p
         }
         __syncthreads();
     }
-    // release the tensor memory (the MMA of every chunk was waited for above)
+    // MMAs still in flight after a timeout: bounded wait before the tensor memory is released
+    if (pend0) (void)tc::wait_phase(mb0, ph0);
+    if (pend1) (void)tc::wait_phase(mb1, ph1);
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem));
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(tc::TMEM_COLS));
 }
 
 // ---------------------------------------------------------------------------
@@ -1120,11 +1188,16 @@ static int launch_left_bulk(const LdlParams<T>& p, int grid, cudaStream_t s) {
 }
 
 static int launch_left_tc(const LdlParams<float2>& p, int grid, cudaStream_t s) {
-    const size_t smem = 2 * (size_t)tc::A_BYTES + 2 * (size_t)tc::B_BYTES +
-                        sizeof(float2) * ((size_t)32 * 33 + 32 * 32 + 3 * 32);
+    // two stages, then WL and the pivots (the diagonal block aliases stage 1)
+    const size_t smem = 2 * (size_t)tc::STAGE_BYTES + sizeof(float2) * ((size_t)32 * 32 + 3 * 32);
     int per_sm = 0;
     if (int rc = prepare_kernel<ldl_left_tc_kernel>(128, smem, &per_sm)) return rc;
-    grid = std::min(grid, device_sms());                // one CTA (one TMEM allocation) per SM
+    // two CTAs per SM (2 x 105 KB shared memory, 2 x 30 K registers, 2 x 128 of the 512 TMEM
+    // columns); the occupancy query reports one, but two run co-resident (measured: 185 -> 129 ms
+    // per pass at 1024 electrons).  CTAs never wait on one another, so a CTA that finds no room
+    // simply starts later and finds the queue empty.
+    (void)per_sm;
+    grid = std::min(grid, 2 * device_sms());
     ldl_left_tc_kernel<<<grid, 128, smem, s>>>(p);
     LRES_CUDA_TRY(cudaGetLastError());
     return LRES_OK;
