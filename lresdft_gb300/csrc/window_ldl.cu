@@ -751,9 +751,10 @@ __global__ void __launch_bounds__(128, 2) ldl_left_tc_kernel(LdlParams<float2> p
                         const int k0 = c * KCC;
 #pragma unroll
                         for (int kk = 0; kk < KCC; ++kk) ar[kk] = active ? grow[(long long)(k0 + kk) * ld] : E::zero();
+                        // panel values: thread = (row cc = tid % 32, k pairs 2p, 2p+1 and 2p+8, 2p+9)
 #pragma unroll
                         for (int q = 0; q < 4; ++q) {
-                            const int idx = tid + NT * q, cc = idx & 31, kk = idx >> 5;
+                            const int cc = tid & 31, kk = 2 * (tid >> 5) + (q & 1) + 8 * (q >> 1);
                             br[q] = G[(j0 + cc) + (long long)(k0 + kk) * ld];
                         }
                     };
@@ -762,25 +763,30 @@ __global__ void __launch_bounds__(128, 2) ldl_left_tc_kernel(LdlParams<float2> p
                         unsigned char* Alo = Ahi + tc::A_BYTES;
                         unsigned char* Bhi = Ahi + 2 * tc::A_BYTES;
                         unsigned char* Blo = Bhi + tc::B_BYTES;
+                        // 16-byte stores: two complex k values = the 4 real K of one core-matrix row
 #pragma unroll
-                        for (int kk = 0; kk < KCC; ++kk) {
-                            float rh, rl, ih, il;
-                            tc::split(ar[kk].x, rh, rl);
-                            tc::split(ar[kk].y, ih, il);
-                            *reinterpret_cast<float2*>(Ahi + tc::off(tid, 2 * kk)) = make_float2(rh, ih);
-                            *reinterpret_cast<float2*>(Alo + tc::off(tid, 2 * kk)) = make_float2(rl, il);
+                        for (int kk = 0; kk < KCC; kk += 2) {
+                            float rh0, rl0, ih0, il0, rh1, rl1, ih1, il1;
+                            tc::split(ar[kk].x, rh0, rl0);
+                            tc::split(ar[kk].y, ih0, il0);
+                            tc::split(ar[kk + 1].x, rh1, rl1);
+                            tc::split(ar[kk + 1].y, ih1, il1);
+                            *reinterpret_cast<float4*>(Ahi + tc::off(tid, 2 * kk)) = make_float4(rh0, ih0, rh1, ih1);
+                            *reinterpret_cast<float4*>(Alo + tc::off(tid, 2 * kk)) = make_float4(rl0, il0, rl1, il1);
                         }
 #pragma unroll
-                        for (int q = 0; q < 4; ++q) {
-                            const int idx = tid + NT * q, cc = idx & 31, kk = idx >> 5;
-                            float rh, rl, ih, il;
-                            tc::split(br[q].x, rh, rl);
-                            tc::split(br[q].y, ih, il);
-                            // rows 2cc (real part of the output) and 2cc+1 (imaginary), K columns 2kk, 2kk+1
-                            *reinterpret_cast<float2*>(Bhi + tc::off(2 * cc, 2 * kk)) = make_float2(rh, -ih);
-                            *reinterpret_cast<float2*>(Blo + tc::off(2 * cc, 2 * kk)) = make_float2(rl, -il);
-                            *reinterpret_cast<float2*>(Bhi + tc::off(2 * cc + 1, 2 * kk)) = make_float2(ih, rh);
-                            *reinterpret_cast<float2*>(Blo + tc::off(2 * cc + 1, 2 * kk)) = make_float2(il, rl);
+                        for (int q = 0; q < 4; q += 2) {
+                            const int cc = tid & 31, kk = 2 * (tid >> 5) + 8 * (q >> 1);
+                            float rh0, rl0, ih0, il0, rh1, rl1, ih1, il1;
+                            tc::split(br[q].x, rh0, rl0);
+                            tc::split(br[q].y, ih0, il0);
+                            tc::split(br[q + 1].x, rh1, rl1);
+                            tc::split(br[q + 1].y, ih1, il1);
+                            // rows 2cc (real part of the output) and 2cc+1 (imaginary), K columns 2kk..2kk+3
+                            *reinterpret_cast<float4*>(Bhi + tc::off(2 * cc, 2 * kk)) = make_float4(rh0, -ih0, rh1, -ih1);
+                            *reinterpret_cast<float4*>(Blo + tc::off(2 * cc, 2 * kk)) = make_float4(rl0, -il0, rl1, -il1);
+                            *reinterpret_cast<float4*>(Bhi + tc::off(2 * cc + 1, 2 * kk)) = make_float4(ih0, rh0, ih1, rh1);
+                            *reinterpret_cast<float4*>(Blo + tc::off(2 * cc + 1, 2 * kk)) = make_float4(il0, rl0, il1, rl1);
                         }
                     };
                     // stage st staged by every thread; one thread issues its 12 MMAs into
@@ -825,8 +831,9 @@ __global__ void __launch_bounds__(128, 2) ldl_left_tc_kernel(LdlParams<float2> p
                             for (int cc = 0; cc < NB; ++cc)
                                 acc[cc] = E::sub(acc[cc], make_float2(v[2 * cc], v[2 * cc + 1]));
                         }
-                        asm volatile("tcgen05.fence::before_thread_sync;");
-                        __syncthreads();                  // bail flag visible; accumulator st read
+                        // no barrier here: the next issue()'s barrier orders this read-back before
+                        // the MMA that reuses accumulator st, and this thread has itself waited
+                        // for the MMAs that read the stage it restages next
                     };
                     load(0, a0, b0r);
                     load(1, a1, b1r);                     // nch is even (>= 2)
@@ -836,22 +843,24 @@ __global__ void __launch_bounds__(128, 2) ldl_left_tc_kernel(LdlParams<float2> p
                     if (nch > 2) load(2, a0, b0r);
                     for (int c = 0; c < nch; c += 2) {
                         // chunk c+1 into stage 1 while the MMAs of chunk c run (stage 1 and its
-                        // accumulator were released by finish(1) of the previous pair)
+                        // accumulator were released by finish(1) of the previous pair); the bail
+                        // flag is read only right after a barrier, so every thread decides alike
                         stage(a1, b1r, 1);
                         issue(1);
                         pend1 = 1;
+                        if (bail_sh) break;
                         if (c + 3 < nch) load(c + 3, a1, b1r);
                         finish(0, ph0, pend0);
-                        if (bail_sh) break;
                         if (c + 2 < nch) {
                             stage(a0, b0r, 0);
                             issue(0);
                             pend0 = 1;
+                            if (bail_sh) break;
                             if (c + 4 < nch) load(c + 4, a0, b0r);
                         }
                         finish(1, ph1, pend1);
-                        if (bail_sh) break;
                     }
+                    __syncthreads();                      // every read-back done; bail flag visible
                 }
                 if (bail_sh) break;
                 if (b0 == 0) {
