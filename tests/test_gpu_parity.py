@@ -222,3 +222,25 @@ def test_pass_captured_in_cuda_graph(systems, precision):
         _copy_device(s.density_device_ptr(), host)
         assert np.array_equal(host, dens_ref)
     s.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_cell_windows_reproduce_published_energy(precision):
+    """The reference's published setting with cell-centred windows (benchmarks/scaling_rigorous.py:36,
+    results/scaling_rigorous.json, n=3): 27 H2 cells, a=6, 10 points per cell, rc=0.6, benchmark
+    basis, windows on the cell centres with R_w=12.1, M=64, SCF tol 1e-6:
+    E_LRes(54 e) = -15.746532895084757.  The published run used float32 vector reuse (~1e-9 Ha);
+    FP64 within 5e-9 Ha, mixed within 2e-7 Ha/electron."""
+    from lresdft_gb300 import LResGPU, system
+    from lresdft_gb300.scf import scf_lcao
+    cr = system.h2_crystal((3, 3, 3), a=6.0, pts_per_cell=10, rc=0.6)
+    b = system.LCAOBasis(cr, rcut=4.5, s_exps=(1.2, 0.4, 0.15), p_exps=(0.5,))
+    s = LResGPU(b, system.cell_centres((3, 3, 3), 6.0), R_w=12.1, M=64, precision=precision)
+    # every cell lies within 10.4 bohr < R_w of every other: 27 whole-cell windows, solved once
+    assert len(s.windows) == 27 and np.all(s.nW == b.nb) and len(s.ctx_windows) == 1
+    r = scf_lcao(cr, s, tol=1e-6)
+    assert r["converged"]
+    err = abs(r["energy"] - (-15.746532895084757))
+    print(precision, "iterations", r["iterations"], "energy error", err)
+    assert err < (5e-9 if precision == "fp64" else 2e-7 * cr.n_elec)
+    s.close()

@@ -6,7 +6,8 @@ oracle's eigen-route window pass over the FULL window spectra (1e-10 density, 1e
 energy); mixed precision within 2e-7 Ha/electron.  The reference's own passes keep only
 the eigenpairs below c + 1.5 R (src/lrft_cpp.cpp:98-111), whose dropped occupations are
 <= 1/(1 + 1.5^M): 5e-12 at M = 64 but 2.3e-6 at M = 32; the pole route sums every state, so
-the comparison uses the untruncated spectra at the oracle's (mu, e_lo)."""
+the comparison uses the untruncated spectra at the oracle's (mu, e_lo).  Also cell-centred
+windows that do not cover the cell."""
 import numpy as np
 import pytest
 
@@ -69,3 +70,18 @@ def test_compressed_crystal_large_windows(R_w):
     o, dens_o, eb_o, mu = _oracle_pass(b, cr.pos, R_w, 64, v)
     assert max(len(w) for w in o.windows) > 500
     _check(b, cr, cr.pos, R_w, 64, v, o, dens_o, eb_o, mu)
+
+
+def test_partial_cell_windows():
+    """Windows on cell centres (lrft/lcao3d.py:287-289) that do not cover the cell: 64 H2
+    cells, a = 6, benchmark basis, R_w = 12.1 (cells 13.4 bohr apart fall outside)."""
+    from lresdft_gb300 import system
+    from oracle import lrft_oracle as orc
+    cr = system.h2_crystal((4, 4, 4), a=6.0, pts_per_cell=8, rc=0.6)
+    b = system.LCAOBasis(cr, rcut=4.5, s_exps=(1.2, 0.4, 0.15), p_exps=(0.5,))
+    cells = system.cell_centres((4, 4, 4), 6.0)
+    v = orc.guess_potential(cr)
+    o, dens_o, eb_o, mu = _oracle_pass(b, cells, 12.1, 64, v)
+    nW = np.array([len(w) for w in o.windows])
+    assert nW.max() < b.nb
+    _check(b, cr, cells, 12.1, 64, v, o, dens_o, eb_o, mu)
