@@ -118,6 +118,35 @@ def adjoint_leg(s, s64, mu, e_lo):
     return out
 
 
+def published_leg():
+    """The reference's published 1024-electron LRes SCF (benchmarks/scaling_rigorous.py:33-38,
+    results/scaling_rigorous.json, n = 8): 512 H2 cells, a = 6, 10 points per cell (80^3 grid),
+    rc = 0.6, benchmark basis (rcut 4.5, s 1.2/0.4/0.15, p 0.5), windows on the cell centres with
+    R_w = 12.1, M = 64, SCF tol 1e-6 with the reference's mixer.  Timed like the reference's `wall`:
+    solver construction + SCF (the basis tabulation before it is excluded there too)."""
+    from lresdft_gb300 import LResGPU, system
+    from lresdft_gb300.scf import scf_lcao
+    cr = system.h2_crystal((8, 8, 8), a=6.0, pts_per_cell=10, rc=0.6)
+    b = system.LCAOBasis(cr, rcut=4.5, s_exps=(1.2, 0.4, 0.15), p_exps=(0.5,))
+    t0 = time.perf_counter()
+    s = LResGPU(b, system.cell_centres((8, 8, 8), 6.0), R_w=12.1, M=64, precision="mixed", tile_config="auto")
+    t1 = time.perf_counter()
+    st = []
+    r = scf_lcao(cr, s, tol=1e-6, step_times=st)
+    t2 = time.perf_counter()
+    E_pub = -298.93659450240705
+    out = {"workload": "8x8x8 H2 cells, a=6, 80^3 grid, cell windows R_w=12.1 (n_W %d-%d), M=64, tol 1e-6, mixed"
+                       % (int(s.nW.min()), int(s.nW.max())),
+           "wall_s": round(t2 - t0, 2), "scf_wall_s": round(t2 - t1, 2), "iterations": r["iterations"],
+           "converged": bool(r["converged"]), "warm_step_s": round(float(np.median(st[1:])), 3) if len(st) > 1 else None,
+           "passes": s.passes, "energy": r["energy"], "energy_err_per_e_vs_published": abs(r["energy"] - E_pub) / cr.n_elec,
+           "reference_published": {"wall_s": 125.4, "scf_wall_s": 115.0, "iterations": 11, "warm_step_s": 6.3,
+                                   "energy": E_pub, "hardware": "1 CPU thread (results/scaling_rigorous.json, median of 3)"},
+           "speedup_wall_vs_published": round(125.4 / (t2 - t0), 1)}
+    s.close()
+    return out
+
+
 def run_ours(args):
     import torch
     from lresdft_gb300 import LResGPU
@@ -348,6 +377,12 @@ def run_ours(args):
                        "Pulay mixer, tol not reached at 1024 e); s/iter = median of iterations 3..end")
         line["scf"] = scf
 
+    if rank == 0 and world == 1 and args.published:
+        try:
+            line["published_scf_1024"] = published_leg()
+        except Exception as exc:
+            line["published_scf_1024"] = {"error": str(exc)[:200]}
+
     if rank == 0 and world == 1 and not args.no_cpu:
         try:
             c = cpu_leg(b, v, s, mu, e_lo)
@@ -420,6 +455,8 @@ def main():
     ap.add_argument("--no-fp64-scf", dest="fp64_scf", action="store_false",
                     help="skip the FP64 SCF window (about a minute at 1024 electrons)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-published", dest="published", action="store_false",
+                    help="skip the reference's published 1024-electron SCF setting")
     ap.add_argument("--no-adjoint", dest="adjoint", action="store_false",
                     help="skip the band-energy adjoint leg (mixed and FP64)")
     ap.add_argument("--cells", type=int, default=8, help="crystal of cells^3 H2 (8 = the benchmark workload)")

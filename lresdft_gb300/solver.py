@@ -159,6 +159,7 @@ class LResGPU:
         # trace rows (passes that need N and E only): installed when the owned points
         # outnumber the window functions clearly (fine grids)
         self._trace = False
+        self._resolved = False      # the last density call re-solved mu
         self.trace_rows = None
         m_w = np.diff(cOoff)
         if trace_rows is True or (trace_rows == "auto" and m_w.mean() > 1.5 * self.ctx_nW.mean()):
@@ -559,13 +560,15 @@ class LResGPU:
         if self.mu is not None:
             mu, e_lo = self.mu, self.e_lo
             if self._edge_ok(mu, e_lo):
-                # with density: when mu is kept (the common warm case) this is the only pass
-                dens, n, eb = self.pole_pass(mu, e_lo)
+                # with density when mu was kept last time (then this is likely the only pass);
+                # over the trace rows when the last call had to re-solve mu
+                dens, n, eb = self.pole_pass(mu, e_lo, want_density=not (self._trace and self._resolved))
                 cnt = n - N
                 if self.lag_mu and abs(cnt) < 0.25:
                     self.mu = mu
                     dens, eb = self._with_density(mu, e_lo, dens, eb)
                     return dens.reshape(cr.shape), eb, mu
+                self._resolved = abs(cnt) > tol
                 if abs(cnt) > tol:
                     mu, dens, eb = self._solve_mu(e_lo, N, ftol, start=(mu, cnt, dens, eb))
                 self.mu = self._mu_last = mu
@@ -593,6 +596,7 @@ class LResGPU:
             mu, dens, eb = self._solve_mu(e_lo, N, ftol, lo_start=lo)
         self.mu, self.e_lo = mu, e_lo
         self._mu_last = mu
+        self._resolved = True
         dens, eb = self._with_density(mu, e_lo, dens, eb)
         return dens.reshape(cr.shape), eb, mu
 
