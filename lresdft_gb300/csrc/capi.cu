@@ -71,6 +71,8 @@ struct lres_ctx {
     std::vector<long long> offC, offF, offQ;
     // device: windows
     int *d_n = nullptr, *d_m = nullptr;
+    int* d_c0 = nullptr;                 // per window: first local column any owned point touches
+    bool skip_rows = false;              // owned-point rows start late enough to skip panels
     long long *d_offC = nullptr, *d_offF = nullptr, *d_offQ = nullptr, *d_Oflat = nullptr;
     int *d_wgrp_off = nullptr, *d_wgrp = nullptr, *d_wgrp_lo = nullptr, *d_gloc = nullptr;
     // block storage
@@ -132,7 +134,7 @@ struct lres_ctx {
 };
 
 lres_ctx::~lres_ctx() {
-    void* ptrs[] = {d_n, d_m, d_offC, d_offF, d_offQ, d_Oflat, d_wgrp_off, d_wgrp, d_wgrp_lo, d_gloc,
+    void* ptrs[] = {d_n, d_m, d_c0, d_offC, d_offF, d_offQ, d_Oflat, d_wgrp_off, d_wgrp, d_wgrp_lo, d_gloc,
                     bp.gptr, bp.bptr, bp.bcol, bp.brow, bp.boff, bp.btrans, bp.pair_blk, sp.soff, sp.sgrid,
                     sp.sval, sp.coff, sp.cslot, d_Sblk, d_Tblk, d_Hblk, d_SW, d_HW, d_F, d_LinvT, d_Y, d_Hhat,
                     d_Hhat32, d_Fhat32, d_LinvT_df, d_H_df, d_Y_df, d_items, d_items_win, d_items_sub, d_counter, d_status, d_npos, d_ws, d_shifts,
@@ -193,6 +195,7 @@ int ldl_launch(lres_ctx* c, LdlJob::Kind kind, int nitems, const int2* items, co
     j.grid = slots;
     j.smem_budget = c->smem_budget;
     j.config = c->config;
+    j.c0 = (kind == LdlJob::R64 || !c->skip_rows) ? nullptr : c->d_c0;
     LRES_CUDA_TRY(cudaMemsetAsync(c->d_counter, 0, sizeof(int), s));
     return run_ldl(j, s);
 }
@@ -639,6 +642,31 @@ extern "C" int lres_ctx_create(lres_ctx** out, const lres_system_desc* d, int pr
     TRY(dalloc(&c->d_Hblk, nval));
     TRY(upload(&c->d_n, c->n_w, s));
     TRY(upload(&c->d_m, c->m_w, s));
+    {
+        // first window column with a nonzero owned-point value: the owned rows F_W (and the
+        // standard-form and trace rows derived from it) are zero before it
+        std::vector<int> c0(c->nwin);
+        for (int w = 0; w < c->nwin; ++w) {
+            int lo = c->n_w[w];
+            for (int64_t pp = d->Ooff[w]; pp < d->Ooff[w + 1]; ++pp) {
+                const int64_t r = d->Oflat[pp];
+                for (int64_t q = d->Xp[r]; q < d->Xp[r + 1]; ++q) {
+                    if (d->Xv[q] == 0.0) continue;
+                    const int f = (int)d->Xi[q];
+                    const int g = group_of_fn[f];
+                    const int l = gloc[(size_t)w * c->ngroups + g];
+                    if (l >= 0) lo = std::min(lo, l + f - c->gptr_h[g]);
+                }
+            }
+            c0[w] = lo;
+        }
+        TRY(upload(&c->d_c0, c0, s));
+        // the skipping kernel pays when windows skip a good share of their columns (cell
+        // windows with a large R_w); with ~10% the extra partial row batches cost more
+        double frac = 0.0;
+        for (int w = 0; w < c->nwin; ++w) frac += c->n_w[w] ? (double)c0[w] / c->n_w[w] : 0.0;
+        c->skip_rows = frac >= 0.25 * c->nwin;
+    }
     TRY(upload(&c->d_offC, c->offC, s));
     TRY(upload(&c->d_offF, c->offF, s));
     TRY(upload(&c->d_offQ, c->offQ, s));

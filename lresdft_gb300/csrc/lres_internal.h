@@ -34,6 +34,7 @@ struct LdlJob {
     size_t smem_budget = 0;
     int config = 0;                 // complex kernels: tile configuration (see lres_tune)
     int keep = 0;                   // complex kernels: keep every item's factor (slot = item index)
+    const int* c0 = nullptr;        // per window: the F rows are zero in the columns before c0[w]
 };
 
 // Panel width of the factor kept for the adjoint (the window is padded to a multiple).

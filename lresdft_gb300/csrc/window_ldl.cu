@@ -72,35 +72,44 @@ struct LdlParams {
     int nmax, mmax;
     int keep;                   // left-looking kernel: one workspace slot per item, the complete
                                 // factor G (diagonal blocks and last panel included) is kept
+    const int* c0;              // per window (nullable): F is zero in the columns before c0[w], so
+                                // its rows of G are zero there too and are not computed
 };
 
 // Dynamic shared memory attribute and occupancy of a kernel, set/queried only when the
 // request grows, so that launches enqueued during CUDA-graph capture issue no attribute
-// calls (the first, eager launch of each instantiation does).
+// calls (the first, eager launch of each instantiation on each device does).  Cached per
+// device (up to kMaxDevices devices in one process).
+constexpr int kMaxDevices = 16;
+
+static int current_device() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return dev < 0 ? 0 : (dev >= kMaxDevices ? kMaxDevices - 1 : dev);
+}
+
 template <auto Kern>
 static int prepare_kernel(int threads, size_t smem, int* per_sm) {
-    static size_t set_smem = 0;          // one cache per kernel instantiation
-    static int cached_per_sm = 0;
-    if (smem > set_smem) {
+    static size_t set_smem[kMaxDevices] = {};     // one cache per kernel instantiation and device
+    static int cached_per_sm[kMaxDevices] = {};
+    const int dev = current_device();
+    if (smem > set_smem[dev]) {
         LRES_CUDA_TRY(cudaFuncSetAttribute(Kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         // prefer the largest shared-memory carveout, so that the occupancy below is the maximum
         LRES_CUDA_TRY(cudaFuncSetAttribute(Kern, cudaFuncAttributePreferredSharedMemoryCarveout,
                                            (int)cudaSharedmemCarveoutMaxShared));
-        LRES_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cached_per_sm, Kern, threads, smem));
-        set_smem = smem;
+        LRES_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cached_per_sm[dev], Kern, threads, smem));
+        set_smem[dev] = smem;
     }
-    *per_sm = cached_per_sm;
+    *per_sm = cached_per_sm[dev];
     return LRES_OK;
 }
 
 static int device_sms() {
-    static int nsm = 0;
-    if (!nsm) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    }
-    return nsm;
+    static int nsm[kMaxDevices] = {};
+    const int dev = current_device();
+    if (!nsm[dev]) cudaDeviceGetAttribute(&nsm[dev], cudaDevAttrMultiProcessorCount, dev);
+    return nsm[dev];
 }
 
 template <class T, int NB, int TR, int TC, int NT>
@@ -364,7 +373,9 @@ __device__ __forceinline__ void stage_chunk(T* buf, const T* G, long long ld, in
     cp_async_commit();
 }
 
-template <class T, int NB, int NT, int KC>
+// SKIP: owned-point rows start at each window's first owned-point panel (compiled separately,
+// so that contexts where no window can skip a panel run the plain batch loop).
+template <class T, int NB, int NT, int KC, bool SKIP>
 __global__ void __launch_bounds__(NT, 512 / NT) ldl_left_kernel(LdlParams<T> p) {
     using E = El<T>;
     using R = typename E::R;
@@ -409,6 +420,188 @@ __global__ void __launch_bounds__(NT, 512 / NT) ldl_left_kernel(LdlParams<T> p) 
             for (int r = tid; r < m; r += NT) qg[r] = E::zero();
         __syncthreads();
 
+        if constexpr (SKIP) {
+        // Owned-point rows are zero before the window's first owned-point column c0 (the
+        // solver orders the atoms that touch no owned point first), so their rows of G are
+        // zero there too: they are processed from the panel holding c0 on, in row batches of
+        // their own whose k sums start at that panel.
+        // When no panel can be skipped (p0 == 0) the rows keep one common batch sequence.
+        const int p0 = (p.c0 && m > 0) ? min(p.c0[w] / NB * NB, np) : 0;
+        const bool split = p0 > 0;
+        for (int j0 = 0; j0 < np; j0 += NB) {
+            // one batch of NT rows starting b0 rows below the panel's first row; rows at
+            // rend and beyond are inactive; the k sums start at kstart
+            auto batch = [&](const int b0, const int rend, const int kstart) {
+                const int ir = b0 + tid;              // row within the panel
+                const int i = j0 + ir;
+                const bool active = ir < rend;
+                T acc[NB];
+                if (active && i < n) {
+                    const R* cp = C ? C + i + (long long)j0 * n : nullptr;
+                    const R* bp = B ? B + i + (long long)j0 * n : nullptr;
+#pragma unroll
+                    for (int c = 0; c < NB; ++c) {
+                        const int col = j0 + c;
+                        T a = E::zero();
+                        if (col <= i) {                // lower triangle (col < n follows)
+                            const R bb = bp ? bp[(long long)c * n] : (i == col ? R(1) : R(0));
+                            const R cc = cp ? cp[(long long)c * n] : R(0);
+                            a = E::shift_minus(z, bb, cc);
+                        }
+                        acc[c] = a;
+                    }
+                } else if (active && i < np) {        // padding row: identity
+#pragma unroll
+                    for (int c = 0; c < NB; ++c) acc[c] = (j0 + c == i) ? E::from(R(1)) : E::zero();
+                } else if (active) {                  // right-hand-side row r = i - np
+                    const R* fp = F + (i - np) + (long long)j0 * m;
+#pragma unroll
+                    for (int c = 0; c < NB; ++c) acc[c] = (j0 + c < n) ? E::from(fp[(long long)c * m]) : E::zero();
+                } else {
+#pragma unroll
+                    for (int c = 0; c < NB; ++c) acc[c] = E::zero();
+                }
+                // Blocked accumulation: each KC-chunk of the k sum is formed from zero in
+                // registers and subtracted from the row's running value, kept in shared memory
+                // (the same rounding pattern as a right-looking update by KC-wide panels).
+                // chunks of the panel's G rows are copied asynchronously into a double buffer:
+                // chunk ci+1 is in flight while chunk ci is used; one barrier per chunk
+                const int nch = (j0 - kstart + KC - 1) / KC;
+                if (nch > 0) {
+#pragma unroll
+                    for (int c = 0; c < NB; ++c) accS[c * NT + tid] = acc[c];
+                    __syncthreads();                  // the previous loop's last buffer is free
+                    stage_chunk<T, NB, NT, KC>(Bs, G, ld, j0, kstart, min(KC, j0 - kstart));
+                }
+                for (int ci = 0; ci < nch; ++ci) {
+                    const int k0 = kstart + ci * KC;
+                    const int kc = min(KC, j0 - k0);   // a multiple of 8
+                    cp_async_wait_all();
+                    __syncthreads();                  // chunk ci visible; chunk ci-1 consumed
+                    if (ci + 1 < nch)
+                        stage_chunk<T, NB, NT, KC>(Bs + ((ci + 1) & 1) * KC * NB, G, ld, j0, k0 + KC,
+                                                   min(KC, j0 - k0 - KC));
+                    if (active) {
+                        const T* gi = G + i + (long long)k0 * ld;
+                        const T* bbuf = Bs + (ci & 1) * KC * NB;
+                        T tmp[NB];
+#pragma unroll
+                        for (int c = 0; c < NB; ++c) tmp[c] = E::zero();
+                        T g0 = gi[0], g1 = gi[ld];
+                        for (int kk = 0; kk < kc; kk += 2) {
+                            T n0 = g0, n1 = g1;
+                            if (kk + 2 < kc) {        // prefetch the next pair of the row's G values
+                                n0 = gi[(long long)(kk + 2) * ld];
+                                n1 = gi[(long long)(kk + 3) * ld];
+                            }
+                            const T* b = bbuf + kk * NB;
+#pragma unroll
+                            for (int c = 0; c < NB; ++c) {
+                                T a = tmp[c];
+                                a = E::fma(g0, b[c], a);
+                                a = E::fma(g1, b[NB + c], a);
+                                tmp[c] = a;
+                            }
+                            g0 = n0;
+                            g1 = n1;
+                        }
+#pragma unroll
+                        for (int c = 0; c < NB; ++c) accS[c * NT + tid] = E::sub(accS[c * NT + tid], tmp[c]);
+                    }
+                }
+                if (nch > 0) {
+#pragma unroll
+                    for (int c = 0; c < NB; ++c) acc[c] = accS[c * NT + tid];
+                }
+                if (b0 == 0) {
+                    // warp 0 parks its accumulated rows (the diagonal block is rows 0..NB-1)
+                    // in shared memory while it factors the block, then reloads them
+                    if (tid < 32) {
+#pragma unroll
+                        for (int c = 0; c < NB; ++c) Dg[tid * (NB + 1) + c] = acc[c];
+                    }
+                    __syncthreads();
+                    if (tid < 32) {
+                        // LDL^T of the NB x NB diagonal block in shared memory: lane = row;
+                        // the column operand L_c,kk is a broadcast read of row c
+                        const int lane = tid;
+                        T* myrow = Dg + lane * (NB + 1);
+                        for (int kk = 0; kk < NB; ++kk) {
+                            __syncwarp();
+                            const T d = Dg[kk * (NB + 1) + kk];
+                            const T dinv = E::inv(d);
+                            const bool mine = lane > kk && lane < NB;
+                            T l = E::zero();
+                            if (mine) {
+                                l = E::mul(myrow[kk], dinv);
+                                myrow[kk] = l;
+                            }
+                            if (lane == kk) {
+                                Dsh[kk] = d;
+                                Dinv[kk] = dinv;
+                                Dsq[kk] = E::csqrt(d);
+                                const double m2 = (double)E::mag2(d);
+                                if (!(m2 > 0.0) || !isfinite(m2)) atomicOr(p.status, ST_ZERO_PIVOT);
+                            }
+                            __syncwarp();
+                            if (mine) {
+                                const T ldv = E::mul(l, d);
+                                for (int c = kk + 1; c <= lane; ++c)
+                                    myrow[c] = E::fms(ldv, Dg[c * (NB + 1) + kk], myrow[c]);
+                            }
+                        }
+                        __syncwarp();
+                        for (int kk = 0; kk < NB; ++kk)
+                            if (lane > kk && lane < NB) WL[kk * NB + lane] = E::mul(Dsh[kk], myrow[kk]);
+                        if (p.keep && lane < NB) {     // the block's G = L sqrt(D), lower part
+                            T* gd = G + (j0 + lane) + (long long)j0 * ld;
+                            for (int c = 0; c <= lane; ++c)
+                                gd[(long long)c * ld] = c == lane ? Dsq[c] : E::mul(myrow[c], Dsq[c]);
+                        }
+                    }
+                    __syncthreads();
+                    // warp 0 reloads its parked rows (rows below the block still need the solve)
+                    if (tid < 32) {
+#pragma unroll
+                        for (int c = 0; c < NB; ++c) acc[c] = Dg[tid * (NB + 1) + c];
+                    }
+                    __syncthreads();
+                }
+                if (active && ir >= NB) {
+#pragma unroll
+                    for (int kk = 0; kk < NB; ++kk) {
+                        const T l = E::mul(acc[kk], Dinv[kk]);
+#pragma unroll
+                        for (int kk2 = kk + 1; kk2 < NB; ++kk2) acc[kk2] = E::fms(l, WL[kk * NB + kk2], acc[kk2]);
+                        acc[kk] = l;
+                    }
+                    if (i >= np && qg) {
+                        // the panel's NB terms of the quadratic form summed from zero, then added
+                        // (blocked summation: one FP32 chain over all n terms loses ~10x accuracy)
+                        T part = E::zero();
+#pragma unroll
+                        for (int kk = 0; kk < NB; ++kk) part = E::fma(E::mul(acc[kk], acc[kk]), Dsh[kk], part);
+                        qg[i - np] = E::add(qg[i - np], part);
+                    }
+                    if (j0 + NB < np || p.keep) {
+                        T* gout = G + i + (long long)j0 * ld;
+#pragma unroll
+                        for (int kk = 0; kk < NB; ++kk) gout[(long long)kk * ld] = E::mul(acc[kk], Dsq[kk]);
+                    }
+                }
+            };
+            if (!split) {
+                const int na = rows - j0;
+                for (int b0 = 0; b0 < na; b0 += NT) batch(b0, na, 0);
+            } else {
+                const int nA = np - j0;               // window rows, then (from panel p0 on) owned rows
+                for (int b0 = 0; b0 < nA; b0 += NT) batch(b0, nA, 0);
+                if (j0 >= p0)
+                    for (int b0 = nA; b0 < rows - j0; b0 += NT) batch(b0, rows - j0, p0);
+            }
+            __syncthreads();                          // finished G columns visible to the next panel
+        }
+        } else {
         for (int j0 = 0; j0 < np; j0 += NB) {
             const int na = rows - j0;
             for (int b0 = 0; b0 < na; b0 += NT) {
@@ -573,6 +766,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) ldl_left_kernel(LdlParams<T> p) 
                 }
             }
             __syncthreads();                          // finished G columns visible to the next panel
+        }
         }
         __syncthreads();
     }
@@ -1212,17 +1406,22 @@ static int launch_left_tc(const LdlParams<float2>& p, int grid, cudaStream_t s) 
     return LRES_OK;
 }
 
-template <class T, int NB, int NT, int KC>
-static int launch_left(const LdlParams<T>& p, int grid, cudaStream_t s) {
+template <class T, int NB, int NT, int KC, bool SKIP = false>
+static int launch_left_v(const LdlParams<T>& p, int grid, cudaStream_t s) {
     const size_t smem = sizeof(T) * ((size_t)2 * KC * NB + 32 * (NB + 1) + NB * NB + 3 * NB + (size_t)NB * NT);
-    auto kern = ldl_left_kernel<T, NB, NT, KC>;
+    auto kern = ldl_left_kernel<T, NB, NT, KC, SKIP>;
     // persistent grid: as many CTAs as fit on the device, at most one workspace slot each
     int per_sm = 0;
-    if (int rc = prepare_kernel<ldl_left_kernel<T, NB, NT, KC>>(NT, smem, &per_sm)) return rc;
+    if (int rc = prepare_kernel<ldl_left_kernel<T, NB, NT, KC, SKIP>>(NT, smem, &per_sm)) return rc;
     grid = std::min(grid, std::max(1, per_sm) * device_sms());
     kern<<<grid, NT, smem, s>>>(p);
     LRES_CUDA_TRY(cudaGetLastError());
     return LRES_OK;
+}
+
+template <class T, int NB, int NT, int KC>
+static int launch_left(const LdlParams<T>& p, int grid, cudaStream_t s) {
+    return p.c0 ? launch_left_v<T, NB, NT, KC, true>(p, grid, s) : launch_left_v<T, NB, NT, KC, false>(p, grid, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -1278,7 +1477,8 @@ int run_ldl(const LdlJob& j, cudaStream_t s) {
         p.mult = nullptr; p.npos = j.npos; p.status = j.status;
         p.ws = (double2*)j.ws; p.ws_stride = j.ws_stride; p.ldp = j.ldp; p.nmax = j.nmax; p.mmax = j.mmax;
         p.keep = j.keep;
-        if (j.keep) return launch_left<double2, kKeepNB128, 256, 32>(p, j.grid, s);
+        p.c0 = j.keep ? nullptr : j.c0;
+        if (j.keep) return launch_left_v<double2, kKeepNB128, 256, 32, false>(p, j.grid, s);
         switch (j.config) {
             case 1: return launch_left<double2, 16, 128, 32>(p, j.grid, s);
             case 2: return launch_left<double2, 16, 256, 16>(p, j.grid, s);
@@ -1296,7 +1496,8 @@ int run_ldl(const LdlJob& j, cudaStream_t s) {
         p.mult = nullptr; p.npos = j.npos; p.status = j.status;
         p.ws = (float2*)j.ws; p.ws_stride = j.ws_stride; p.ldp = j.ldp; p.nmax = j.nmax; p.mmax = j.mmax;
         p.keep = j.keep;
-        if (j.keep) return launch_left<float2, kKeepNB64, 256, 32>(p, j.grid, s);
+        p.c0 = j.keep ? nullptr : j.c0;
+        if (j.keep) return launch_left_v<float2, kKeepNB64, 256, 32, false>(p, j.grid, s);
         switch (j.config) {
             case 1: return launch_left<float2, 32, 128, 32>(p, j.grid, s);
             case 2: return launch_left<float2, 32, 256, 16>(p, j.grid, s);

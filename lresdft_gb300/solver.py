@@ -112,6 +112,18 @@ class LResGPU:
                     self._ctx_of[gr] = k
                 cw = [self.windows[gr[0]] for gr in groups]
                 cown = [np.sort(np.concatenate([self.own[B] for B in gr])) for gr in groups]
+        # within each solved window, the atoms whose functions vanish on every owned point
+        # come first: the owned-point rows are then zero in those leading columns and the
+        # pole kernel starts them at the first column an owned point touches
+        aof = np.asarray(basis.atom_of_fn)
+        ordered = []
+        for W, o in zip(cw, cown):
+            sub = basis.Xr[o]
+            touched = np.zeros(int(aof.max()) + 1, bool)
+            touched[aof[sub.indices[sub.data != 0]]] = True
+            t = touched[aof[W]]
+            ordered.append(np.concatenate([W[~t], W[t]]) if t.any() and not t.all() else W)
+        cw = ordered
         self.ctx_windows, self.ctx_own = cw, cown
         self.ctx_nW = np.array([len(W) for W in cw])
         cWflat = np.concatenate(cw).astype(np.int64)
@@ -289,10 +301,14 @@ class LResGPU:
         K = self.owned_gram()
         rows, blocks = [], []
         for Kw in self.window_blocks(K):
-            lam, V = np.linalg.eigh(Kw)
+            n = Kw.shape[0]
+            nz = np.flatnonzero(np.diag(Kw) > 0)
+            c0 = int(nz[0]) if nz.size else n          # columns before c0: no owned-point value
+            lam, V = np.linalg.eigh(Kw[c0:, c0:])
             top = lam[-1] if lam.size else 0.0
             keep = lam > rtol * top if top > 0 else np.zeros(lam.size, bool)
-            R = np.sqrt(lam[keep])[:, None] * V[:, keep].T
+            R = np.zeros((int(keep.sum()), n))
+            R[:, c0:] = np.sqrt(lam[keep])[:, None] * V[:, keep].T   # exact zeros before c0
             rows.append(R.shape[0])
             blocks.append(R.ravel(order="F"))
         r_w = np.asarray(rows, np.int32)

@@ -39,8 +39,10 @@ def jit2():
 
 
 def _oracle(b, cr, s, v, mu, e_lo, M):
+    """The oracle on the windows the GPU solves (``ctx_windows``: merged, atoms reordered), so
+    that per-window gradients compare in the same layout."""
     from oracle.lrft_adjoint import adjoint
-    return adjoint(b.H(v.ravel()), b.S, b.Xr, s.windows, s.own, cr.dV, mu, e_lo, M)
+    return adjoint(b.H(v.ravel()), b.S, b.Xr, s.ctx_windows, s.ctx_own, cr.dV, mu, e_lo, M)
 
 
 def _solver(b, cr, g, precision):
