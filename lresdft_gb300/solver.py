@@ -71,6 +71,58 @@ def _plain_lcao(basis):
             and hasattr(basis, "Xr"))
 
 
+def solved_windows(basis, windows, own, merge=True):
+    """The windows the GPU solves, from the reference's windows and ownership:
+
+    * windows with identical function sets (R_w reaching across the cell) merged into one
+      with the union of their owned points (N, E_band and the density are sums over owned
+      points of the same resolvent);
+    * within each, the atoms whose functions vanish on every owned point first (whole atoms,
+      each group in its original order): the owned-point rows are then zero in those leading
+      columns and the pole kernel starts them at the first column an owned point touches.
+
+    Returns (windows, owned points, index of the solved window of every input window)."""
+    cw, cown = list(windows), list(own)
+    ctx_of = np.arange(len(windows))
+    if merge:
+        first, groups = {}, []
+        for B, W in enumerate(windows):
+            key = np.asarray(W).tobytes()
+            if key not in first:
+                first[key] = len(groups)
+                groups.append([])
+            groups[first[key]].append(B)
+        if len(groups) < len(windows):
+            for k, gr in enumerate(groups):
+                ctx_of[gr] = k
+            cw = [windows[gr[0]] for gr in groups]
+            cown = [np.sort(np.concatenate([own[B] for B in gr])) for gr in groups]
+    aof = np.asarray(basis.atom_of_fn)
+    ordered = []
+    for W, o in zip(cw, cown):
+        sub = basis.Xr[o]
+        touched = np.zeros(int(aof.max()) + 1, bool)
+        touched[aof[sub.indices[sub.data != 0]]] = True
+        t = touched[aof[W]]
+        ordered.append(np.concatenate([W[~t], W[t]]) if t.any() and not t.all() else W)
+    return ordered, cown, ctx_of
+
+
+def trace_factor(K, rtol=1e-14):
+    """R with R^T R = K (to the eigenvalues above rtol * max) for a window's owned-row Gram
+    matrix K = F^T F: Lambda^1/2 V^T of the block from the first column with a nonzero
+    diagonal on (the columns before it are exactly zero in R, as they are in F)."""
+    n = K.shape[0]
+    nz = np.flatnonzero(np.diag(K) > 0)
+    c0 = int(nz[0]) if nz.size else n
+    lam, V = np.linalg.eigh(K[c0:, c0:])
+    top = lam[-1] if lam.size else 0.0
+    keep = lam > rtol * top if top > 0 else np.zeros(lam.size, bool)
+    R = np.zeros((int(keep.sum()), n))
+    R[:, c0:] = np.sqrt(lam[keep])[:, None] * V[:, keep].T
+    return R
+
+
 class LResGPU:
     """GPU pole-route LRes window solver with the LRFTLCAOCpp interface.
 
@@ -94,36 +146,8 @@ class LResGPU:
         self.Woff = np.concatenate([[0], np.cumsum(self.nW)]).astype(np.int64)
         self.Oflat = np.concatenate(self.own).astype(np.int64)
         self.Ooff = np.concatenate([[0], np.cumsum([len(o) for o in self.own])]).astype(np.int64)
-        # the windows the GPU solves: windows with identical function sets (R_w reaching
-        # across the cell) merged into one with the union of their owned points, since
-        # N, E_band and the density are sums over owned points of the same resolvent
-        cw, cown = self.windows, self.own
-        self._ctx_of = np.arange(len(self.windows))     # solved window of every window
-        if merge_windows:
-            first, groups = {}, []
-            for B, W in enumerate(self.windows):
-                key = W.tobytes()
-                if key not in first:
-                    first[key] = len(groups)
-                    groups.append([])
-                groups[first[key]].append(B)
-            if len(groups) < len(self.windows):
-                for k, gr in enumerate(groups):
-                    self._ctx_of[gr] = k
-                cw = [self.windows[gr[0]] for gr in groups]
-                cown = [np.sort(np.concatenate([self.own[B] for B in gr])) for gr in groups]
-        # within each solved window, the atoms whose functions vanish on every owned point
-        # come first: the owned-point rows are then zero in those leading columns and the
-        # pole kernel starts them at the first column an owned point touches
-        aof = np.asarray(basis.atom_of_fn)
-        ordered = []
-        for W, o in zip(cw, cown):
-            sub = basis.Xr[o]
-            touched = np.zeros(int(aof.max()) + 1, bool)
-            touched[aof[sub.indices[sub.data != 0]]] = True
-            t = touched[aof[W]]
-            ordered.append(np.concatenate([W[~t], W[t]]) if t.any() and not t.all() else W)
-        cw = ordered
+        # the windows the GPU solves (merged identical windows, atoms reordered)
+        cw, cown, self._ctx_of = solved_windows(basis, self.windows, self.own, merge=bool(merge_windows))
         self.ctx_windows, self.ctx_own = cw, cown
         self.ctx_nW = np.array([len(W) for W in cw])
         cWflat = np.concatenate(cw).astype(np.int64)
@@ -301,14 +325,7 @@ class LResGPU:
         K = self.owned_gram()
         rows, blocks = [], []
         for Kw in self.window_blocks(K):
-            n = Kw.shape[0]
-            nz = np.flatnonzero(np.diag(Kw) > 0)
-            c0 = int(nz[0]) if nz.size else n          # columns before c0: no owned-point value
-            lam, V = np.linalg.eigh(Kw[c0:, c0:])
-            top = lam[-1] if lam.size else 0.0
-            keep = lam > rtol * top if top > 0 else np.zeros(lam.size, bool)
-            R = np.zeros((int(keep.sum()), n))
-            R[:, c0:] = np.sqrt(lam[keep])[:, None] * V[:, keep].T   # exact zeros before c0
+            R = trace_factor(Kw, rtol)
             rows.append(R.shape[0])
             blocks.append(R.ravel(order="F"))
         r_w = np.asarray(rows, np.int32)
