@@ -96,3 +96,52 @@ def test_oracle_whole_cell_equals_dense_ks(sysjit2):
     G, kap = dense_ks_gradient(H, b.S, cr.n_elec, cr.dV, mu, e_lo, M)
     assert abs(a["kappa"] - kap) < 1e-12 * abs(kap)
     assert np.max(np.abs(a["gH"] - G)) < 1e-12 * np.max(np.abs(G))
+
+
+def test_pole_route_mu_derivatives_and_gradients(sysjit2):
+    """The combination lres_adjoint evaluates (lresdft_gb300/csrc/adjoint.cu), restated on the
+    pole route in numpy: A_c = Re sum_k c_k Z_k Z_k^T with Z_k = (z_k S - H)^-1 F^T and c in
+    {w, wz, wz^2}, U_c = 4 dV <S, A_c>; with a0 = 1/2 - c/(2R), a1 = 1/(2R):
+        dN/dmu = N/(2R) - (a0 U_w + a1 U_wz),
+        dE/dmu = E/R + N/2 - c N/(2R) - (a0 U_wz + a1 U_wz2),
+        dE/dH_W = 4 dV (A_wz - kappa A_w),  dE/dS_W = -4 dV (A_wz2 - kappa A_wz),
+    against the oracle's closed-form (eigen-route) derivatives."""
+    from scipy import linalg
+    from oracle import lrft_oracle as O
+    from oracle.lrft_adjoint import adjoint
+    g, cr, b = sysjit2
+    windows, own = _setup(b, cr, 5.0)
+    M, dV = int(g["M"]), cr.dV
+    mu, e_lo = float(g["cold_mu"]), float(g["cold_elo"])
+    H = b.H(g["v"].ravel())
+    zs, ws = O.nodes(M, mu, e_lo)
+    N = E = 0.0
+    U = np.zeros(3)
+    As = []
+    for W, o in zip(windows, own):
+        HW, SW = H[W][:, W].toarray(), b.S[W][:, W].toarray()
+        F = b.Xr[o][:, W].toarray()                       # m x n
+        A = np.zeros((3, len(W), len(W)))
+        for z, w in zip(zs, ws):
+            Z = linalg.solve(z * SW - HW, F.T.astype(complex))
+            t = np.sum(F.T * Z)                          # tr(G F^T F)
+            N += 4 * dV * np.real(w * t)
+            E += 4 * dV * np.real(w * z * t)
+            P = Z @ Z.T
+            for c, cw in enumerate((w, w * z, w * z * z)):
+                A[c] += np.real(cw * P)
+        As.append(A)
+        for c in range(3):
+            U[c] += 4 * dV * np.sum(SW * A[c])
+    cc, R = 0.5 * (mu + e_lo), 0.5 * (mu - e_lo)
+    a0, a1 = 0.5 - cc / (2 * R), 1 / (2 * R)
+    dN = N / (2 * R) - (a0 * U[0] + a1 * U[1])
+    dE = E / R + 0.5 * N - cc * N / (2 * R) - (a0 * U[1] + a1 * U[2])
+    kappa = dE / dN
+    o = adjoint(H, b.S, b.Xr, windows, own, dV, mu, e_lo, M)
+    assert abs(N - o["N"]) < 1e-10 * o["N"] and abs(E - o["E"]) < 1e-10 * abs(o["E"])
+    assert abs(dN - o["dNdmu"]) < 1e-9 * abs(o["dNdmu"])
+    assert abs(dE - o["dEdmu"]) < 1e-9 * abs(o["dEdmu"])
+    for A, gH, gS in zip(As, o["dH"], o["dS"]):
+        assert np.max(np.abs(4 * dV * (A[1] - kappa * A[0]) - gH)) < 1e-9 * np.max(np.abs(gH))
+        assert np.max(np.abs(-4 * dV * (A[2] - kappa * A[1]) - gS)) < 1e-9 * np.max(np.abs(gS))
