@@ -209,6 +209,29 @@ int lres_adjoint(lres_ctx* ctx, double mu, double e_lo, double* dv, int dv_on_de
 int lres_owned_gram(lres_ctx* ctx, double* K, int on_device, void* stream);
 int lres_set_trace_rows(lres_ctx* ctx, const int32_t* r_w, const double* R, void* stream);
 
+/* Host assembly of an atom-grouped grid basis (no GPU involved) — replaces the sparse
+ * assembly of LCAOBasis.__init__ and LCAOBasis._matrices (lrft/lcao3d.py:80-96; T_FD of
+ * lrft/three_d.py:151-164).  Input: ngroups groups of functions, group g owning functions
+ * [gptr[g], gptr[g+1]) (1..8) that share one support; cnt[g] tabulated points per group,
+ * their grid indices idx[] concatenated in group order (duplicates allowed: periodic
+ * images of one point, summed in the order given), values val[] concatenated in group
+ * order, each group function-major (function f of group g at point e: val[voff_g + f *
+ * cnt[g] + e]).  Builds X (ng x nb), S = dV X^T X and T = dV X^T T_FD X, where T_FD is
+ * the periodic 7-point stencil with diagonal t_diag and off-diagonal t_off (3/dx^2 and
+ * -0.5/dx^2 for -Lap/2).  Every entry is the sum of the reference's scipy products in
+ * their order (ascending shared index, each product rounded, zero sums dropped), so S
+ * and T equal the reference's bit for bit; threads (nthreads, 0 = all cores) only split
+ * the rows.  nnz[3] receives the entries of X, S and T; lres_basis_fetch copies out X as
+ * CSC (Xp[nb+1], columns = functions) and CSR (Xrp[ng+1]) and S, T as CSR (nb+1
+ * pointers), all with sorted indices; any triple may be NULL to skip it. */
+typedef struct lres_basis lres_basis;
+int lres_basis_build(lres_basis** out, int64_t ngroups, const int64_t* gptr, const int64_t* cnt,
+                     const int64_t* idx, const double* val, const int64_t shape[3], double dV, double t_diag,
+                     double t_off, int nthreads, int64_t* nnz);
+int lres_basis_fetch(const lres_basis* b, int64_t* Xp, int64_t* Xi, double* Xv, int64_t* Xrp, int64_t* Xri,
+                     double* Xrv, int64_t* Sp, int64_t* Si, double* Sv, int64_t* Tp, int64_t* Ti, double* Tv);
+int lres_basis_free(lres_basis* b);
+
 /* Grid kernels on device arrays of ng doubles (context supplies shape and cell). */
 int lres_lda_xc(lres_ctx* ctx, const double* dens, double* exc, double* vxc, void* stream);
 int lres_hartree(lres_ctx* ctx, const double* dens, double* vh, void* stream);

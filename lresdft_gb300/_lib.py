@@ -19,7 +19,8 @@ ERRORS = {-22: "EINVAL", -12: "ENOMEM", -5: "ECUDA", -33: "ENUMERIC", -71: "ESTA
 EXPORTS = ("lres_version", "lres_last_error", "lres_ctx_create", "lres_ctx_destroy", "lres_set_potential",
            "lres_set_hamiltonian_csr", "lres_pass", "lres_pass_async", "lres_status", "lres_density_ptr", "lres_autotune", "lres_timings", "lres_window_sums", "lres_inertia", "lres_min_eig",
            "lres_voronoi_owner", "lres_lda_xc", "lres_hartree", "lres_ion_potential", "lres_inertia_noalloc",
-           "lres_set_windows", "lres_window_ptrs", "lres_adjoint", "lres_owned_gram", "lres_set_trace_rows")
+           "lres_set_windows", "lres_window_ptrs", "lres_adjoint", "lres_owned_gram", "lres_set_trace_rows",
+           "lres_basis_build", "lres_basis_fetch", "lres_basis_free")
 
 
 class LResError(RuntimeError):
@@ -78,6 +79,9 @@ def _load():
         "lres_adjoint": (i32, [vp, dbl, dbl, vp, i32, vp, vp, i32, PD, vp]),
         "lres_owned_gram": (i32, [vp, vp, i32, vp]),
         "lres_set_trace_rows": (i32, [vp, vp, vp, vp]),
+        "lres_basis_build": (i32, [C.POINTER(vp), i64, P64, P64, P64, PD, P64, dbl, dbl, dbl, i32, P64]),
+        "lres_basis_fetch": (i32, [vp, P64, P64, PD, P64, P64, PD, P64, P64, PD, P64, P64, PD]),
+        "lres_basis_free": (i32, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -122,3 +126,24 @@ def voronoi_owner(shape, cell, centres):
     check(lib.lres_voronoi_owner(ptr64(shape), ptrd(cell), centres.shape[0], ptrd(centres),
                                  owner.ctypes.data_as(C.POINTER(C.c_int32))))
     return owner
+
+
+def basis_matrices(gptr, cnt, idx, val, shape, dV, t_diag, t_off, nthreads=0):
+    """Host assembly of the grouped grid basis (lres_basis_build): returns the CSC arrays
+    of X (columns = functions), the CSR arrays of X, S and T, each (indptr, indices, data)."""
+    gptr, cnt, idx, val, shape = i64(gptr), i64(cnt), i64(idx), f64(val), i64(shape)
+    ngroups = len(cnt)
+    h = C.c_void_p()
+    nnz = np.zeros(3, np.int64)
+    check(lib.lres_basis_build(C.byref(h), ngroups, ptr64(gptr), ptr64(cnt), ptr64(idx), ptrd(val), ptr64(shape),
+                               float(dV), float(t_diag), float(t_off), int(nthreads), ptr64(nnz)))
+    try:
+        nb, ng = int(gptr[-1]), int(np.prod(shape))
+        out = []
+        for n_ptr, n in ((nb + 1, nnz[0]), (ng + 1, nnz[0]), (nb + 1, nnz[1]), (nb + 1, nnz[2])):
+            out.append((np.empty(n_ptr, np.int64), np.empty(int(n), np.int64), np.empty(int(n), np.float64)))
+        args = [f(a) for t in out for f, a in zip((ptr64, ptr64, ptrd), t)]
+        check(lib.lres_basis_fetch(h, *args))
+    finally:
+        lib.lres_basis_free(h)
+    return out

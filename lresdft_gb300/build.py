@@ -1,5 +1,7 @@
-"""Build liblres_gb300.so (sm_103a) in-tree with nvcc: every .cu under csrc/ is
-compiled in parallel into _build/, then linked into lresdft_gb300/liblres_gb300.so.
+"""Build liblres_gb300.so (sm_103a) in-tree with nvcc: every .cu (device code) and
+.cpp (host-only code, no FMA contraction so that its sums round as written) under
+csrc/ is compiled in parallel into _build/, then linked into
+lresdft_gb300/liblres_gb300.so.
 
     python -m lresdft_gb300.build            # incremental
     python -m lresdft_gb300.build --force    # rebuild everything
@@ -22,8 +24,11 @@ FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", 
          "--expt-relaxed-constexpr", "-I", os.path.join(os.path.dirname(HERE), "include")]
 
 
+HOST_FLAGS = ["-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-pthread"]
+
+
 def _sources():
-    return sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    return sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
 
 
 def _headers():
@@ -32,7 +37,10 @@ def _headers():
 
 
 def _compile(src, force, extra):
-    obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+    stem, ext = os.path.splitext(os.path.basename(src))
+    obj = os.path.join(BUILD, stem + ".o")
+    if ext == ".cpp":
+        extra = HOST_FLAGS + list(extra)
     newest_dep = max([os.path.getmtime(src)] + [os.path.getmtime(h) for h in _headers()])
     if not force and os.path.exists(obj) and os.path.getmtime(obj) >= newest_dep:
         return obj, None
@@ -53,7 +61,7 @@ def build(force: bool = False, verbose: bool = False, extra=()):
         raise RuntimeError("nvcc failed:\n" + "\n".join(errs))
     objs = [o for o, _ in results]
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
-        cmd = [NVCC, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"]
+        cmd = [NVCC, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart", "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

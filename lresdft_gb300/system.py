@@ -162,9 +162,16 @@ class LCAOBasis:
     """s/p Gaussians times the compact cutoff (1-(r/rcut)^2)^2 tabulated on the grid,
     each normalised on the grid; S = X^T X dV and T = X^T T_FD X dV
     (lrft/lcao3d.py:49-96).  Functions of one atom are contiguous and share one
-    support, which the GPU side uses to assemble H(v) by atom pairs."""
+    support, which the GPU side uses to assemble H(v) by atom pairs.
 
-    def __init__(self, cr: Crystal, rcut=5.5, s_exps=None, p_exps=None, atom_exps=None):
+    The tabulation is numpy, operation by operation as in the reference.  The sparse
+    assembly (X from the tabulated points, X^T X, X^T T_FD X) runs in the native
+    library (``assembly="native"``, lres_basis_build: the reference's scipy sums in
+    their order, per atom pair, on all host cores); ``assembly="scipy"`` forms them
+    with scipy.sparse as the reference does."""
+
+    def __init__(self, cr: Crystal, rcut=5.5, s_exps=None, p_exps=None, atom_exps=None, assembly="native",
+                 nthreads=0):
         self.cr, self.rcut = cr, rcut
         s_exps = S_EXPS if s_exps is None else s_exps
         p_exps = P_EXPS if p_exps is None else p_exps
@@ -172,8 +179,7 @@ class LCAOBasis:
         n1, n2, n3 = cr.shape
         rad = int(np.ceil(rcut / dx))
         off = np.arange(-rad, rad + 1)
-        rows, cols, vals = [], [], []
-        atom_of_fn, fn_ptr = [], [0]
+        idxs, blocks, atom_of_fn, fn_ptr = [], [], [], [0]
         fn = 0
         for a, R in enumerate(cr.pos):
             if atom_exps is not None:
@@ -192,23 +198,44 @@ class LCAOBasis:
             for al in p_exps:
                 g = np.exp(-al * r**2) * cut
                 funcs += [d[:, 0] * g, d[:, 1] * g, d[:, 2] * g]
-            for f in funcs:
-                f = f / np.sqrt(np.sum(f**2) * cr.dV)
-                rows.append(idx)
-                cols.append(np.full(idx.size, fn))
-                vals.append(f)
-                atom_of_fn.append(a)
-                fn += 1
+            idxs.append(idx)
+            blocks.append([f / np.sqrt(np.sum(f**2) * cr.dV) for f in funcs])
+            atom_of_fn += [a] * len(funcs)
+            fn += len(funcs)
             fn_ptr.append(fn)
         self.nb = fn
         self.atom_of_fn = np.array(atom_of_fn)
         self.atom_fn_ptr = np.array(fn_ptr, dtype=np.int64)   # functions of atom a: [ptr[a], ptr[a+1])
-        self.X = sparse.csc_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
-                                   shape=(cr.ng, fn))
-        self.Xr = self.X.tocsr()
-        self._matrices()
+        if assembly == "native":
+            self._assemble_native(idxs, blocks, nthreads)
+        elif assembly == "scipy":
+            rows = [idx for idx, blk in zip(idxs, blocks) for _ in blk]
+            cols = [np.full(idx.size, f) for f, idx in enumerate(rows)]
+            self.X = sparse.csc_matrix((np.concatenate([f for blk in blocks for f in blk]),
+                                        (np.concatenate(rows), np.concatenate(cols))), shape=(cr.ng, fn))
+            self.Xr = self.X.tocsr()
+            self._matrices()
+        else:
+            raise ValueError(f"assembly must be 'native' or 'scipy', not {assembly!r}")
+
+    def _assemble_native(self, idxs, blocks, nthreads):
+        from . import _lib
+        cr = self.cr
+        dx = cr.dx
+        cnt = np.array([idx.size for idx in idxs], np.int64)
+        (Xp, Xi, Xv), (Rp, Ri, Rv), (Sp, Si, Sv), (Tp, Ti, Tv) = _lib.basis_matrices(
+            self.atom_fn_ptr, cnt, np.concatenate(idxs), np.concatenate([f for blk in blocks for f in blk]),
+            cr.shape, cr.dV, 3.0 / dx**2, -0.5 / dx**2, nthreads)
+        ng, nb = cr.ng, self.nb
+        self.X = sparse.csc_matrix((Xv, Xi, Xp), shape=(ng, nb))
+        self.Xr = sparse.csr_matrix((Rv, Ri, Rp), shape=(ng, nb))
+        self.S = sparse.csr_matrix((Sv, Si, Sp), shape=(nb, nb))
+        self.T = sparse.csr_matrix((Tv, Ti, Tp), shape=(nb, nb))
+        for A in (self.X, self.Xr, self.S, self.T):
+            A.has_sorted_indices = True
 
     def _matrices(self):
+        """S and T with scipy.sparse, as the reference forms them (lrft/lcao3d.py:86-96)."""
         dV = self.cr.dV
         self.S = (self.X.T @ self.X).tocsr() * dV
         T = fd_hamiltonian(self.cr, np.zeros(self.cr.shape))
