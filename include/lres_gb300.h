@@ -30,6 +30,7 @@
  *   lres_lda_xc                 lrft/three_d.py:132-148
  *   lres_hartree                lrft/three_d.py:122-129
  *   lres_ion_potential          lrft/three_d.py:102-112,119 (erf part; no GTH short-range term)
+ *   lres_basis_build / _fetch   the sparse assembly of LCAOBasis (lrft/lcao3d.py:86-96), on the host
  */
 #ifndef LRES_GB300_H
 #define LRES_GB300_H
@@ -43,7 +44,7 @@ extern "C" {
 enum {
     LRES_OK = 0,
     LRES_EINVAL = -22,     /* bad argument or inconsistent input */
-    LRES_ENOMEM = -12,     /* device allocation failed */
+    LRES_ENOMEM = -12,     /* allocation failed (device; host memory for lres_basis_build) */
     LRES_ECUDA = -5,       /* CUDA runtime error */
     LRES_ENUMERIC = -33,   /* a zero or non-finite pivot in some window (per-window status kept) */
     LRES_ESTATE = -71      /* call out of order (e.g. lres_pass before a Hamiltonian was set) */
@@ -210,7 +211,7 @@ int lres_owned_gram(lres_ctx* ctx, double* K, int on_device, void* stream);
 int lres_set_trace_rows(lres_ctx* ctx, const int32_t* r_w, const double* R, void* stream);
 
 /* Host assembly of an atom-grouped grid basis (no GPU involved) — replaces the sparse
- * assembly of LCAOBasis.__init__ and LCAOBasis._matrices (lrft/lcao3d.py:80-96; T_FD of
+ * assembly of LCAOBasis.__init__ and LCAOBasis._matrices (lrft/lcao3d.py:86-96; T_FD of
  * lrft/three_d.py:151-164).  Input: ngroups groups of functions, group g owning functions
  * [gptr[g], gptr[g+1]) (1..8) that share one support; cnt[g] tabulated points per group,
  * their grid indices idx[] concatenated in group order (duplicates allowed: periodic
