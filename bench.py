@@ -39,10 +39,10 @@ WORKLOAD = dict(workload="8x8x8 H2 crystal, 1024 electrons, a=4.5, jitter U(+-0.
                 grid="64^3", l2="inputs larger than L2 (no flush)")
 
 
-def build_system(cells=8):
+def build_system(cells=8, assembly="native"):
     from lresdft_gb300 import system
     cr = system.jittered_h2((cells,) * 3, a=4.5, bond=1.4, pts_per_cell=8, jitter=0.1, seed=0)
-    return cr, system.LCAOBasis(cr)
+    return cr, system.LCAOBasis(cr, assembly=assembly)
 
 
 def read_peaks():
@@ -406,7 +406,7 @@ def run_reference(args):
     if rank != 0:
         return
     from oracle import lrft_oracle as orc
-    cr, b = build_system()
+    cr, b = build_system(assembly="scipy")      # the reference's own scipy assembly
     # the potential and (mu, e_lo) of the reference's own cold call (tests/golden/jit8.npz)
     g = np.load(os.path.join(ROOT, "tests", "golden", "jit8.npz"))
     vion = orc.ion_potential(cr)
