@@ -25,7 +25,7 @@ extern "C" void lres_set_error(const char* fmt, ...);
 
 namespace {
 
-constexpr int kLanes = 8;   // functions per group, padded
+constexpr int kMaxLanes = 8;   // functions per group
 
 struct Rows {                // one group's output rows (S or T)
     std::vector<int64_t> cnt;     // entries per function row
@@ -61,11 +61,11 @@ void parallel_for(int nthreads, int64_t n, F&& body) {
 
 struct lres_basis {
     int64_t nb = 0, ng = 0, ngroups = 0;
-    int nthreads = 1;
+    int nthreads = 1, lanes = 1;
     std::vector<int64_t> gptr;
-    // group supports: grid indices ascending, values padded to 8 lanes per point
+    // group supports: grid indices ascending, values in `lanes` lanes per point
     std::vector<int64_t> sptr, sidx;
-    std::vector<double> sval;            // [slot][8]
+    std::vector<double> sval;            // [slot][lanes]
     // point -> (group, slot), groups ascending within a point
     std::vector<int64_t> pptr;
     std::vector<int32_t> pgrp;
@@ -73,45 +73,13 @@ struct lres_basis {
     std::vector<Rows> S, T;               // rows of each group
 };
 
-extern "C" int lres_basis_build(lres_basis** out, int64_t ngroups, const int64_t* gptr, const int64_t* cnt,
-                                const int64_t* idx, const double* val, const int64_t shape[3], double dV,
-                                double t_diag, double t_off, int nthreads, int64_t* nnz) {
-    if (!out || !gptr || !cnt || !shape || !nnz || ngroups <= 0) {
-        lres_set_error("lres_basis_build: null argument or no groups");
-        return LRES_EINVAL;
-    }
-    *out = nullptr;
-    for (int i = 0; i < 3; ++i)
-        if (shape[i] < 1) {
-            lres_set_error("lres_basis_build: grid shape must be positive");
-            return LRES_EINVAL;
-        }
-    if (gptr[0] != 0) {
-        lres_set_error("lres_basis_build: gptr must start at 0");
-        return LRES_EINVAL;
-    }
-    int64_t nent = 0;
-    for (int64_t g = 0; g < ngroups; ++g) {
-        const int64_t nf = gptr[g + 1] - gptr[g];
-        if (nf < 1 || nf > kLanes || cnt[g] < 0) {
-            lres_set_error("lres_basis_build: group %lld has %lld functions (1..8) and %lld points", (long long)g,
-                           (long long)nf, (long long)cnt[g]);
-            return LRES_EINVAL;
-        }
-        nent += cnt[g];
-    }
-    if (nent && (!idx || !val)) {
-        lres_set_error("lres_basis_build: null idx / val");
-        return LRES_EINVAL;
-    }
+// The assembly with L value lanes per grid point (L = the largest group; lanes past a
+// group's own functions hold zeros).
+template <int L>
+int build(lres_basis** out, int64_t ngroups, const int64_t* gptr, const int64_t* cnt, const int64_t* idx,
+          const double* val, const int64_t shape[3], double dV, double t_diag, double t_off, int nthreads,
+          int64_t* nnz) {
     const int64_t n1 = shape[0], n2 = shape[1], n3 = shape[2], ng = n1 * n2 * n3;
-    for (int64_t e = 0; e < nent; ++e)
-        if (idx[e] < 0 || idx[e] >= ng) {
-            lres_set_error("lres_basis_build: grid index %lld out of range", (long long)idx[e]);
-            return LRES_EINVAL;
-        }
-    if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
-
     lres_basis* b = nullptr;
     try {
         b = new lres_basis;
@@ -119,6 +87,7 @@ extern "C" int lres_basis_build(lres_basis** out, int64_t ngroups, const int64_t
         b->ng = ng;
         b->ngroups = ngroups;
         b->nthreads = nthreads;
+        b->lanes = L;
         b->gptr.assign(gptr, gptr + ngroups + 1);
         std::vector<int64_t> eoff(ngroups + 1, 0), voff(ngroups + 1, 0);
         for (int64_t g = 0; g < ngroups; ++g) {
@@ -141,13 +110,13 @@ extern "C" int lres_basis_build(lres_basis** out, int64_t ngroups, const int64_t
             auto& ov = gval[g];
             for (int64_t k = 0; k < c;) {
                 const int64_t r = ix[perm[k]];
-                double acc[kLanes] = {0};
+                double acc[L] = {0};
                 for (int f = 0; f < nf; ++f) acc[f] = v[f * c + perm[k]];
                 int64_t j = k + 1;
                 for (; j < c && ix[perm[j]] == r; ++j)
                     for (int f = 0; f < nf; ++f) acc[f] += v[f * c + perm[j]];
                 oi.push_back(r);
-                ov.insert(ov.end(), acc, acc + kLanes);
+                ov.insert(ov.end(), acc, acc + L);
                 k = j;
             }
         });
@@ -155,10 +124,10 @@ extern "C" int lres_basis_build(lres_basis** out, int64_t ngroups, const int64_t
         for (int64_t g = 0; g < ngroups; ++g) b->sptr[g + 1] = b->sptr[g] + (int64_t)gidx[g].size();
         const int64_t nslot = b->sptr[ngroups];
         b->sidx.resize(nslot);
-        b->sval.resize((size_t)nslot * kLanes);
+        b->sval.resize((size_t)nslot * L);
         parallel_for(nthreads, ngroups, [&](int64_t g, int) {
             std::copy(gidx[g].begin(), gidx[g].end(), b->sidx.begin() + b->sptr[g]);
-            std::copy(gval[g].begin(), gval[g].end(), b->sval.begin() + b->sptr[g] * kLanes);
+            std::copy(gval[g].begin(), gval[g].end(), b->sval.begin() + b->sptr[g] * L);
             std::vector<int64_t>().swap(gidx[g]);
             std::vector<double>().swap(gval[g]);
         });
@@ -246,13 +215,13 @@ extern "C" int lres_basis_build(lres_basis** out, int64_t ngroups, const int64_t
                             l = (int32_t)sc.touched.size();
                             sc.loc[g] = l;
                             sc.touched.push_back(g);
-                            if ((size_t)(l + 1) * kLanes > sc.acc.size()) sc.acc.resize((size_t)(l + 1) * kLanes * 2);
-                            std::fill(sc.acc.begin() + (size_t)l * kLanes, sc.acc.begin() + (size_t)(l + 1) * kLanes, 0.0);
+                            if ((size_t)(l + 1) * L > sc.acc.size()) sc.acc.resize((size_t)(l + 1) * L * 2);
+                            std::fill(sc.acc.begin() + (size_t)l * L, sc.acc.begin() + (size_t)(l + 1) * L, 0.0);
                         }
-                        const double* x = &b->sval[(size_t)b->pslot[p] * kLanes];
-                        double* a = &sc.acc[(size_t)l * kLanes];
+                        const double* x = &b->sval[(size_t)b->pslot[p] * L];
+                        double* a = &sc.acc[(size_t)l * L];
                         const double cf = coef[q];
-                        for (int h = 0; h < kLanes; ++h) a[h] += cf * x[h];
+                        for (int h = 0; h < L; ++h) a[h] += cf * x[h];
                     }
                 }
                 sc.order.assign(sc.touched.begin(), sc.touched.end());
@@ -260,8 +229,8 @@ extern "C" int lres_basis_build(lres_basis** out, int64_t ngroups, const int64_t
                 yc.push_back((int64_t)sc.order.size());
                 for (int32_t g : sc.order) {
                     yg.push_back(g);
-                    const double* a = &sc.acc[(size_t)sc.loc[g] * kLanes];
-                    yv.insert(yv.end(), a, a + kLanes);
+                    const double* a = &sc.acc[(size_t)sc.loc[g] * L];
+                    yv.insert(yv.end(), a, a + L);
                 }
                 for (int32_t g : sc.touched) sc.loc[g] = -1;
             }
@@ -276,13 +245,13 @@ extern "C" int lres_basis_build(lres_basis** out, int64_t ngroups, const int64_t
                 }
         }
         std::vector<int32_t> Yg(yptr[ng]);
-        std::vector<double> Yv((size_t)yptr[ng] * kLanes);
+        std::vector<double> Yv((size_t)yptr[ng] * L);
         {
             std::vector<int64_t> chstart(nchunk + 1, 0);
             for (int64_t ch = 0; ch < nchunk; ++ch) chstart[ch + 1] = chstart[ch] + (int64_t)ygrp[ch].size();
             parallel_for(nthreads, nchunk, [&](int64_t ch, int) {
                 std::copy(ygrp[ch].begin(), ygrp[ch].end(), Yg.begin() + chstart[ch]);
-                std::copy(yval[ch].begin(), yval[ch].end(), Yv.begin() + chstart[ch] * kLanes);
+                std::copy(yval[ch].begin(), yval[ch].end(), Yv.begin() + chstart[ch] * L);
                 std::vector<int32_t>().swap(ygrp[ch]);
                 std::vector<double>().swap(yval[ch]);
             });
@@ -306,11 +275,11 @@ extern "C" int lres_basis_build(lres_basis** out, int64_t ngroups, const int64_t
                 l = (int32_t)A.touched.size();
                 A.loc[g] = l;
                 A.touched.push_back(g);
-                const size_t need = (size_t)(l + 1) * kLanes * kLanes;
+                const size_t need = (size_t)(l + 1) * L * L;
                 if (need > A.a.size()) A.a.resize(need * 2);
-                std::fill(A.a.begin() + (size_t)l * kLanes * kLanes, A.a.begin() + need, 0.0);
+                std::fill(A.a.begin() + (size_t)l * L * L, A.a.begin() + need, 0.0);
             }
-            return &A.a[(size_t)l * kLanes * kLanes];
+            return &A.a[(size_t)l * L * L];
         };
         auto emit = [&](Acc& A, int64_t ga, Rows& out) {
             const int nfa = (int)(gptr[ga + 1] - gptr[ga]);
@@ -320,7 +289,7 @@ extern "C" int lres_basis_build(lres_basis** out, int64_t ngroups, const int64_t
             for (int f = 0; f < nfa; ++f)
                 for (int32_t g : order) {
                     const int nfb = (int)(gptr[g + 1] - gptr[g]);
-                    const double* a = &A.a[((size_t)A.loc[g] * kLanes + f) * kLanes];
+                    const double* a = &A.a[((size_t)A.loc[g] * L + f) * L];
                     for (int h = 0; h < nfb; ++h)
                         if (a[h] != 0.0) {
                             out.col.push_back(gptr[g] + h);
@@ -335,21 +304,21 @@ extern "C" int lres_basis_build(lres_basis** out, int64_t ngroups, const int64_t
             const int nfa = (int)(gptr[ga + 1] - gptr[ga]);
             for (int64_t s = b->sptr[ga]; s < b->sptr[ga + 1]; ++s) {
                 const int64_t r = b->sidx[s];
-                const double* xa = &b->sval[(size_t)s * kLanes];
+                const double* xa = &b->sval[(size_t)s * L];
                 for (int64_t p = b->pptr[r]; p < b->pptr[r + 1]; ++p) {
                     double* a = slot_of(accS[t], b->pgrp[p]);
-                    const double* xb = &b->sval[(size_t)b->pslot[p] * kLanes];
+                    const double* xb = &b->sval[(size_t)b->pslot[p] * L];
                     for (int f = 0; f < nfa; ++f) {
                         const double xf = xa[f];
-                        for (int h = 0; h < kLanes; ++h) a[f * kLanes + h] += xf * xb[h];
+                        for (int h = 0; h < L; ++h) a[f * L + h] += xf * xb[h];
                     }
                 }
                 for (int64_t p = yptr[r]; p < yptr[r + 1]; ++p) {
                     double* a = slot_of(accT[t], Yg[p]);
-                    const double* yb = &Yv[(size_t)p * kLanes];
+                    const double* yb = &Yv[(size_t)p * L];
                     for (int f = 0; f < nfa; ++f) {
                         const double xf = xa[f];
-                        for (int h = 0; h < kLanes; ++h) a[f * kLanes + h] += xf * yb[h];
+                        for (int h = 0; h < L; ++h) a[f * L + h] += xf * yb[h];
                     }
                 }
             }
@@ -374,6 +343,59 @@ extern "C" int lres_basis_build(lres_basis** out, int64_t ngroups, const int64_t
     return LRES_OK;
 }
 
+extern "C" int lres_basis_build(lres_basis** out, int64_t ngroups, const int64_t* gptr, const int64_t* cnt,
+                                const int64_t* idx, const double* val, const int64_t shape[3], double dV,
+                                double t_diag, double t_off, int nthreads, int64_t* nnz) {
+    if (!out || !gptr || !cnt || !shape || !nnz || ngroups <= 0) {
+        lres_set_error("lres_basis_build: null argument or no groups");
+        return LRES_EINVAL;
+    }
+    *out = nullptr;
+    for (int i = 0; i < 3; ++i)
+        if (shape[i] < 1) {
+            lres_set_error("lres_basis_build: grid shape must be positive");
+            return LRES_EINVAL;
+        }
+    if (gptr[0] != 0) {
+        lres_set_error("lres_basis_build: gptr must start at 0");
+        return LRES_EINVAL;
+    }
+    int64_t nent = 0;
+    for (int64_t g = 0; g < ngroups; ++g) {
+        const int64_t nf = gptr[g + 1] - gptr[g];
+        if (nf < 1 || nf > kMaxLanes || cnt[g] < 0) {
+            lres_set_error("lres_basis_build: group %lld has %lld functions (1..8) and %lld points", (long long)g,
+                           (long long)nf, (long long)cnt[g]);
+            return LRES_EINVAL;
+        }
+        nent += cnt[g];
+    }
+    if (nent && (!idx || !val)) {
+        lres_set_error("lres_basis_build: null idx / val");
+        return LRES_EINVAL;
+    }
+    const int64_t n1 = shape[0], n2 = shape[1], n3 = shape[2], ng = n1 * n2 * n3;
+    for (int64_t e = 0; e < nent; ++e)
+        if (idx[e] < 0 || idx[e] >= ng) {
+            lres_set_error("lres_basis_build: grid index %lld out of range", (long long)idx[e]);
+            return LRES_EINVAL;
+        }
+    if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
+
+    int nfmax = 1;
+    for (int64_t g = 0; g < ngroups; ++g) nfmax = std::max<int>(nfmax, (int)(gptr[g + 1] - gptr[g]));
+    switch (nfmax) {
+        case 1: return build<1>(out, ngroups, gptr, cnt, idx, val, shape, dV, t_diag, t_off, nthreads, nnz);
+        case 2: return build<2>(out, ngroups, gptr, cnt, idx, val, shape, dV, t_diag, t_off, nthreads, nnz);
+        case 3: return build<3>(out, ngroups, gptr, cnt, idx, val, shape, dV, t_diag, t_off, nthreads, nnz);
+        case 4: return build<4>(out, ngroups, gptr, cnt, idx, val, shape, dV, t_diag, t_off, nthreads, nnz);
+        case 5: return build<5>(out, ngroups, gptr, cnt, idx, val, shape, dV, t_diag, t_off, nthreads, nnz);
+        case 6: return build<6>(out, ngroups, gptr, cnt, idx, val, shape, dV, t_diag, t_off, nthreads, nnz);
+        case 7: return build<7>(out, ngroups, gptr, cnt, idx, val, shape, dV, t_diag, t_off, nthreads, nnz);
+        default: return build<8>(out, ngroups, gptr, cnt, idx, val, shape, dV, t_diag, t_off, nthreads, nnz);
+    }
+}
+
 extern "C" int lres_basis_fetch(const lres_basis* b, int64_t* Xp, int64_t* Xi, double* Xv, int64_t* Xrp, int64_t* Xri,
                                 double* Xrv, int64_t* Sp, int64_t* Si, double* Sv, int64_t* Tp, int64_t* Ti,
                                 double* Tv) {
@@ -396,7 +418,7 @@ extern "C" int lres_basis_fetch(const lres_basis* b, int64_t* Xp, int64_t* Xi, d
                     const int64_t at = base[g] + f * len;
                     for (int64_t s = 0; s < len; ++s) {
                         Xi[at + s] = b->sidx[b->sptr[g] + s];
-                        Xv[at + s] = b->sval[(size_t)(b->sptr[g] + s) * kLanes + f];
+                        Xv[at + s] = b->sval[(size_t)(b->sptr[g] + s) * b->lanes + f];
                     }
                     Xp[gp[g] + f + 1] = at + len;
                 }
@@ -417,7 +439,7 @@ extern "C" int lres_basis_fetch(const lres_basis* b, int64_t* Xp, int64_t* Xi, d
                         const int32_t g = b->pgrp[p];
                         for (int64_t f = 0; f < gp[g + 1] - gp[g]; ++f) {
                             Xri[at] = gp[g] + f;
-                            Xrv[at] = b->sval[(size_t)b->pslot[p] * kLanes + f];
+                            Xrv[at] = b->sval[(size_t)b->pslot[p] * b->lanes + f];
                             ++at;
                         }
                     }
