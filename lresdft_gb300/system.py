@@ -179,14 +179,20 @@ class LCAOBasis:
         n1, n2, n3 = cr.shape
         rad = int(np.ceil(rcut / dx))
         off = np.arange(-rad, rad + 1)
+        cube = np.stack(np.meshgrid(off, off, off, indexing="ij"), -1).reshape(-1, 3)
+        if assembly == "native" and np.all((rad + 1) * dx < 0.5 * np.asarray(cr.cell, float)):
+            # The cube stays inside half the cell, so the minimum image leaves every offset
+            # as it is, and offsets more than rad + 1 points from the centre lie farther than
+            # (rad + 1 - sqrt(3)/2) dx > rcut: the mask below would drop them.  Leaving them
+            # out keeps the same points in the same order with the same values.
+            cube = cube[np.sum(cube**2, axis=1) <= (rad + 1) ** 2]
         idxs, blocks, atom_of_fn, fn_ptr = [], [], [], [0]
         fn = 0
         for a, R in enumerate(cr.pos):
             if atom_exps is not None:
                 s_exps, p_exps = atom_exps[a]
             c = np.round(R / dx).astype(int)
-            I, J, K = np.meshgrid(c[0] + off, c[1] + off, c[2] + off, indexing="ij")
-            P = np.stack([I, J, K], -1).reshape(-1, 3)
+            P = c + cube
             d = P * dx - R
             d = min_image(d, cr.cell)
             r = np.linalg.norm(d, axis=1)
