@@ -178,3 +178,23 @@ def test_stale_mu_retries_cold(case):
     n, e, mu = s.density(v)
     assert raised and abs(mu - g["cold_mu"]) < 1e-9 and abs(e - g["cold_eband"]) < 1e-9
     assert np.max(np.abs(n.ravel() - g["cold_dens"])) < 1e-10
+
+
+def test_solve_mu_fixed_n(case):
+    """solve_mu_fixed_n (the mu solve at fixed N behind BandEnergy and the finite-difference
+    checks): a bracket grown from the current mu by slope steps, then Brent's method, to
+    |N(mu) - N| <= tol on passes without density; the root of the closed-form count."""
+    from scipy.optimize import brentq
+    g, cr, b = case
+    s = _make(case)
+    v = g["v"].reshape(cr.shape)
+    s.density(v)
+    s.set_potential(1.002 * v)
+    mu, N, E = s.solve_mu_fixed_n(tol=1e-10)
+    assert abs(N - cr.n_elec) <= 1e-10
+
+    def count(m):
+        return s.pole_pass(m, s.e_lo, want_density=False)[1] - cr.n_elec
+    ref = brentq(count, s.e_lo + 1e-6, s.mu + 1.0, xtol=1e-15)
+    assert abs(mu - ref) < 1e-9
+    assert abs(E - s.pole_pass(mu, s.e_lo, want_density=False)[2]) == 0.0
