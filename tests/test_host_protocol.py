@@ -198,3 +198,33 @@ def test_solve_mu_fixed_n(case):
     ref = brentq(count, s.e_lo + 1e-6, s.mu + 1.0, xtol=1e-15)
     assert abs(mu - ref) < 1e-9
     assert abs(E - s.pole_pass(mu, s.e_lo, want_density=False)[2]) == 0.0
+
+
+class _HostGrid:
+    """The grid steps of the SCF driver answered by the oracle on the host."""
+
+    def __init__(self, cr):
+        self.cr = cr
+
+    def ion_potential(self):
+        from oracle import lrft_oracle as O
+        return O.ion_potential(self.cr)
+
+    def lda_hartree(self, dens):
+        from oracle import lrft_oracle as O
+        exc, vxc = O.lda_xc(dens)
+        return exc, vxc, O.hartree(self.cr, dens)
+
+
+def test_scf_driver_reproduces_reference_scf(case):
+    """lresdft_gb300.scf.scf_lcao (DIIS over 6 histories, mix 0.4, clamp, renormalisation,
+    Harris-Foulkes energy; lrft/lcao3d.py:237-284) over the host-backed solver and grid: the
+    reference's LRFTLCAOCpp(reuse_vectors=False) SCF to tol 1e-8, same iteration count,
+    energy to 1e-10 Ha/electron, final input density to 1e-9."""
+    from lresdft_gb300.scf import scf_lcao
+    g, cr, b = case
+    s = _make(case)
+    r = scf_lcao(cr, s, tol=1e-8, maxiter=60, grid=_HostGrid(cr))
+    assert r["converged"] and r["iterations"] == int(g["scf_iterations"])
+    assert abs(r["energy"] - float(g["scf_energy"])) / cr.n_elec < 1e-10
+    assert np.max(np.abs(r["dens_in"].ravel() - g["scf_dens_in"])) < 1e-9
