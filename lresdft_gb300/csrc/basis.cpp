@@ -281,20 +281,20 @@ int build(lres_basis** out, int64_t ngroups, const int64_t* gptr, const int64_t*
             }
             return &A.a[(size_t)l * L * L];
         };
-        auto emit = [&](Acc& A, int64_t ga, Rows& out) {
+        auto emit = [&](Acc& A, int64_t ga, Rows& rows) {
             const int nfa = (int)(gptr[ga + 1] - gptr[ga]);
             std::vector<int32_t> order(A.touched);
             std::sort(order.begin(), order.end());
-            out.cnt.assign(nfa, 0);
+            rows.cnt.assign(nfa, 0);
             for (int f = 0; f < nfa; ++f)
                 for (int32_t g : order) {
                     const int nfb = (int)(gptr[g + 1] - gptr[g]);
                     const double* a = &A.a[((size_t)A.loc[g] * L + f) * L];
                     for (int h = 0; h < nfb; ++h)
                         if (a[h] != 0.0) {
-                            out.col.push_back(gptr[g] + h);
-                            out.val.push_back(a[h] * dV);
-                            ++out.cnt[f];
+                            rows.col.push_back(gptr[g] + h);
+                            rows.val.push_back(a[h] * dV);
+                            ++rows.cnt[f];
                         }
                 }
             for (int32_t g : A.touched) A.loc[g] = -1;
