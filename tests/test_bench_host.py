@@ -1,0 +1,59 @@
+"""bench.py's host side on the CPU: the reference arm's JSON line carries every key of the
+benchmark contract (run on a 2x2x2 crystal instead of the 1024-electron workload), the
+nvidia-smi clock samples are parsed into the `clocks` object, and the algorithmic work of
+the roofline is (32/3) n^3 real flops per window-pole solve."""
+import json
+import types
+
+import numpy as np
+
+KEYS = ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+        "vs_baseline", "dtype", "data", "config", "e2e", "cpu_baseline")
+
+
+def test_reference_arm_line(monkeypatch, capsys):
+    import bench
+    from lresdft_gb300 import system
+    cr = system.jittered_h2((2, 2, 2), a=4.5, bond=1.4, pts_per_cell=8, jitter=0.1, seed=0)
+    seen = {}
+
+    def small_system(cells=8, assembly="native"):
+        seen["assembly"] = assembly
+        return cr, system.LCAOBasis(cr, assembly=assembly)
+
+    monkeypatch.setattr(bench, "build_system", small_system)
+    bench.run_reference(types.SimpleNamespace(steps=1, warmup=3))
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert seen["assembly"] == "scipy"          # the reference's own basis assembly
+    assert all(k in line for k in KEYS) and line["impl"] == "reference"
+    assert line["value"] > 0 and line["higher_is_better"] is True and line["vs_baseline"] is None
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["cpu_baseline"]["value"] == line["value"] == line["e2e"]["value"]
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+    assert "workload" in line["config"]
+
+
+def test_clock_samples_parsed():
+    import bench
+    c = bench.Clocks()
+    c.f.write("0, 1965, 2070, 900.50, 0x0000000000000004, Not Active, Not Active, Not Active, Active\n"
+              "0, 1980, 2070, 950.10, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active\n"
+              "0, 2010, 2070, 990.00, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active\n")
+
+    class Proc:
+        def terminate(self):
+            pass
+
+        def wait(self):
+            pass
+
+    c.p = Proc()
+    out = c.stop()
+    assert out["sm_mhz"] == 1980.0 and out["sm_max_mhz"] == 2070.0 and out["samples"] == 3
+    assert out["reasons"] == ["sw_power_cap"]
+
+
+def test_algorithmic_flops():
+    import bench
+    nW = np.array([264, 288, 312])
+    assert bench.algorithmic_flops(nW, 32) == 32 * (32.0 / 3.0) * float(np.sum(nW.astype(float) ** 3))
