@@ -11,16 +11,20 @@ warm/cold decisions:
 * warm step (lrft/lcao3d.py:413-448): keep mu and e_lo if the smallest window
   eigenvalue lies in (e_lo + margin/3, e_lo + 2 margin) and below the truncation
   edge c + 1.5 R; the reference reads it from its window spectra, here two
-  Sylvester-inertia counts decide it; keep mu if |N(mu) - N| <= 1e-8 N, else solve
-  for mu and return the density of a pass at the new mu (the reference with
-  reuse_vectors=False; the pole route stores no eigenvectors, so reuse_vectors is
-  accepted for signature compatibility only);
+  Sylvester-inertia counts decide it; keep mu if |N(mu) - N| <= 1e-8 N (1e-7 N in
+  mixed precision, the FP32 count-noise floor), else solve for mu and return the
+  density of a pass at the new mu (the reference with reuse_vectors=False; the pole
+  route stores no eigenvectors, so reuse_vectors is accepted for signature
+  compatibility only);
 * cold step (lrft/lcao3d.py:449-456): e_lo = lambda_min - margin with lambda_min
-  from inertia bisection, then mu from the bracket [max(lambda_min, e_lo+1e-6), +1]
-  widened by 0.5 (lrft/lcao3d.py:387-398).
+  from inertia bisection; mu bracketed from the previous accepted mu when there is one
+  (the count is monotone in mu, so the root is the same), else from
+  [max(lambda_min, e_lo+1e-6), +1] widened by 0.5 (lrft/lcao3d.py:387-398).
 
 Each N(mu) evaluation is a full pole pass (the poles move with mu), so mu is found
 by Brent's method on pass results; the last pass at the accepted mu is the density.
+With trace rows installed (fine grids) the trial passes run over them and produce no
+density; the accepted mu then gets one density pass over the owned points.
 """
 from __future__ import annotations
 
