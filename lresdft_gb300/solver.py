@@ -137,8 +137,14 @@ class LResGPU:
 
     def __init__(self, basis, cells, R_w=12.1, M=64, margin=0.3, nthreads=1, lag_mu=False, reuse_vectors=True,
                  precision="fp64", tile_config=None, trace_rows="auto", merge_windows="auto"):
-        if M % 2:
-            raise ValueError("M must be even")
+        if M % 2 or M < 2:
+            raise ValueError(f"M must be even and >= 2 (got {M})")
+        if precision not in ("fp64", "mixed"):
+            raise ValueError(f"precision must be 'fp64' or 'mixed' (got {precision!r})")
+        if not R_w > 0:
+            raise ValueError(f"R_w must be positive (got {R_w})")
+        if not (tile_config is None or tile_config == "auto" or tile_config in range(6)):
+            raise ValueError(f"tile_config must be None, 'auto' or 0..5 (got {tile_config!r})")
         self.b, self.M, self.margin = basis, M, margin
         self.lag_mu, self.reuse_vectors, self.nthreads = lag_mu, reuse_vectors, nthreads
         self.precision = precision

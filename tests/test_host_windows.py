@@ -75,3 +75,17 @@ def test_trace_factor():
     assert R.shape[0] == min(m, n - c0)
     assert np.all(R[:, :c0] == 0.0)
     assert np.max(np.abs(R.T @ R - K)) < 1e-12 * np.max(np.abs(K))
+
+
+@pytest.mark.parametrize("kw", [dict(M=63), dict(M=0), dict(precision="fp32"), dict(R_w=0.0),
+                                dict(tile_config=7), dict(tile_config="fast")])
+def test_solver_rejects_bad_arguments(kw):
+    """Constructor arguments are checked before any device work (ValueError, as the
+    reference's own argument errors)."""
+    from lresdft_gb300 import LResGPU, system
+    cr = system.cubic_h2((1, 1, 1), pts_per_cell=8)
+    b = system.LCAOBasis(cr)
+    args = dict(R_w=8.0, M=64, precision="fp64", tile_config=None)
+    args.update(kw)
+    with pytest.raises(ValueError):
+        LResGPU(b, cr.pos, **args)
