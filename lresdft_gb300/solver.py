@@ -472,11 +472,12 @@ class LResGPU:
             x0, f0, d0, e0 = start
             cache[x0] = (d0, e0)
             hist.append((x0, f0))
-            # Newton step with the slope dN/dmu of the previous solve; stop if it lands within
-            # the tolerance, bracket on a sign change, else widen with secant steps
+            # Newton step with the slope dN/dmu of the previous solve (at most 1 Ha, the width
+            # of the reference's first bracket); stop if it lands within the tolerance, bracket
+            # on a sign change, else continue with secant steps
             slope = self._slope if self._slope and self._slope > 0 else max(N, 1.0)
             step = -f0 / slope
-            step = math.copysign(min(max(abs(step), 1e-7), 0.1), step)
+            step = math.copysign(min(max(abs(step), 1e-7), 1.0), step)
             a, fa = x0, f0
             b = None
             for _ in range(40):
@@ -490,9 +491,10 @@ class LResGPU:
                 if (f1 > 0) != (fa > 0):
                     b, fb = x1, f1
                     break
-                # secant extrapolation from the last two points, at least 1.5x further
+                # secant extrapolation from the last two points, 10% past its root so that the
+                # next point brackets (twice the step where the count did not move)
                 sec = -f1 * (x1 - a) / (f1 - fa) if f1 != fa else 2 * step
-                step = math.copysign(min(max(abs(sec) * 1.1, 1.5 * abs(step)), 1.0), step)
+                step = math.copysign(min(abs(sec) * 1.1, 1.0), step)
                 a, fa = x1, f1
             if b is None:
                 raise StaleMu("no sign change of the electron count near the warm-start mu")

@@ -220,11 +220,14 @@ def test_scf_driver_reproduces_reference_scf(case):
     """lresdft_gb300.scf.scf_lcao (DIIS over 6 histories, mix 0.4, clamp, renormalisation,
     Harris-Foulkes energy; lrft/lcao3d.py:237-284) over the host-backed solver and grid: the
     reference's LRFTLCAOCpp(reuse_vectors=False) SCF to tol 1e-8, same iteration count,
-    energy to 1e-10 Ha/electron, final input density to 1e-9."""
+    energy to 1e-10 Ha/electron, final input density to 1e-9.  The pole passes the mu
+    searches spend over the whole SCF stay within the counts of the current search (each one
+    is a full GPU pass: 16 electrons 70 passes over 21 steps, 54 electrons 65 over 10)."""
     from lresdft_gb300.scf import scf_lcao
     g, cr, b = case
     s = _make(case)
     r = scf_lcao(cr, s, tol=1e-8, maxiter=60, grid=_HostGrid(cr))
+    assert s.passes <= {16: 70, 54: 65}[cr.n_elec], s.passes
     assert r["converged"] and r["iterations"] == int(g["scf_iterations"])
     assert abs(r["energy"] - float(g["scf_energy"])) / cr.n_elec < 1e-10
     assert np.max(np.abs(r["dens_in"].ravel() - g["scf_dens_in"])) < 1e-9
