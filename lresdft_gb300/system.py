@@ -18,6 +18,7 @@ of the batched benchmark: ``cubic_h2`` (no jitter, bond along z) and
 """
 from __future__ import annotations
 
+import os
 from dataclasses import dataclass
 
 import numpy as np
@@ -167,11 +168,12 @@ class LCAOBasis:
     The tabulation is numpy, operation by operation as in the reference.  The sparse
     assembly (X from the tabulated points, X^T X, X^T T_FD X) runs in the native
     library (``assembly="native"``, lres_basis_build: the reference's scipy sums in
-    their order, per atom pair, on all host cores); ``assembly="scipy"`` forms them
+    their order, per atom pair, on the cores this process may use, or ``nthreads``);
+    ``assembly="scipy"`` forms them
     with scipy.sparse as the reference does."""
 
     def __init__(self, cr: Crystal, rcut=5.5, s_exps=None, p_exps=None, atom_exps=None, assembly="native",
-                 nthreads=0):
+                 nthreads=None):
         self.cr, self.rcut = cr, rcut
         s_exps = S_EXPS if s_exps is None else s_exps
         p_exps = P_EXPS if p_exps is None else p_exps
@@ -227,6 +229,8 @@ class LCAOBasis:
     def _assemble_native(self, idxs, blocks, nthreads):
         from . import _lib
         cr = self.cr
+        if nthreads is None:        # the cores this process may run on
+            nthreads = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
         dx = cr.dx
         cnt = np.array([idx.size for idx in idxs], np.int64)
         (Xp, Xi, Xv), (Rp, Ri, Rv), (Sp, Si, Sv), (Tp, Ti, Tv) = _lib.basis_matrices(
