@@ -169,8 +169,7 @@ class LCAOBasis:
     assembly (X from the tabulated points, X^T X, X^T T_FD X) runs in the native
     library (``assembly="native"``, lres_basis_build: the reference's scipy sums in
     their order, per atom pair, on the cores this process may use, or ``nthreads``);
-    ``assembly="scipy"`` forms them
-    with scipy.sparse as the reference does."""
+    ``assembly="scipy"`` forms them with scipy.sparse as the reference does."""
 
     def __init__(self, cr: Crystal, rcut=5.5, s_exps=None, p_exps=None, atom_exps=None, assembly="native",
                  nthreads=None):
