@@ -79,3 +79,20 @@ def test_invalid_input_is_reported():
         _lib.basis_matrices(np.array([0, 1]), cnt, np.array([8]), np.ones(1), (2, 2, 2), 1.0, 1.0, -1.0)
     h = C.c_void_p()
     assert _lib.lib.lres_basis_build(C.byref(h), 0, None, None, None, None, None, 1.0, 1.0, -1.0, 1, None) == -22
+
+
+def test_one_and_eight_function_atoms_and_many_threads():
+    """Atoms with a single s function and with eight (five s + one p shell), the widest value
+    lane count; 64 threads (more than the host has) give the same matrices as one."""
+    from lresdft_gb300 import system
+    cr = system.jittered_h2((2, 2, 2), a=5.0, bond=1.4, pts_per_cell=8, jitter=0.1, seed=2)
+    kinds = [((0.8,), ()), ((1.5, 0.9, 0.5, 0.25, 0.1), (0.4,))]
+    atom_exps = [kinds[a % 2] for a in range(len(cr.pos))]
+    bn, bs = _pair(cr, atom_exps=atom_exps)
+    assert set(np.diff(bn.atom_fn_ptr)) == {1, 8}
+    for attr in ("X", "Xr", "S", "T"):
+        _same(getattr(bn, attr), getattr(bs, attr), exact=False)
+    b1 = system.LCAOBasis(cr, atom_exps=atom_exps, nthreads=1)
+    b64 = system.LCAOBasis(cr, atom_exps=atom_exps, nthreads=64)
+    for attr in ("X", "Xr", "S", "T"):
+        _same(getattr(b1, attr), getattr(b64, attr))
