@@ -64,17 +64,51 @@ def test_solved_windows_merge_identical():
     assert len(cw2) == len(windows)
 
 
-def test_trace_factor():
+@pytest.mark.parametrize("pivoted", [True, False])
+def test_trace_factor(monkeypatch, pivoted):
+    """R^T R = K with rank(K) rows and zero leading columns, by the pivoted Cholesky and by
+    its eigendecomposition fallback; a zero column inside the touching block stays zero."""
+    from scipy.linalg import lapack
     from lresdft_gb300.solver import trace_factor
+    if not pivoted:
+        monkeypatch.setattr(lapack, "dpstrf", None, raising=False)
     rng = np.random.default_rng(1)
     n, c0, m = 40, 9, 25
     F = np.zeros((m, n))
     F[:, c0:] = rng.normal(size=(m, n - c0))
+    F[:, 20] = 0.0
     K = F.T @ F
     R = trace_factor(K)
-    assert R.shape[0] == min(m, n - c0)
+    assert R.shape[0] == min(m, n - c0 - 1)
     assert np.all(R[:, :c0] == 0.0)
+    # the pivoted factor never picks a zero pivot; the eigenvectors carry rounding there
+    assert np.max(np.abs(R[:, 20])) <= (0.0 if pivoted else 1e-12 * np.max(np.abs(R)))
     assert np.max(np.abs(R.T @ R - K)) < 1e-12 * np.max(np.abs(K))
+    assert trace_factor(np.zeros((5, 5))).shape == (0, 5)
+
+
+def test_trace_factor_on_owned_rows():
+    """Owned-row Gram matrices of the 3x3x3 golden crystal's windows: the trace over the
+    factor's rows equals the trace over the owned points for a resolvent (z S - H)^-1,
+    to 1e-12 relative."""
+    from scipy import linalg
+    from lresdft_gb300 import system
+    from lresdft_gb300.solver import trace_factor
+    from oracle import lrft_oracle as O
+    g = load("cubic3")
+    cr = crystal(g)
+    b = system.LCAOBasis(cr)
+    windows, own, _ = O.window_setup(b, cr.pos, float(g["R_w"]))
+    H = b.H(g["v"].ravel())
+    z = O.nodes(64, float(g["cold_mu"]), float(g["cold_elo"]))[0][5]
+    for W, o in list(zip(windows, own))[:6]:
+        F = b.Xr[o][:, W].toarray()
+        K = F.T @ F
+        R = trace_factor(K)
+        assert R.shape[0] <= min(len(o), len(W))
+        Ai = linalg.inv(z * b.S[W][:, W].toarray() - H[W][:, W].toarray())
+        ex = np.trace(Ai @ K)
+        assert abs(np.trace(Ai @ (R.T @ R)) - ex) < 1e-12 * abs(ex)
 
 
 @pytest.mark.parametrize("kw", [dict(M=63), dict(M=0), dict(precision="fp32"), dict(R_w=0.0),
