@@ -131,7 +131,10 @@ def trace_factor(K, rtol=1e-14):
     from scipy.linalg import lapack
     pstrf = getattr(lapack, "dpstrf", None)
     if pstrf is not None:
-        U, piv, rank, info = pstrf(Ks, tol=rtol * top, lower=0)
+        try:
+            U, piv, rank, info = pstrf(Ks, tol=rtol * top, lower=0)
+        except (TypeError, ValueError):       # a scipy whose wrapper differs: use the fallback
+            info = -1
         if info >= 0:
             R = np.zeros((int(rank), n))
             R[:, c0 + piv - 1] = np.triu(U)[:rank]

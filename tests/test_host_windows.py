@@ -64,14 +64,19 @@ def test_solved_windows_merge_identical():
     assert len(cw2) == len(windows)
 
 
-@pytest.mark.parametrize("pivoted", [True, False])
+@pytest.mark.parametrize("pivoted", [True, False, "broken"])
 def test_trace_factor(monkeypatch, pivoted):
     """R^T R = K with rank(K) rows and zero leading columns, by the pivoted Cholesky and by
     its eigendecomposition fallback; a zero column inside the touching block stays zero."""
     from scipy.linalg import lapack
     from lresdft_gb300.solver import trace_factor
-    if not pivoted:
+    if pivoted is False:
         monkeypatch.setattr(lapack, "dpstrf", None, raising=False)
+    elif pivoted == "broken":
+        def old_wrapper(a):
+            raise TypeError("no tol keyword")
+        monkeypatch.setattr(lapack, "dpstrf", old_wrapper, raising=False)
+        pivoted = False
     rng = np.random.default_rng(1)
     n, c0, m = 40, 9, 25
     F = np.zeros((m, n))
