@@ -57,3 +57,12 @@ def test_algorithmic_flops():
     import bench
     nW = np.array([264, 288, 312])
     assert bench.algorithmic_flops(nW, 32) == 32 * (32.0 / 3.0) * float(np.sum(nW.astype(float) ** 3))
+
+
+def test_reference_arm_other_ranks_do_nothing(monkeypatch, capsys):
+    """Under torchrun only rank 0 runs the reference arm and prints its line."""
+    import bench
+    monkeypatch.setenv("RANK", "1")
+    monkeypatch.setattr(bench, "build_system", lambda *a, **k: (_ for _ in ()).throw(AssertionError("ran")))
+    bench.run_reference(types.SimpleNamespace(steps=1, warmup=3))
+    assert capsys.readouterr().out == ""
