@@ -52,6 +52,19 @@ enum {
 
 enum { LRES_FP64 = 0, LRES_MIXED = 1 };
 
+/* Routes of the pole solves (lres_set_route).
+ *   LRES_ROUTE_LDL      one fused pivot-free LDL^T per (window, pole) of the augmented matrix
+ *                       [[z S_W - H_W, F_W], [F_W^T, 0]] (window_ldl.cu): O(n^3) per pole.
+ *   LRES_ROUTE_TRIDIAG  the standard-form window A = L^-1 H_W L^-T reduced once per
+ *                       Hamiltonian to tridiagonal form T = Q^T A Q (Householder), the owned
+ *                       rows carried through the reflectors (Y = F^ Q), then each pole is a
+ *                       tridiagonal LDL^T of z I - T and one forward sweep per row (O(n)):
+ *                       the mu trials of a density call cost O(P m n) each (tridiag.cu).
+ * Both evaluate the same resolvent quadratic forms; the default is the tridiagonal route
+ * unless the context has fewer than 4 windows or windows too large for its shared-memory
+ * panels. */
+enum { LRES_ROUTE_LDL = 0, LRES_ROUTE_TRIDIAG = 1 };
+
 typedef struct lres_ctx lres_ctx;
 
 /* System description, host pointers; copied to the device by lres_ctx_create. */
@@ -127,10 +140,21 @@ int lres_density_ptr(lres_ctx* ctx, const double** d_dens);
 int lres_autotune(lres_ctx* ctx, double mu, double e_lo, int32_t force_config, int32_t* chosen,
                   double* ms_per_config, void* stream);
 
+/* Route of the pole solves (LRES_ROUTE_LDL or LRES_ROUTE_TRIDIAG, see above).  Switching
+ * to the tridiagonal route allocates its buffers and, when a Hamiltonian is set, reduces
+ * it (LRES_EINVAL if the windows are too large for the reduction); the tile configuration
+ * of lres_autotune applies to the LDL^T kernel.  On the tridiagonal route lres_inertia and
+ * lres_min_eig count by Sturm sequences of T - sigma, T being congruent to the pencil
+ * (H_W, S_W) (for LRES_MIXED: of the FP32 standard form). */
+int lres_set_route(lres_ctx* ctx, int32_t route, void* stream);
+int lres_get_route(lres_ctx* ctx, int32_t* route);
+
 /* Device time (ms, CUDA events on the launching stream) of the most recent launch of:
- * ms[0] the fused pole kernel, ms[1] the pole sums, ms[2] the H(v) assembly, ms[3] the
- * window gather, ms[4] the standard-form transform (LRES_MIXED), ms[5] the inertia kernel;
- * -1 for one not launched yet.  Fills min(n, 6) entries, waits for their end events. */
+ * ms[0] the pole kernel (LDL^T kernel, or the shifted tridiagonal solves), ms[1] the pole
+ * sums, ms[2] the H(v) assembly, ms[3] the window gather, ms[4] the standard-form transform,
+ * ms[5] the inertia kernel, ms[6] the tridiagonal reduction, ms[7] the rows through its
+ * reflectors; -1 for one not launched yet.  Fills min(n, 8) entries, waits for their end
+ * events. */
 int lres_timings(lres_ctx* ctx, double* ms, int n);
 
 /* Per-window electron counts and band energies of the last pass (host arrays of nwin). */
@@ -154,18 +178,24 @@ int lres_voronoi_owner(const int64_t shape[3], const double cell[3], int64_t nce
 /* Window inertia counts that allocate nothing — no counterpart in the reference.
  * For callers that cannot allocate device memory themselves: hosts that own all GPU
  * memory through their own arena or caching allocator, or loops that cannot afford the
- * device-wide synchronisation of cudaMalloc / cudaFree.  Same result as lres_inertia,
- * computed from caller-provided device arrays: n_w[nwin] (int32 window dimensions),
- * offC[nwin] (int64 offsets of each window's column-major n_w x n_w block in H and S),
- * dense window blocks H and S (float64), output below[nwin] (int32, device) = number of
- * generalised eigenvalues of (H_W, S_W) below sigma.  nmax bounds every n_w.
+ * device-wide synchronisation of cudaMalloc / cudaFree.  Counts by a pivot-free FP64
+ * LDL^T of sigma S_W - H_W (Sylvester inertia), computed from caller-provided device
+ * arrays: n_w[nwin] (int32 window dimensions), offC[nwin] (int64 offsets of each
+ * window's column-major n_w x n_w block in H and S), dense window blocks H and S
+ * (float64), output below[nwin] (int32, device) = number of generalised eigenvalues of
+ * (H_W, S_W) below sigma.  nmax bounds every n_w.
  * Scratch comes from one fixed array inside the library (16.5 MiB, held by every GPU
  * that loads it until the process exits): at most 65536 windows and nmax <= 512 per
- * call, larger requests return LRES_EINVAL.  The first call on each device looks up the
- * array's device address (once per device; make that first call before any stream
- * capture).  All calls on a device share the array and reset its work queue and status
- * at the start: calls that overlap on the GPU race and must be serialised by the caller
- * (one stream, or events).  Waits for the stream to read the kernel status. */
+ * call, larger requests return LRES_EINVAL (so does a window larger than the nmax
+ * given).  The array holds eight factorisation workspaces, so the windows are spread
+ * over eight CTAs: on many windows this runs several times slower than lres_inertia.
+ * Returns LRES_ENUMERIC when some window meets a zero or non-finite pivot (NaN or Inf in
+ * H or S, or sigma exactly on an eigenvalue); its counts are then meaningless.  The
+ * first call on each device looks up the array's device address (once per device; make
+ * that first call before any stream capture).  All calls on a device share the array
+ * and reset its work queue and status at the start: calls that overlap on the GPU race
+ * and must be serialised by the caller (one stream, or events).  Waits for the stream to
+ * read the kernel status. */
 int lres_inertia_noalloc(int32_t nwin, const int32_t* n_w, const int64_t* offC, const double* H, const double* S,
                          double sigma, int32_t* below, int32_t nmax, void* stream);
 

@@ -14,10 +14,12 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liblres_gb300.so")
 
 LRES_FP64, LRES_MIXED = 0, 1
+LRES_ROUTE_LDL, LRES_ROUTE_TRIDIAG = 0, 1
 ERRORS = {-22: "EINVAL", -12: "ENOMEM", -5: "ECUDA", -33: "ENUMERIC", -71: "ESTATE"}
 
 EXPORTS = ("lres_version", "lres_last_error", "lres_ctx_create", "lres_ctx_destroy", "lres_set_potential",
-           "lres_set_hamiltonian_csr", "lres_pass", "lres_pass_async", "lres_status", "lres_density_ptr", "lres_autotune", "lres_timings", "lres_window_sums", "lres_inertia", "lres_min_eig",
+           "lres_set_hamiltonian_csr", "lres_pass", "lres_pass_async", "lres_status", "lres_density_ptr", "lres_autotune",
+           "lres_set_route", "lres_get_route", "lres_timings", "lres_window_sums", "lres_inertia", "lres_min_eig",
            "lres_voronoi_owner", "lres_lda_xc", "lres_hartree", "lres_ion_potential", "lres_inertia_noalloc",
            "lres_set_windows", "lres_window_ptrs", "lres_adjoint", "lres_owned_gram", "lres_set_trace_rows",
            "lres_basis_build", "lres_basis_fetch", "lres_basis_free")
@@ -65,6 +67,8 @@ def _load():
         "lres_status": (i32, [vp, C.POINTER(C.c_int32), vp]),
         "lres_density_ptr": (i32, [vp, C.POINTER(C.c_void_p)]),
         "lres_autotune": (i32, [vp, dbl, dbl, C.c_int32, C.POINTER(C.c_int32), PD, vp]),
+        "lres_set_route": (i32, [vp, C.c_int32, vp]),
+        "lres_get_route": (i32, [vp, C.POINTER(C.c_int32)]),
         "lres_timings": (i32, [vp, PD, i32]),
         "lres_window_sums": (i32, [vp, PD, PD]),
         "lres_inertia": (i32, [vp, dbl, C.POINTER(C.c_int32), C.POINTER(i64), vp]),

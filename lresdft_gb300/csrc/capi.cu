@@ -86,7 +86,36 @@ struct lres_ctx {
     double *d_LinvT = nullptr, *d_Y = nullptr, *d_Hhat = nullptr;
     float2 *d_LinvT_df = nullptr, *d_H_df = nullptr, *d_Y_df = nullptr;   // double-float operands
     float *d_Hhat32 = nullptr, *d_Fhat32 = nullptr;
+    double *d_Fhat64 = nullptr, *d_FhatT64 = nullptr;   // FP64 standard-form rows (FP64 tridiagonal route)
     long long sizeC = 0, sizeF = 0;
+    // multi-shift tridiagonal route (tridiag.cu): T = Q^T H^ Q per window once per Hamiltonian,
+    // rows Y = F^ Q, then each pass is one fused shifted-solve + pole-sum kernel
+    int route = LRES_ROUTE_LDL;
+    bool tri_alloc = false, tri_ready = false;
+    int tri_nb = 0, tri_ldv = 0;
+    std::vector<long long> offN;                 // window vectors (sum of n)
+    long long sizeN = 0, sizeA = 0;
+    long long* d_offN = nullptr;
+    long long* d_offA = nullptr;                 // working blocks: leading dimension n rounded up to 4
+    int* d_order_w = nullptr;                    // windows, most expensive first
+    int* d_tstatus = nullptr;                    // status of the reduction (kept across passes)
+    void *d_triA = nullptr, *d_trid = nullptr, *d_trie = nullptr, *d_tritau = nullptr;
+    void *d_Yown = nullptr, *d_Ytr = nullptr;
+    double* d_lam = nullptr;                     // per-window smallest eigenvalue
+    struct RowItems {                            // work items over the rows of every window
+        int4* apply = nullptr;                   // (window, first row, rows <= 256)
+        int napply = 0;
+        int4* pass = nullptr;                    // (window, first row, rows <= rows per pass item)
+        int npass = 0;
+        int *first = nullptr, *count = nullptr;  // pass items of each window (contiguous)
+        double* part = nullptr;                  // per pass item: sums of n(r), e(r)
+        void release() {
+            for (void* q : {(void*)apply, (void*)pass, (void*)first, (void*)count, (void*)part})
+                if (q) cudaFree(q);
+            *this = RowItems{};
+        }
+    };
+    RowItems ri_own, ri_tr;
     // pole work
     int2 *d_items = nullptr, *d_items_win = nullptr, *d_items_sub = nullptr;
     int nitems = 0;
@@ -128,8 +157,9 @@ struct lres_ctx {
     double2* d_fftwork = nullptr;
     // CUDA events bracketing the launches, for lres_timings: pairs (begin, end) of
     // 0 pole kernel, 1 pole sums, 2 H(v) assembly, 3 window gather, 4 standard-form transform, 5 inertia kernel
-    cudaEvent_t ev[12] = {};
-    bool ev_used[6] = {};
+    // 6 tridiagonal reduction, 7 rows through the reflectors
+    cudaEvent_t ev[16] = {};
+    bool ev_used[8] = {};
     ~lres_ctx();
 };
 
@@ -140,9 +170,12 @@ lres_ctx::~lres_ctx() {
                     d_Hhat32, d_Fhat32, d_LinvT_df, d_H_df, d_Y_df, d_items, d_items_win, d_items_sub, d_counter, d_status, d_npos, d_ws, d_shifts,
                     d_wq, d_wzq, d_q, d_dens, d_nw, d_ew, d_v, d_fftwork, d_adjA[0], d_adjA[1], d_adjA[2],
                     d_dHW, d_dSW, d_gH, d_adjdv, d_adju, d_cw, d_order, d_eoff, d_poff, d_ent, d_pent, d_adjws,
-                    d_mT, d_offFT, d_offQT, d_FT, d_FhatT32, d_qT};
+                    d_mT, d_offFT, d_offQT, d_FT, d_FhatT32, d_qT, d_Fhat64, d_FhatT64, d_offN, d_offA, d_order_w,
+                    d_tstatus, d_triA, d_trid, d_trie, d_tritau, d_Yown, d_Ytr, d_lam};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    ri_own.release();
+    ri_tr.release();
     if (fft) fft3_destroy(fft);
     for (cudaEvent_t e : ev)
         if (e) cudaEventDestroy(e);
@@ -226,6 +259,18 @@ int read_status(lres_ctx* c, cudaStream_t s, int* st) {
     return LRES_OK;
 }
 
+// Status of the last pass: its kernels, and on the tridiagonal route the reduction of the
+// current Hamiltonian.
+int read_pass_status(lres_ctx* c, cudaStream_t s, int* st) {
+    int v[2] = {0, 0};
+    LRES_CUDA_TRY(cudaMemcpyAsync(&v[0], c->d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (c->route == LRES_ROUTE_TRIDIAG && c->d_tstatus)
+        LRES_CUDA_TRY(cudaMemcpyAsync(&v[1], c->d_tstatus, sizeof(int), cudaMemcpyDeviceToHost, s));
+    LRES_CUDA_TRY(cudaStreamSynchronize(s));
+    *st = v[0] | v[1];
+    return LRES_OK;
+}
+
 __global__ void identity_kernel(const int* n_w, const long long* off, double* I, int nwin) {
     const int w = blockIdx.x;
     if (w >= nwin) return;
@@ -264,14 +309,25 @@ __global__ void window_total_kernel(int nwin, const double* nw, const double* ew
 
 int window_transform(lres_ctx* c, cudaStream_t s) {
     // H^_W = L^-1 H_W L^-T with LinvT = L^-T (upper triangular) stored column-major:
-    // Y = H LinvT (k <= column), then the lower triangle of H^ = LinvT^T Y (k <= row),
-    // both in double-float arithmetic on the FP32 pipes, H^ rounded to FP32 at the end
-    TRY(split_f64(c->d_HW, c->d_H_df, c->sizeC, s));
-    TRY(batched_gemm_df64(c->nwin, c->d_n, c->d_offC, c->nmax, false, 1, c->d_H_df, c->d_LinvT_df, c->d_Y_df,
-                          nullptr, s));
-    TRY(batched_gemm_df64(c->nwin, c->d_n, c->d_offC, c->nmax, true, 2, c->d_LinvT_df, c->d_Y_df, nullptr,
-                          c->d_Hhat32, s));
+    // Y = H LinvT (k <= column), then the lower triangle of H^ = LinvT^T Y (k <= row)
+    if (c->precision == LRES_MIXED) {
+        // both in double-float arithmetic on the FP32 pipes, H^ rounded to FP32 at the end
+        TRY(split_f64(c->d_HW, c->d_H_df, c->sizeC, s));
+        TRY(batched_gemm_df64(c->nwin, c->d_n, c->d_offC, c->nmax, false, 1, c->d_H_df, c->d_LinvT_df, c->d_Y_df,
+                              nullptr, s));
+        TRY(batched_gemm_df64(c->nwin, c->d_n, c->d_offC, c->nmax, true, 2, c->d_LinvT_df, c->d_Y_df, nullptr,
+                              c->d_Hhat32, s));
+    } else {
+        // FP64 (the FP64 tridiagonal route)
+        TRY(batched_gemm(c->nwin, c->d_n, c->d_offC, c->nmax, false, c->d_HW, c->d_LinvT, c->d_Y, s, 1));
+        TRY(batched_gemm(c->nwin, c->d_n, c->d_offC, c->nmax, true, c->d_LinvT, c->d_Y, c->d_Hhat, s, 2));
+    }
     return LRES_OK;
+}
+
+// The standard form is used by the mixed path (both routes) and by the FP64 tridiagonal route.
+bool needs_standard_form(const lres_ctx* c) {
+    return c->precision == LRES_MIXED || c->route == LRES_ROUTE_TRIDIAG;
 }
 
 int mark(lres_ctx* c, int which, int end, cudaStream_t s) {
@@ -284,51 +340,65 @@ int mark(lres_ctx* c, int which, int end, cudaStream_t s) {
     return LRES_OK;
 }
 
+int tri_prepare(lres_ctx* c, cudaStream_t s);
+
 int after_h_blocks(lres_ctx* c, cudaStream_t s) {
     TRY(mark(c, 3, 0, s));
     LRES_CUDA_TRY(cudaMemsetAsync(c->d_HW, 0, sizeof(double) * c->sizeC, s));
     TRY(gather_windows(c->bp, c->nwin, c->d_wgrp_off, c->d_wgrp, c->d_wgrp_lo, c->d_gloc, c->d_offC, c->d_n, c->nmax,
                        c->d_Hblk, c->d_HW, s));
     TRY(mark(c, 3, 1, s));
-    if (c->precision == LRES_MIXED) {
+    if (needs_standard_form(c)) {
         TRY(mark(c, 4, 0, s));
         TRY(window_transform(c, s));
         TRY(mark(c, 4, 1, s));
     }
+    if (c->route == LRES_ROUTE_TRIDIAG) TRY(tri_prepare(c, s));
     c->have_h = true;
     return LRES_OK;
 }
 
-// Trace rows in the standard form: R^ = R L^-T, FP32.
+// Trace rows in the standard form: R^ = R L^-T (FP32 for the mixed path, FP64 otherwise).
 int trace_standard_form(lres_ctx* c, cudaStream_t s) {
+    const bool mixed = c->precision == LRES_MIXED;
+    double* out = mixed ? nullptr : c->d_FhatT64;
     double* tmp = nullptr;
-    TRY(dalloc(&tmp, c->sizeFT));
+    if (mixed) TRY(dalloc(&tmp, c->sizeFT));
     int rc = batched_gemm_rect_upper(c->nwin, c->d_n, c->d_mT, c->d_offFT, c->d_offC, c->nmax, c->mmaxT, c->d_FT,
-                                     c->d_LinvT, tmp, s);
-    if (!rc) rc = convert_f64_f32(tmp, c->d_FhatT32, c->sizeFT, s);
+                                     c->d_LinvT, mixed ? tmp : out, s);
+    if (!rc && mixed) rc = convert_f64_f32(tmp, c->d_FhatT32, c->sizeFT, s);
     cudaError_t e = cudaStreamSynchronize(s);
-    cudaFree(tmp);
+    if (tmp) cudaFree(tmp);
     if (rc) return rc;
     LRES_CUDA_TRY(e);
     return LRES_OK;
 }
 
-// Standard form of the mixed path from the current S_W: L_c^-1 (stored as L^-T, FP64 and as
-// double-float pairs) and F^ = L_c^-1 F (FP32).  Allocates on the first call.
+// Standard form from the current S_W: L_c^-1 (stored as L^-T in FP64; for the mixed path also
+// as double-float pairs) and F^ = L_c^-1 F (FP32 for the mixed path, FP64 for the FP64
+// tridiagonal route).  Allocates on the first call.
 int setup_standard_form(lres_ctx* c, cudaStream_t s) {
+    const bool mixed = c->precision == LRES_MIXED;
     if (!c->d_LinvT) {
         TRY(dalloc(&c->d_LinvT, c->sizeC));
-        TRY(dalloc(&c->d_LinvT_df, c->sizeC));
-        TRY(dalloc(&c->d_H_df, c->sizeC));
-        TRY(dalloc(&c->d_Y_df, c->sizeC));
-        TRY(dalloc(&c->d_Hhat32, c->sizeC));
-        TRY(dalloc(&c->d_Fhat32, c->sizeF));
+        if (mixed) {
+            TRY(dalloc(&c->d_LinvT_df, c->sizeC));
+            TRY(dalloc(&c->d_H_df, c->sizeC));
+            TRY(dalloc(&c->d_Y_df, c->sizeC));
+            TRY(dalloc(&c->d_Hhat32, c->sizeC));
+            TRY(dalloc(&c->d_Fhat32, c->sizeF));
+        } else {
+            TRY(dalloc(&c->d_Y, c->sizeC));
+            TRY(dalloc(&c->d_Hhat, c->sizeC));
+            TRY(dalloc(&c->d_Fhat64, c->sizeF));
+        }
     }
+    if (!mixed && c->have_trace && !c->d_FhatT64) TRY(dalloc(&c->d_FhatT64, c->sizeFT));
     double* I = nullptr;
     double* Fhat = nullptr;
     double* one = nullptr;
     TRY(dalloc(&I, c->sizeC));
-    TRY(dalloc(&Fhat, c->sizeF));
+    if (mixed) TRY(dalloc(&Fhat, c->sizeF));
     TRY(dalloc(&one, 1));
     const double h_one = 1.0;
     LRES_CUDA_TRY(cudaMemcpyAsync(one, &h_one, sizeof(double), cudaMemcpyHostToDevice, s));
@@ -342,20 +412,116 @@ int setup_standard_form(lres_ctx* c, cudaStream_t s) {
     // F^ = F L^-T (owned-point rows in the standard form), any number of rows
     if (!rc)
         rc = batched_gemm_rect_upper(c->nwin, c->d_n, c->d_m, c->d_offF, c->d_offC, c->nmax, c->mmax, c->d_F,
-                                     c->d_LinvT, Fhat, s);
-    if (!rc) rc = convert_f64_f32(Fhat, c->d_Fhat32, c->sizeF, s);
+                                     c->d_LinvT, mixed ? Fhat : c->d_Fhat64, s);
+    if (!rc && mixed) rc = convert_f64_f32(Fhat, c->d_Fhat32, c->sizeF, s);
     if (!rc && c->have_trace) rc = trace_standard_form(c, s);
-    if (!rc) rc = split_f64(c->d_LinvT, c->d_LinvT_df, c->sizeC, s);
+    if (!rc && mixed) rc = split_f64(c->d_LinvT, c->d_LinvT_df, c->sizeC, s);
     int st = 0;
     if (!rc) rc = read_status(c, s, &st);
     cudaFree(I);
-    cudaFree(Fhat);
+    if (Fhat) cudaFree(Fhat);
     cudaFree(one);
     if (rc) return rc;
     if (st) {
         lres_set_error("Cholesky of a window overlap S_W failed (status %d)", st);
         return LRES_ENUMERIC;
     }
+    return LRES_OK;
+}
+
+// Work items over the rows of every window, windows in the order of c->order (most
+// expensive first): blocks of 256 rows for the reflector application, batches of the pass
+// kernel's rows per item for the pole passes (each window's batches contiguous).
+int build_row_items(lres_ctx* c, const std::vector<int>& m, lres_ctx::RowItems& ri, cudaStream_t s) {
+    ri.release();
+    const int rb = tri_rows_per_item(c->precision == LRES_MIXED, c->npoles);
+    std::vector<int4> ap, pa;
+    std::vector<int> first(c->nwin, 0), count(c->nwin, 0);
+    for (int w : c->order) {
+        for (int r0 = 0; r0 < m[w]; r0 += 256) ap.push_back(make_int4(w, r0, std::min(256, m[w] - r0), 0));
+        first[w] = (int)pa.size();
+        for (int r0 = 0; r0 < m[w]; r0 += rb) pa.push_back(make_int4(w, r0, std::min(rb, m[w] - r0), 0));
+        count[w] = (int)pa.size() - first[w];
+    }
+    ri.napply = (int)ap.size();
+    ri.npass = (int)pa.size();
+    TRY(upload(&ri.apply, ap, s));
+    TRY(upload(&ri.pass, pa, s));
+    TRY(upload(&ri.first, first, s));
+    TRY(upload(&ri.count, count, s));
+    TRY(dalloc(&ri.part, 2 * (size_t)std::max(ri.npass, 1)));
+    LRES_CUDA_TRY(cudaStreamSynchronize(s));     // the host vectors go out of scope
+    return LRES_OK;
+}
+
+// Buffers of the tridiagonal route (once per context).
+int tri_setup(lres_ctx* c, cudaStream_t s) {
+    if (c->tri_alloc) return LRES_OK;
+    const bool fp32 = c->precision == LRES_MIXED;
+    const size_t el = fp32 ? sizeof(float) : sizeof(double);
+    TRY(tri_pick_nb(fp32, c->nmax, c->smem_budget, &c->tri_nb, &c->tri_ldv));
+    TRY(dalloc((char**)&c->d_triA, el * (size_t)c->sizeA));
+    TRY(dalloc((char**)&c->d_trid, el * (size_t)c->sizeN));
+    TRY(dalloc((char**)&c->d_trie, el * (size_t)c->sizeN));
+    TRY(dalloc((char**)&c->d_tritau, el * (size_t)c->sizeN));
+    TRY(dalloc((char**)&c->d_Yown, el * (size_t)std::max<long long>(c->sizeF, 1)));
+    TRY(dalloc(&c->d_lam, c->nwin));
+    TRY(dalloc(&c->d_tstatus, 1));
+    LRES_CUDA_TRY(cudaMemsetAsync(c->d_tstatus, 0, sizeof(int), s));
+    TRY(build_row_items(c, c->m_w, c->ri_own, s));
+    if (c->have_trace) {
+        std::vector<int> mT(c->nwin);
+        LRES_CUDA_TRY(cudaMemcpy(mT.data(), c->d_mT, sizeof(int) * c->nwin, cudaMemcpyDeviceToHost));
+        TRY(build_row_items(c, mT, c->ri_tr, s));
+        TRY(dalloc((char**)&c->d_Ytr, el * (size_t)std::max<long long>(c->sizeFT, 1)));
+    }
+    c->tri_alloc = true;
+    return LRES_OK;
+}
+
+// Rows of one row set (owned points or trace rows) through the reflectors.
+int tri_rows(lres_ctx* c, bool trace, cudaStream_t s) {
+    const bool fp32 = c->precision == LRES_MIXED;
+    const lres_ctx::RowItems& ri = trace ? c->ri_tr : c->ri_own;
+    const void* F = trace ? (fp32 ? (const void*)c->d_FhatT32 : (const void*)c->d_FhatT64)
+                          : (fp32 ? (const void*)c->d_Fhat32 : (const void*)c->d_Fhat64);
+    return tri_apply(fp32, ri.napply, ri.apply, c->d_n, trace ? c->d_mT : c->d_m, c->d_offA, c->d_offN,
+                     trace ? c->d_offFT : c->d_offF, c->d_triA, c->d_tritau, F, trace ? c->d_Ytr : c->d_Yown,
+                     c->tri_nb, c->tri_ldv, s);
+}
+
+// Tridiagonal form of the current standard-form windows and the rows through its reflectors
+// (kernels and memsets only).
+int tri_prepare(lres_ctx* c, cudaStream_t s) {
+    const bool fp32 = c->precision == LRES_MIXED;
+    LRES_CUDA_TRY(cudaMemsetAsync(c->d_tstatus, 0, sizeof(int), s));
+    TRY(mark(c, 6, 0, s));
+    TRY(tri_reduce(fp32, c->nwin, c->d_order_w, c->d_counter, c->d_n, c->d_offC, c->d_offA, c->d_offN,
+                   fp32 ? (const void*)c->d_Hhat32 : (const void*)c->d_Hhat, c->d_triA, c->d_trid, c->d_trie,
+                   c->d_tritau, c->d_tstatus, c->tri_nb, c->tri_ldv, c->smem_budget, s));
+    TRY(mark(c, 6, 1, s));
+    TRY(mark(c, 7, 0, s));
+    TRY(tri_rows(c, false, s));
+    if (c->have_trace) TRY(tri_rows(c, true, s));
+    TRY(mark(c, 7, 1, s));
+    c->tri_ready = true;
+    return LRES_OK;
+}
+
+// The pole pass of the tridiagonal route over one row set (nodes and weights already set):
+// per-window N and E_band into d_nw / d_ew, the density into d_dens for the owned points.
+int tri_run_pass(lres_ctx* c, bool trace, cudaStream_t s) {
+    const bool fp32 = c->precision == LRES_MIXED;
+    const lres_ctx::RowItems& ri = trace ? c->ri_tr : c->ri_own;
+    TRY(mark(c, 0, 0, s));
+    TRY(tri_pass(fp32, ri.npass, ri.pass, c->d_counter, c->d_n, trace ? c->d_mT : c->d_m, c->d_offN,
+                 trace ? c->d_offFT : c->d_offF, trace ? c->d_offQT : c->d_offQ, trace ? nullptr : c->d_Oflat,
+                 trace ? c->d_Ytr : c->d_Yown, c->d_trid, c->d_trie, c->npoles, c->d_shifts, c->d_wq, c->d_wzq,
+                 trace ? nullptr : c->d_dens, ri.part, c->d_status, c->tri_ldv, c->smem_budget, s));
+    TRY(mark(c, 0, 1, s));
+    TRY(mark(c, 1, 0, s));
+    TRY(tri_window_sums(c->nwin, ri.first, ri.count, ri.part, c->dV, c->d_nw, c->d_ew, s));
+    TRY(mark(c, 1, 1, s));
     return LRES_OK;
 }
 
@@ -748,8 +914,30 @@ extern "C" int lres_ctx_create(lres_ctx** out, const lres_system_desc* d, int pr
 
     // workspace of the window kernels: allocated by the first launch that needs it
 
-    // ---- standard form for the mixed path
-    if (precision == LRES_MIXED) TRY(setup_standard_form(c.get(), s));
+    // ---- route of the pole solves: tridiagonal unless the windows are too few to fill the
+    //      GPU with one CTA each, or too large for the reduction's shared-memory panels
+    c->offN.assign(c->nwin + 1, 0);
+    for (int w = 0; w < c->nwin; ++w) c->offN[w + 1] = c->offN[w] + c->n_w[w];
+    c->sizeN = c->offN[c->nwin];
+    TRY(upload(&c->d_offN, c->offN, s));
+    {
+        std::vector<long long> offA(c->nwin + 1, 0);
+        for (int w = 0; w < c->nwin; ++w) offA[w + 1] = offA[w] + (long long)((c->n_w[w] + 3) & ~3) * c->n_w[w];
+        c->sizeA = offA[c->nwin];
+        TRY(upload(&c->d_offA, offA, s));
+        LRES_CUDA_TRY(cudaStreamSynchronize(s));
+    }
+    TRY(upload(&c->d_order_w, c->order, s));
+    {
+        int nb = 0, ldv = 0;
+        const bool fits = tri_pick_nb(precision == LRES_MIXED, c->nmax, c->smem_budget, &nb, &ldv) == LRES_OK;
+        lres_set_error("");
+        c->route = (fits && c->nwin >= 4) ? LRES_ROUTE_TRIDIAG : LRES_ROUTE_LDL;
+    }
+
+    // ---- standard form (mixed path; FP64 tridiagonal route)
+    if (needs_standard_form(c.get())) TRY(setup_standard_form(c.get(), s));
+    if (c->route == LRES_ROUTE_TRIDIAG) TRY(tri_setup(c.get(), s));
 
     // ---- pass buffers
     TRY(dalloc((char**)&c->d_shifts, (size_t)c->npoles * 16));
@@ -839,26 +1027,32 @@ extern "C" int lres_pass(lres_ctx* c, double mu, double e_lo, double* dens, int 
     LRES_CUDA_TRY(cudaMemsetAsync(c->d_status, 0, sizeof(int), s));
     LRES_CUDA_TRY(cudaMemsetAsync(c->d_counter, 0, sizeof(int), s));
     // no density requested and trace rows installed: the pass over the trace rows
-    const Rows rw = select_rows(c, !dens && c->have_trace);
-    TRY(mark(c, 0, 0, s));
-    if (mixed)
-        TRY(ldl_launch(c, LdlJob::C64, c->nitems, c->d_items, c->d_Hhat32, nullptr, rw.F, rw.m, rw.offF,
-                       c->d_shifts, rw.q, nullptr, c->nmax + rw.mmax, rw.mmax, s, rw.offQ, rw.npts));
-    else
-        TRY(ldl_launch(c, LdlJob::C128, c->nitems, c->d_items, c->d_HW, c->d_SW, rw.F, rw.m, rw.offF,
-                       c->d_shifts, rw.q, nullptr, c->nmax + rw.mmax, rw.mmax, s, rw.offQ, rw.npts));
-    TRY(mark(c, 0, 1, s));
-    TRY(mark(c, 1, 0, s));
-    TRY(pole_sums(c->nwin, rw.offQ, rw.m, rw.Oflat, mixed, rw.q, rw.npts, P, c->d_wq, c->d_wzq, c->dV, rw.dens,
-                  c->d_nw, c->d_ew, s));
-    TRY(mark(c, 1, 1, s));
+    const bool trace = !dens && c->have_trace;
+    if (c->route == LRES_ROUTE_TRIDIAG) {
+        if (!c->tri_ready) TRY(tri_prepare(c, s));
+        TRY(tri_run_pass(c, trace, s));
+    } else {
+        const Rows rw = select_rows(c, trace);
+        TRY(mark(c, 0, 0, s));
+        if (mixed)
+            TRY(ldl_launch(c, LdlJob::C64, c->nitems, c->d_items, c->d_Hhat32, nullptr, rw.F, rw.m, rw.offF,
+                           c->d_shifts, rw.q, nullptr, c->nmax + rw.mmax, rw.mmax, s, rw.offQ, rw.npts));
+        else
+            TRY(ldl_launch(c, LdlJob::C128, c->nitems, c->d_items, c->d_HW, c->d_SW, rw.F, rw.m, rw.offF,
+                           c->d_shifts, rw.q, nullptr, c->nmax + rw.mmax, rw.mmax, s, rw.offQ, rw.npts));
+        TRY(mark(c, 0, 1, s));
+        TRY(mark(c, 1, 0, s));
+        TRY(pole_sums(c->nwin, rw.offQ, rw.m, rw.Oflat, mixed, rw.q, rw.npts, P, c->d_wq, c->d_wzq, c->dV,
+                      rw.dens, c->d_nw, c->d_ew, s));
+        TRY(mark(c, 1, 1, s));
+    }
     LRES_CUDA_TRY(cudaMemcpyAsync(c->nw_h.data(), c->d_nw, sizeof(double) * c->nwin, cudaMemcpyDeviceToHost, s));
     LRES_CUDA_TRY(cudaMemcpyAsync(c->ew_h.data(), c->d_ew, sizeof(double) * c->nwin, cudaMemcpyDeviceToHost, s));
     if (dens)
         LRES_CUDA_TRY(cudaMemcpyAsync(dens, c->d_dens, sizeof(double) * c->ng,
                                       dens_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
     int st = 0;
-    TRY(read_status(c, s, &st));
+    TRY(read_pass_status(c, s, &st));
     double N = 0.0, E = 0.0;
     for (int w = 0; w < c->nwin; ++w) {
         N += c->nw_h[w];
@@ -896,6 +1090,13 @@ extern "C" int lres_autotune(lres_ctx* c, double mu, double e_lo, int32_t force_
     double out[3];
     double best = 1e300;
     int arg = 0;
+    // the tile configurations belong to the LDL^T kernel: time them on that route
+    struct RouteGuard {
+        lres_ctx* c;
+        int saved;
+        ~RouteGuard() { c->route = saved; }
+    } guard{c, c->route};
+    c->route = LRES_ROUTE_LDL;
     for (int cfg = 0; cfg < kLeftConfigs; ++cfg) {
         // the tensor-core variant (3xTF32) is timed but chosen only when forced: its
         // measured error is about 5x that of the FP32 SIMT configurations
@@ -919,12 +1120,53 @@ extern "C" int lres_autotune(lres_ctx* c, double mu, double e_lo, int32_t force_
     return LRES_OK;
 }
 
+extern "C" int lres_set_route(lres_ctx* c, int32_t route, void* stream) {
+    if (!c || (route != LRES_ROUTE_LDL && route != LRES_ROUTE_TRIDIAG)) {
+        lres_set_error("route must be LRES_ROUTE_LDL or LRES_ROUTE_TRIDIAG");
+        return LRES_EINVAL;
+    }
+    if (route == c->route) return LRES_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (route == LRES_ROUTE_LDL) {
+        c->route = route;
+        c->tri_ready = false;               // T no longer follows the Hamiltonian
+        return LRES_OK;
+    }
+    int nb = 0, ldv = 0;
+    TRY(tri_pick_nb(c->precision == LRES_MIXED, c->nmax, c->smem_budget, &nb, &ldv));
+    const int old = c->route;
+    c->route = route;
+    int rc = LRES_OK;
+    if (c->precision != LRES_MIXED && !c->d_LinvT) rc = setup_standard_form(c, s);
+    if (!rc) rc = tri_setup(c, s);
+    if (!rc && c->have_h) {
+        if (c->precision != LRES_MIXED) rc = window_transform(c, s);   // H^ (FP64) of the current H
+        if (!rc) rc = tri_prepare(c, s);
+    }
+    if (rc) {
+        c->route = old;
+        c->tri_ready = false;
+        return rc;
+    }
+    LRES_CUDA_TRY(cudaStreamSynchronize(s));
+    return LRES_OK;
+}
+
+extern "C" int lres_get_route(lres_ctx* c, int32_t* route) {
+    if (!c || !route) {
+        lres_set_error("null argument");
+        return LRES_EINVAL;
+    }
+    *route = c->route;
+    return LRES_OK;
+}
+
 extern "C" int lres_timings(lres_ctx* c, double* ms, int n) {
     if (!c || !ms || n < 0) {
         lres_set_error("bad arguments to lres_timings");
         return LRES_EINVAL;
     }
-    for (int i = 0; i < n && i < 6; ++i) {
+    for (int i = 0; i < n && i < 8; ++i) {
         ms[i] = -1.0;
         if (!c->ev_used[i]) continue;
         LRES_CUDA_TRY(cudaEventSynchronize(c->ev[2 * i + 1]));
@@ -932,7 +1174,7 @@ extern "C" int lres_timings(lres_ctx* c, double* ms, int n) {
         LRES_CUDA_TRY(cudaEventElapsedTime(&t, c->ev[2 * i], c->ev[2 * i + 1]));
         ms[i] = t;
     }
-    for (int i = 6; i < n; ++i) ms[i] = -1.0;
+    for (int i = 8; i < n; ++i) ms[i] = -1.0;
     return LRES_OK;
 }
 
@@ -955,14 +1197,19 @@ extern "C" int lres_pass_async(lres_ctx* c, double mu, double e_lo, double* d_ou
     poles_kernel<<<(P + 63) / 64, 64, 0, s>>>(P, c->M, mu, e_lo, mixed ? 1 : 0, c->d_shifts, c->d_wq, c->d_wzq);
     LRES_CUDA_TRY(cudaGetLastError());
     LRES_CUDA_TRY(cudaMemsetAsync(c->d_status, 0, sizeof(int), s));
-    if (mixed)
-        TRY(ldl_launch(c, LdlJob::C64, c->nitems, c->d_items, c->d_Hhat32, nullptr, c->d_Fhat32, c->d_m, c->d_offF,
-                       c->d_shifts, c->d_q, nullptr, c->nmax + c->mmax, c->mmax, s));
-    else
-        TRY(ldl_launch(c, LdlJob::C128, c->nitems, c->d_items, c->d_HW, c->d_SW, c->d_F, c->d_m, c->d_offF,
-                       c->d_shifts, c->d_q, nullptr, c->nmax + c->mmax, c->mmax, s));
-    TRY(pole_sums(c->nwin, c->d_offQ, c->d_m, c->d_Oflat, mixed, c->d_q, c->npts, P, c->d_wq, c->d_wzq, c->dV,
-                  c->d_dens, c->d_nw, c->d_ew, s));
+    if (c->route == LRES_ROUTE_TRIDIAG) {
+        if (!c->tri_ready) TRY(tri_prepare(c, s));
+        TRY(tri_run_pass(c, false, s));
+    } else {
+        if (mixed)
+            TRY(ldl_launch(c, LdlJob::C64, c->nitems, c->d_items, c->d_Hhat32, nullptr, c->d_Fhat32, c->d_m,
+                           c->d_offF, c->d_shifts, c->d_q, nullptr, c->nmax + c->mmax, c->mmax, s));
+        else
+            TRY(ldl_launch(c, LdlJob::C128, c->nitems, c->d_items, c->d_HW, c->d_SW, c->d_F, c->d_m, c->d_offF,
+                           c->d_shifts, c->d_q, nullptr, c->nmax + c->mmax, c->mmax, s));
+        TRY(pole_sums(c->nwin, c->d_offQ, c->d_m, c->d_Oflat, mixed, c->d_q, c->npts, P, c->d_wq, c->d_wzq,
+                      c->dV, c->d_dens, c->d_nw, c->d_ew, s));
+    }
     window_total_kernel<<<1, 1, 0, s>>>(c->nwin, c->d_nw, c->d_ew, d_out);
     LRES_CUDA_TRY(cudaGetLastError());
     return LRES_OK;
@@ -974,7 +1221,7 @@ extern "C" int lres_status(lres_ctx* c, int32_t* status, void* stream) {
         return LRES_EINVAL;
     }
     int st = 0;
-    TRY(read_status(c, (cudaStream_t)stream, &st));
+    TRY(read_pass_status(c, (cudaStream_t)stream, &st));
     *status = st;
     return LRES_OK;
 }
@@ -1008,14 +1255,23 @@ extern "C" int lres_inertia(lres_ctx* c, double sigma, int32_t* below, int64_t* 
         return LRES_ESTATE;
     }
     cudaStream_t s = (cudaStream_t)stream;
-    LRES_CUDA_TRY(cudaMemcpyAsync(c->d_shifts, &sigma, sizeof(double), cudaMemcpyHostToDevice, s));
-    LRES_CUDA_TRY(cudaMemsetAsync(c->d_status, 0, sizeof(int), s));
-    // positive pivots of (sigma S - H) = eigenvalues of (H, S) below sigma
-    LRES_CUDA_TRY(cudaMemsetAsync(c->d_counter, 0, sizeof(int), s));
-    TRY(mark(c, 5, 0, s));
-    TRY(ldl_launch(c, LdlJob::R64, c->nwin, c->d_items_win, c->d_HW, c->d_SW, nullptr, c->d_m, c->d_offF,
-                   c->d_shifts, nullptr, nullptr, c->nmax, 0, s));
-    TRY(mark(c, 5, 1, s));
+    if (c->route == LRES_ROUTE_TRIDIAG) {
+        // Sturm counts of T - sigma: T is congruent to the pencil (H_W, S_W)
+        if (!c->tri_ready) TRY(tri_prepare(c, s));
+        TRY(mark(c, 5, 0, s));
+        TRY(tri_sturm(c->precision == LRES_MIXED, c->nwin, c->d_n, c->d_offN, c->d_trid, c->d_trie, sigma,
+                      c->d_npos, s));
+        TRY(mark(c, 5, 1, s));
+    } else {
+        LRES_CUDA_TRY(cudaMemcpyAsync(c->d_shifts, &sigma, sizeof(double), cudaMemcpyHostToDevice, s));
+        LRES_CUDA_TRY(cudaMemsetAsync(c->d_status, 0, sizeof(int), s));
+        // positive pivots of (sigma S - H) = eigenvalues of (H, S) below sigma
+        LRES_CUDA_TRY(cudaMemsetAsync(c->d_counter, 0, sizeof(int), s));
+        TRY(mark(c, 5, 0, s));
+        TRY(ldl_launch(c, LdlJob::R64, c->nwin, c->d_items_win, c->d_HW, c->d_SW, nullptr, c->d_m, c->d_offF,
+                       c->d_shifts, nullptr, nullptr, c->nmax, 0, s));
+        TRY(mark(c, 5, 1, s));
+    }
     std::vector<int> cnt(c->nwin);
     LRES_CUDA_TRY(cudaMemcpyAsync(cnt.data(), c->d_npos, sizeof(int) * c->nwin, cudaMemcpyDeviceToHost, s));
     LRES_CUDA_TRY(cudaStreamSynchronize(s));
@@ -1053,6 +1309,17 @@ extern "C" int lres_min_eig(lres_ctx* c, double lo, double hi, double tol, doubl
         return LRES_ESTATE;
     }
     cudaStream_t s = (cudaStream_t)stream;
+    if (c->route == LRES_ROUTE_TRIDIAG) {
+        // every window's smallest eigenvalue by Sturm bisection on T, to width tol
+        if (!c->tri_ready) TRY(tri_prepare(c, s));
+        TRY(tri_min_eig(c->precision == LRES_MIXED, c->nwin, c->d_n, c->d_offN, c->d_trid, c->d_trie, tol,
+                        c->d_lam, s));
+        std::vector<double> lam(c->nwin);
+        LRES_CUDA_TRY(cudaMemcpyAsync(lam.data(), c->d_lam, sizeof(double) * c->nwin, cudaMemcpyDeviceToHost, s));
+        LRES_CUDA_TRY(cudaStreamSynchronize(s));
+        *lam_min = *std::min_element(lam.begin(), lam.end());
+        return LRES_OK;
+    }
     std::vector<int> all(c->nwin), cnt;
     std::iota(all.begin(), all.end(), 0);
     auto any_below = [&](double sigma, const std::vector<int>& wins, std::vector<int>* keep) -> int {
@@ -1193,9 +1460,10 @@ extern "C" int lres_set_windows(lres_ctx* c, const double* HW, const double* SW,
     if (HW) LRES_CUDA_TRY(cudaMemcpyAsync(c->d_HW, HW, sizeof(double) * c->sizeC, kind, s));
     if (SW) {
         LRES_CUDA_TRY(cudaMemcpyAsync(c->d_SW, SW, sizeof(double) * c->sizeC, kind, s));
-        if (c->precision == LRES_MIXED) TRY(setup_standard_form(c, s));
+        if (needs_standard_form(c)) TRY(setup_standard_form(c, s));
     }
-    if (c->precision == LRES_MIXED) TRY(window_transform(c, s));
+    if (needs_standard_form(c)) TRY(window_transform(c, s));
+    if (c->route == LRES_ROUTE_TRIDIAG) TRY(tri_prepare(c, s));
     c->have_h = true;
     if (!on_device) LRES_CUDA_TRY(cudaStreamSynchronize(s));
     return LRES_OK;
@@ -1460,13 +1728,16 @@ extern "C" int lres_set_trace_rows(lres_ctx* c, const int32_t* r_w, const double
     cudaStream_t s = (cudaStream_t)stream;
     LRES_CUDA_TRY(cudaStreamSynchronize(s));
     for (void* p : {(void*)c->d_mT, (void*)c->d_offFT, (void*)c->d_offQT, (void*)c->d_FT, (void*)c->d_FhatT32,
-                    c->d_qT})
+                    c->d_qT, (void*)c->d_FhatT64, c->d_Ytr})
         if (p) cudaFree(p);
     c->d_mT = nullptr;
     c->d_offFT = c->d_offQT = nullptr;
     c->d_FT = nullptr;
     c->d_FhatT32 = nullptr;
+    c->d_FhatT64 = nullptr;
     c->d_qT = nullptr;
+    c->d_Ytr = nullptr;
+    c->ri_tr.release();
     c->have_trace = false;
     if (!r_w) return LRES_OK;                 // removed
     if (!R) {
@@ -1500,6 +1771,14 @@ extern "C" int lres_set_trace_rows(lres_ctx* c, const int32_t* r_w, const double
     if (mixed) {
         TRY(dalloc(&c->d_FhatT32, c->sizeFT));
         TRY(trace_standard_form(c, s));
+    } else if (needs_standard_form(c)) {
+        TRY(dalloc(&c->d_FhatT64, c->sizeFT));
+        TRY(trace_standard_form(c, s));
+    }
+    if (c->tri_alloc) {
+        TRY(build_row_items(c, m, c->ri_tr, s));
+        TRY(dalloc((char**)&c->d_Ytr, (mixed ? sizeof(float) : sizeof(double)) * (size_t)std::max<long long>(c->sizeFT, 1)));
+        if (c->tri_ready) TRY(tri_rows(c, true, s));
     }
     LRES_CUDA_TRY(cudaStreamSynchronize(s));
     return LRES_OK;

@@ -103,6 +103,27 @@ int pole_sums(int nwin, const long long* offQ, const int* m_w, const long long* 
               const void* q, long long qstride, int npoles, const double2* wq, const double2* wzq, double dV,
               double* dens, double* n_w, double* e_w, cudaStream_t s);
 
+// Multi-shift tridiagonal route (tridiag.cu): R = float (fp32) or double.
+int tri_pick_nb(bool fp32, int nmax, size_t smem_budget, int* nb, int* ldv);
+int tri_reduce(bool fp32, int nwin, const int* order, int* counter, const int* n_w, const long long* offC,
+               const long long* offA, const long long* offN, const void* H, void* A, void* d, void* e, void* tau,
+               int* status, int nb, int ldv, size_t smem_budget, cudaStream_t s);
+int tri_apply(bool fp32, int nitems, const int4* items, const int* n_w, const int* m_w, const long long* offA,
+              const long long* offN, const long long* offF, const void* A, const void* tau, const void* F, void* Y,
+              int nb, int ldv, cudaStream_t s);
+int tri_rows_per_item(bool fp32, int P);
+int tri_pass(bool fp32, int nitems, const int4* items, int* counter, const int* n_w, const int* m_w,
+             const long long* offN, const long long* offF, const long long* offQ, const long long* Oflat,
+             const void* Y, const void* d, const void* e, int P, const void* shifts, const double2* wq,
+             const double2* wzq, double* dens, double* part, int* status, int ldv, size_t smem_budget,
+             cudaStream_t s);
+int tri_window_sums(int nwin, const int* first, const int* count, const double* part, double dV, double* nw,
+                    double* ew, cudaStream_t s);
+int tri_sturm(bool fp32, int nwin, const int* n_w, const long long* offN, const void* d, const void* e,
+              double sigma, int* below, cudaStream_t s);
+int tri_min_eig(bool fp32, int nwin, const int* n_w, const long long* offN, const void* d, const void* e,
+                double tol, double* lam, cudaStream_t s);
+
 // Adjoint of the window solve (adjoint.cu)
 int adj_backsolve(bool fp32, const int2* items, int nitems, const int* n_w, const int* m_w, void* ws,
                   long long ws_stride, int* status, cudaStream_t s);

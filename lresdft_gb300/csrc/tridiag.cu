@@ -1,0 +1,912 @@
+// Multi-shift tridiagonal route of the pole solves (sm_103a).
+//
+// All M/2 poles of a window share its standard-form matrix A = L^-1 H_W L^-T (real
+// symmetric): the shifted systems differ only by z_k I.  The route therefore reduces A
+// once per Hamiltonian to tridiagonal form T = Q^T A Q (Householder), carries the
+// owned-point rows through the same reflectors, Y = F^ Q, and then every pole costs a
+// complex-symmetric LDL^T of the tridiagonal z_k I - T (O(n)) and one forward sweep per
+// row (O(n)):
+//
+//     d_k(r) = f^_r (z_k I - A)^-1 f^_r^T = y_r (z_k I - T)^-1 y_r^T = sum_i u_i^2 / D_i,
+//     D_0 = z - t_0,   D_i = (z - t_i) - e_{i-1}^2 / D_{i-1},
+//     u_0 = y_0,       u_i = y_i + (e_{i-1} / D_{i-1}) u_{i-1}.
+//
+// For Im z > 0, Im D_i >= Im z > 0, so no pivot vanishes and no pivoting is needed.  This
+// is the multi-shift reduction used for transfer functions at many frequencies (A. J.
+// Laub, "Efficient multivariable frequency response computations", IEEE Trans. Autom.
+// Control 26 (1981) 407-408: one Hessenberg reduction, then each shift in O(n^2); for a
+// symmetric matrix the Hessenberg form is tridiagonal and each shift is O(n)).  The
+// quantities are the same as those of the LDL^T route (window_ldl.cu): the density, the
+// electron count and the band energy of every window at every pole, and the pole sums
+// are fused into the pass kernel.
+//
+// Kernels (R = float for the mixed path, double for the FP64 path):
+//   tri_reduce_kernel  one CTA per window (work queue, largest first): blocked Householder
+//                      tridiagonalisation of the full symmetric window matrix held in an
+//                      L2-resident working copy; the rank-2 updates of each panel of nb
+//                      columns are delayed (the panel's v and w vectors in shared memory)
+//                      and applied once per panel.  Algorithmic work (4/3) n^3 flops.
+//   tri_apply_kernel   one CTA per (window, block of up to 256 rows), one thread per row:
+//                      Y = F^ Q by panels in compact WY form, y <- y - ((y V) T_p) V^T.
+//                      Algorithmic work 2 m n^2 flops per window.
+//   tri_pass_kernel    one CTA per (window, batch of rows) from a work queue: thread =
+//                      (pole, rows); the pivot recurrence of its pole is shared by its rows,
+//                      the row values staged in shared memory by asynchronous copies; the
+//                      quadratic forms are reduced over the poles into n(r) and e(r) in
+//                      FP64 in a fixed order.  Algorithmic work ~11 real flops per (pole,
+//                      row, step) plus the pivot recurrence.
+//   tri_sturm_kernel / tri_mineig_kernel   Sturm counts of T - sigma (FP64 arithmetic): the
+//                      Sylvester inertia of sigma S_W - H_W, and the smallest eigenvalue of
+//                      every window by bisection.
+#include "common.cuh"
+#include "launch.cuh"
+#include "lres_internal.h"
+
+#include <algorithm>
+#include <cmath>
+
+namespace lres {
+namespace {
+
+template <class R> struct Cplx;
+template <> struct Cplx<float> { using T = float2; };
+template <> struct Cplx<double> { using T = double2; };
+
+template <class R>
+__device__ __forceinline__ R warp_sum(R x) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    return x;
+}
+
+// Sum over the CTA; every thread gets the same value, bit for bit (the butterfly gives all
+// lanes one result and the warp totals are added in one fixed order).  red: NT/32 slots.
+template <int NT, class R>
+__device__ __forceinline__ R block_sum(R x, R* red) {
+    x = warp_sum(x);
+    __syncthreads();                          // red may still be read by a previous call
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = x;
+    __syncthreads();
+    R s = red[0];
+#pragma unroll
+    for (int w = 1; w < NT / 32; ++w) s += red[w];
+    return s;
+}
+
+constexpr int kRedNT = 512;                   // threads of the reduction kernel
+constexpr int kAppNT = 256;                   // threads (rows) of the apply kernel
+
+// ---------------------------------------------------------------------------
+// Householder tridiagonalisation
+// ---------------------------------------------------------------------------
+
+// Four consecutive rows of a column (16-byte aligned for float, two 16-byte loads for double).
+__device__ __forceinline__ void ld4(const float* p, float (&x)[4]) {
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    x[0] = v.x; x[1] = v.y; x[2] = v.z; x[3] = v.w;
+}
+__device__ __forceinline__ void ld4(const double* p, double (&x)[4]) {
+    const double2 a = *reinterpret_cast<const double2*>(p), b = *reinterpret_cast<const double2*>(p + 2);
+    x[0] = a.x; x[1] = a.y; x[2] = b.x; x[3] = b.y;
+}
+__device__ __forceinline__ void st4(float* p, const float (&x)[4]) {
+    *reinterpret_cast<float4*>(p) = make_float4(x[0], x[1], x[2], x[3]);
+}
+__device__ __forceinline__ void st4(double* p, const double (&x)[4]) {
+    *reinterpret_cast<double2*>(p) = make_double2(x[0], x[1]);
+    *reinterpret_cast<double2*>(p + 2) = make_double2(x[2], x[3]);
+}
+
+template <class R>
+struct TriReduceParams {
+    int nwin;
+    const int* order;        // windows, largest first
+    int* counter;            // work-queue head (zeroed before launch)
+    const int* n_w;
+    const long long* offC;   // standard-form blocks (n x n, column-major)
+    const long long* offA;   // working blocks (ld x n, ld = n rounded up to 4)
+    const long long* offN;   // window vectors (n)
+    const R* H;              // standard-form matrices (lower triangle read)
+    R* A;                    // working copies; on return the reflectors below the subdiagonal
+    R* d;                    // diagonal of T
+    R* e;                    // subdiagonal of T (e[i] couples i and i+1)
+    R* tau;                  // reflector scalars
+    int* status;
+    int nb;                  // panel width (<= 32)
+    int ldv;                 // length of the shared vectors (multiple of 32, >= every n)
+};
+
+// Shared memory of the reduction, in elements of R.
+inline size_t reduce_smem_elems(int nb, int ldv) {
+    const size_t big = std::max((size_t)2 * nb * ldv, (size_t)(kRedNT / 32) * 32 * 33);
+    return big + 2 * (size_t)ldv + 4 * (size_t)kRedNT + 64 + kRedNT / 32;
+}
+
+template <class R, int NT>
+__global__ void __launch_bounds__(NT) tri_reduce_kernel(TriReduceParams<R> p) {
+    constexpr int NW = NT / 32;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int ldv = p.ldv, nb = p.nb;
+    R* const big = reinterpret_cast<R*>(smem_raw);
+    R* const Vs = big;                                   // [nb][ldv]: v_l[i] at Vs[l*ldv + i]
+    R* const Ws = big + (size_t)nb * ldv;                // [nb][ldv]
+    R* const cv = big + std::max((size_t)2 * nb * ldv, (size_t)NW * 32 * 33);   // [ldv] current column
+    R* const pv = cv + ldv;                              // [ldv] p = tau (A v)
+    R* const psum = pv + ldv;                            // [4 NT] split sums of A v
+    R* const dots = psum + 4 * NT;                       // [64] W^T v, V^T v
+    R* const red = dots + 64;                            // [NW]
+    __shared__ int item_sh;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+    for (;;) {
+        if (tid == 0) item_sh = atomicAdd(p.counter, 1);
+        __syncthreads();
+        const int it = item_sh;
+        if (it >= p.nwin) return;
+        const int w = p.order[it];
+        const int n = p.n_w[w];
+        if (n > ldv || n < 1) {
+            if (tid == 0) atomicOr(p.status, ST_BAD_SHAPE);
+            __syncthreads();
+            continue;
+        }
+        const int ld = (n + 3) & ~3;
+        const R* H = p.H + p.offC[w];
+        R* A = p.A + p.offA[w];
+        R* dw = p.d + p.offN[w];
+        R* ew = p.e + p.offN[w];
+        R* tw = p.tau + p.offN[w];
+
+        // ---- A = the full symmetric matrix from the lower triangle of H, by 32 x 32 blocks
+        //      (each warp owns a padded tile: both the block and its transpose are written
+        //      with coalesced stores)
+        {
+            R* tile = big + (size_t)warp * 32 * 33;
+            const int nt = (n + 31) / 32;
+            for (int t = warp; t < nt * (nt + 1) / 2; t += NW) {
+                int bi = 0, bk = t;                      // t-th block of the lower block triangle
+                while (bk > bi) {
+                    bk -= bi + 1;
+                    ++bi;
+                }
+                const int i0 = bi * 32, k0 = bk * 32;
+                for (int c = 0; c < 32; ++c) {
+                    const int i = i0 + lane, k = k0 + c;
+                    tile[c * 33 + lane] = (i < n && k < n) ? H[i + (long long)k * n] : R(0);
+                }
+                __syncwarp();
+                for (int c = 0; c < 32; ++c) {
+                    const int i = i0 + lane, k = k0 + c;
+                    if (i < n && k < n)
+                        A[i + (long long)k * ld] = (bi != bk || lane >= c) ? tile[c * 33 + lane] : tile[lane * 33 + c];
+                }
+                if (bi != bk)
+                    for (int c = 0; c < 32; ++c) {
+                        const int k = k0 + lane, i = i0 + c;
+                        if (i < n && k < n) A[k + (long long)i * ld] = tile[lane * 33 + c];
+                    }
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+
+        // with one row per thread, the panel-start value of column j+1 for the row this thread
+        // handles at step j+1 is loaded during step j
+        const bool pf = n <= NT;
+        R cpre = R(0);
+        for (int j0 = 0; j0 < n - 2; j0 += nb) {
+            const int nbp = min(nb, n - 2 - j0);
+            for (int jj = 0; jj < nbp; ++jj) {
+                const int j = j0 + jj;
+                R cnext = R(0);
+                if (pf && jj + 1 < nbp && j + 1 + tid < n) cnext = A[(j + 1 + tid) + (long long)(j + 1) * ld];
+                // (a) column j of the current matrix (panel-start values minus the pending
+                //     rank-2 updates of this panel), rows >= j; squares of rows >= j+2
+                R part = R(0);
+                for (int i = j + tid; i < n; i += NT) {
+                    R c = (pf && jj > 0) ? cpre : A[i + (long long)j * ld];
+                    for (int l = 0; l < jj; ++l)
+                        c -= Vs[l * ldv + i] * Ws[l * ldv + j] + Ws[l * ldv + i] * Vs[l * ldv + j];
+                    cv[i] = c;
+                    if (i >= j + 2) part += c * c;
+                }
+                cpre = cnext;
+                // (b) reflector H_j = I - tau v v^T with v_{j+1} = 1 mapping rows j+1.. of the
+                //     column onto beta e_{j+1}
+                const R s2 = block_sum<NT>(part, red);    // its barriers also publish cv
+                const R alpha = cv[j + 1];
+                R beta = alpha, tau = R(0), scal = R(0);
+                if (s2 > R(0)) {
+                    const R nrm = sqrt(alpha * alpha + s2);
+                    beta = alpha >= R(0) ? -nrm : nrm;
+                    tau = (beta - alpha) / beta;
+                    scal = R(1) / (alpha - beta);
+                }
+                if (tid == 0) {
+                    dw[j] = cv[j];
+                    ew[j] = beta;
+                    tw[j] = tau;
+                    if (!isfinite((double)beta) || !isfinite((double)cv[j])) atomicOr(p.status, ST_ZERO_PIVOT);
+                }
+                for (int i = tid; i < ldv; i += NT) {
+                    R vi = R(0);
+                    if (i == j + 1) vi = R(1);
+                    else if (i > j + 1 && i < n) vi = cv[i] * scal;
+                    Vs[jj * ldv + i] = vi;
+                    if (i > j + 1 && i < n) A[i + (long long)j * ld] = vi;   // kept for Y = F^ Q
+                }
+                __syncthreads();
+                // (c) p = A v - V (W^T v) - W (V^T v) on rows j+1..n-1
+                for (int q = warp; q < 2 * jj; q += NW) {
+                    const R* X = q < jj ? Ws + (size_t)q * ldv : Vs + (size_t)(q - jj) * ldv;
+                    R acc = R(0);
+                    for (int i = j + 1 + lane; i < n; i += 32) acc += X[i] * Vs[jj * ldv + i];
+                    acc = warp_sum(acc);
+                    if (lane == 0) dots[q] = acc;
+                }
+                // A v by quads of rows (16-byte loads) from the aligned row i0 <= j+1; when the
+                // quads are few, the columns are split across thread groups and the partial
+                // sums added in a fixed order.  Sums are blocked: each run of 32 terms from zero.
+                const int i0 = (j + 1) & ~3;
+                const int nq = (ld - i0) >> 2;
+                const int nsplit = nq >= NT ? 1 : NT / nq;
+                {
+                    const R* vv = Vs + (size_t)jj * ldv;
+                    const int qstep = nq >= NT ? NT : nq;
+                    if (tid < qstep * nsplit) {
+                        const int sp = tid / qstep;
+                        for (int q = tid % qstep; q < nq; q += qstep) {
+                            const R* Aq = A + i0 + 4 * q;
+                            R a[4] = {R(0), R(0), R(0), R(0)};
+                            for (int kb = j + 1 + sp; kb < n; kb += 32 * nsplit) {
+                                const int ke = min(n, kb + 32 * nsplit);
+                                R c[4] = {R(0), R(0), R(0), R(0)};
+#pragma unroll 8
+                                for (int k = kb; k < ke; k += nsplit) {
+                                    R x[4];
+                                    ld4(Aq + (long long)k * ld, x);
+                                    const R vk = vv[k];
+#pragma unroll
+                                    for (int r = 0; r < 4; ++r) c[r] = fma(x[r], vk, c[r]);
+                                }
+#pragma unroll
+                                for (int r = 0; r < 4; ++r) a[r] += c[r];
+                            }
+                            if (nsplit > 1) {
+#pragma unroll
+                                for (int r = 0; r < 4; ++r) psum[(sp * nq + q) * 4 + r] = a[r];
+                            } else {
+#pragma unroll
+                                for (int r = 0; r < 4; ++r) {
+                                    const int i = i0 + 4 * q + r;
+                                    if (i > j && i < n) pv[i] = a[r];
+                                }
+                            }
+                        }
+                    }
+                }
+                __syncthreads();
+                // (d) p *= tau, K = tau/2 p.v, w = p - K v
+                R partK = R(0);
+                for (int i = j + 1 + tid; i < n; i += NT) {
+                    R pi;
+                    if (nsplit > 1) {
+                        const int q = (i - i0) >> 2, r = (i - i0) & 3;
+                        pi = R(0);
+                        for (int sp = 0; sp < nsplit; ++sp) pi += psum[(sp * nq + q) * 4 + r];
+                    } else {
+                        pi = pv[i];
+                    }
+                    for (int l = 0; l < jj; ++l) pi -= Vs[l * ldv + i] * dots[l] + Ws[l * ldv + i] * dots[jj + l];
+                    pi *= tau;
+                    pv[i] = pi;
+                    partK += pi * Vs[jj * ldv + i];
+                }
+                const R K = R(0.5) * tau * block_sum<NT>(partK, red);
+                for (int i = tid; i < ldv; i += NT)
+                    Ws[jj * ldv + i] = (i > j && i < n) ? pv[i] - K * Vs[jj * ldv + i] : R(0);
+                __syncthreads();
+            }
+            // ---- trailing update of both triangles: A -= V W^T + W V^T on rows, columns >= t0,
+            //      one quad of rows x TC columns per thread (rows below t0 left unchanged)
+            const int t0 = j0 + nbp;
+            if (t0 < n) {
+                constexpr int TC = 4;
+                const int q0 = t0 & ~3;
+                const int nq = (ld - q0) >> 2;
+                const int ncb = (n - t0 + TC - 1) / TC;
+                for (int tile = tid; tile < nq * ncb; tile += NT) {
+                    const int q = tile % nq, cb = tile / nq;
+                    const int i = q0 + 4 * q, c0 = t0 + cb * TC;
+                    R acc[TC][4];
+#pragma unroll
+                    for (int c = 0; c < TC; ++c)
+#pragma unroll
+                        for (int r = 0; r < 4; ++r) acc[c][r] = R(0);
+                    for (int l = 0; l < nbp; ++l) {
+                        R vi[4], wi[4];
+#pragma unroll
+                        for (int r = 0; r < 4; ++r) {
+                            vi[r] = Vs[l * ldv + i + r];
+                            wi[r] = Ws[l * ldv + i + r];
+                        }
+#pragma unroll
+                        for (int c = 0; c < TC; ++c) {
+                            const int col = min(c0 + c, ldv - 1);     // reads stay inside the vectors
+                            const R wk = Ws[l * ldv + col], vk = Vs[l * ldv + col];
+#pragma unroll
+                            for (int r = 0; r < 4; ++r) acc[c][r] = fma(vi[r], wk, fma(wi[r], vk, acc[c][r]));
+                        }
+                    }
+#pragma unroll
+                    for (int c = 0; c < TC; ++c) {
+                        if (c0 + c >= n) continue;
+                        R x[4];
+                        R* dst = A + i + (long long)(c0 + c) * ld;
+                        ld4(dst, x);
+#pragma unroll
+                        for (int r = 0; r < 4; ++r)
+                            if (i + r >= t0) x[r] -= acc[c][r];
+                        st4(dst, x);
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        // ---- the last (at most 2 x 2) block, fully updated
+        if (tid == 0) {
+            if (n >= 2) {
+                dw[n - 2] = A[(n - 2) + (long long)(n - 2) * ld];
+                ew[n - 2] = A[(n - 1) + (long long)(n - 2) * ld];
+                dw[n - 1] = A[(n - 1) + (long long)(n - 1) * ld];
+                tw[n - 2] = R(0);
+                tw[n - 1] = R(0);
+                ew[n - 1] = R(0);
+            } else {
+                dw[0] = A[0];
+                tw[0] = R(0);
+                ew[0] = R(0);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Y = F^ Q: the rows through the reflectors, compact WY per panel
+// ---------------------------------------------------------------------------
+
+template <class R>
+struct TriApplyParams {
+    int nitems;
+    const int4* items;       // (window, first row, rows <= 256, -)
+    const int* n_w;
+    const int* m_w;          // rows of each window
+    const long long* offA;   // reflectors (working blocks, leading dimension n rounded up to 4)
+    const long long* offN;
+    const long long* offF;   // row blocks, F[r + a*m]
+    const R* A;              // reflectors below the subdiagonal (tri_reduce_kernel)
+    const R* tau;
+    const R* F;              // standard-form rows
+    R* Y;                    // F^ Q, same layout
+    int ldv;
+};
+
+template <class R, int NT, int NB>
+__global__ void __launch_bounds__(NT) tri_apply_kernel(TriApplyParams<R> p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R* const Vs = reinterpret_cast<R*>(smem_raw);         // [ldv][NB]: v_l[k] at Vs[k*NB + l]
+    R* const Tm = Vs + (size_t)p.ldv * NB;                 // [NB][NB] upper triangular factor
+    R* const Gm = Tm + NB * NB;                            // [NB][NB] V^T V (above the diagonal)
+    const int4 item = p.items[blockIdx.x];
+    const int w = item.x, r0 = item.y, nr = item.z;
+    const int n = p.n_w[w], m = p.m_w[w];
+    if (n > p.ldv) return;                                 // the reduction flagged this window
+    const long long ld = (n + 3) & ~3;
+    const R* Aw = p.A + p.offA[w];
+    const R* tw = p.tau + p.offN[w];
+    const R* Fw = p.F + p.offF[w];
+    R* Yw = p.Y + p.offF[w];
+    const int tid = threadIdx.x;
+    const bool act = tid < nr && r0 + tid < m;
+    const long long r = r0 + tid;
+    if (act) {
+#pragma unroll 8
+        for (int k = 0; k < n; ++k) Yw[r + (long long)k * m] = Fw[r + (long long)k * m];
+    }
+
+    for (int j0 = 0; j0 < n - 2; j0 += NB) {
+        const int nbp = min(NB, n - 2 - j0);
+        __syncthreads();                                   // the previous panel is consumed
+        for (int idx = tid; idx < (n - j0) * NB; idx += NT) {
+            const int k = j0 + idx / NB, l = idx % NB;
+            R v = R(0);
+            if (l < nbp) {
+                const int j = j0 + l;
+                if (k == j + 1) v = R(1);
+                else if (k > j + 1) v = Aw[k + j * ld];
+            }
+            Vs[(size_t)k * NB + l] = v;
+        }
+        __syncthreads();
+        for (int q = tid; q < NB * NB; q += NT) {
+            const int a = q / NB, b = q % NB;
+            R g = R(0);
+            if (a < b && b < nbp)
+                for (int k = j0 + b + 1; k < n; ++k) g += Vs[(size_t)k * NB + a] * Vs[(size_t)k * NB + b];
+            Gm[q] = g;
+        }
+        __syncthreads();
+        // T (forward, columnwise): T_ll = tau_l, T[0:l, l] = -tau_l T[0:l, 0:l] (V^T V)[0:l, l]
+        if (tid < 32) {
+            for (int l = 0; l < NB; ++l) {
+                const R tl = l < nbp ? tw[j0 + l] : R(0);
+                for (int a = tid; a < NB; a += 32) {
+                    R val = R(0);
+                    if (a < l) {
+                        R s = R(0);
+                        for (int b = a; b < l; ++b) s += Tm[a * NB + b] * Gm[b * NB + l];
+                        val = -tl * s;
+                    } else if (a == l) {
+                        val = tl;
+                    }
+                    Tm[a * NB + l] = val;
+                }
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+        if (act) {
+            R sv[NB];
+#pragma unroll
+            for (int l = 0; l < NB; ++l) sv[l] = R(0);
+#pragma unroll 8
+            for (int k = j0 + 1; k < n; ++k) {
+                const R y = Yw[r + (long long)k * m];
+                const R* vk = Vs + (size_t)k * NB;
+#pragma unroll
+                for (int l = 0; l < NB; ++l) sv[l] = fma(y, vk[l], sv[l]);
+            }
+            // s <- s T in place (T upper triangular: column b needs s_0..s_b, so b descends)
+#pragma unroll
+            for (int b = NB - 1; b >= 0; --b) {
+                R acc = R(0);
+#pragma unroll
+                for (int a = 0; a <= b; ++a) acc = fma(sv[a], Tm[a * NB + b], acc);
+                sv[b] = acc;
+            }
+#pragma unroll 8
+            for (int k = j0 + 1; k < n; ++k) {
+                const R* vk = Vs + (size_t)k * NB;
+                R acc = R(0);
+#pragma unroll
+                for (int l = 0; l < NB; ++l) acc = fma(sv[l], vk[l], acc);
+                Yw[r + (long long)k * m] -= acc;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// shifted tridiagonal solves at all poles, fused with the pole sums
+// ---------------------------------------------------------------------------
+
+template <class R>
+struct TriPassParams {
+    int nitems;
+    const int4* items;       // (window, first row, rows <= rows per batch, -)
+    int* counter;
+    const int* n_w;
+    const int* m_w;
+    const long long* offN;
+    const long long* offF;   // rows Y[r + i*m]
+    const long long* offQ;   // first point of each window in Oflat
+    const long long* Oflat;  // grid index of every owned point (nullable: no density)
+    const R* Y;
+    const R* d;
+    const R* e;
+    int P;                   // poles (upper half plane)
+    const typename Cplx<R>::T* shifts;
+    const double2* wq;       // w_k
+    const double2* wzq;      // w_k z_k
+    double* dens;            // nullable
+    double* part;            // [2 * nitems]: sum over the item's rows of n(r), e(r)
+    int* status;
+    int ldv;
+};
+
+template <class R>
+__device__ __forceinline__ void cp_async4(R* dst, const R* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    if constexpr (sizeof(R) == 8) asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src));
+    else asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src));
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+constexpr int kPassNT = 256;
+constexpr int kPassIC = 32;                   // steps per staged chunk
+constexpr int kPassMaxRows = 256;             // rows per pass item at most
+
+// Row groups of the pass kernel: thread = (pole, group), each group RR rows.
+__host__ __device__ inline int pass_groups(int P, int RR) {
+    const int g = kPassNT / P, cap = kPassMaxRows / RR;
+    return g < cap ? g : cap;
+}
+
+inline size_t pass_smem_bytes(int elem, int P, int RR, int ldv) {
+    const int RB = pass_groups(P, RR) * RR;
+    return sizeof(double2) * (size_t)RB * P + (size_t)elem * (2 * (size_t)ldv + 2 * (size_t)kPassIC * RB);
+}
+
+template <class R, int NT, int RR>
+__global__ void __launch_bounds__(NT) tri_pass_kernel(TriPassParams<R> p) {
+    using C = typename Cplx<R>::T;
+    constexpr int IC = kPassIC;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int P = p.P;
+    const int G = pass_groups(P, RR);              // row groups
+    const int RB = G * RR;                         // rows per item
+    double2* const red = reinterpret_cast<double2*>(smem_raw);      // [RB][P]
+    R* const ds = reinterpret_cast<R*>(red + (size_t)RB * P);         // [ldv]
+    R* const es = ds + p.ldv;                                         // [ldv]
+    R* const yb = es + p.ldv;                                         // [2][IC][RB]
+    __shared__ double sred[NT / 32];
+    __shared__ int item_sh;
+    const int tid = threadIdx.x;
+    const int k = tid % P, g = tid / P;
+    const bool on = g < G;
+
+    for (;;) {
+        if (tid == 0) item_sh = atomicAdd(p.counter, 1);
+        __syncthreads();
+        const int it = item_sh;
+        if (it >= p.nitems) return;
+        const int4 item = p.items[it];
+        const int w = item.x, r0 = item.y, nr = item.z;
+        const int n = p.n_w[w], m = p.m_w[w];
+        if (n > p.ldv || nr > RB) {
+            if (tid == 0) atomicOr(p.status, ST_BAD_SHAPE);
+            __syncthreads();
+            continue;
+        }
+        const R* Yw = p.Y + p.offF[w] + r0;
+        for (int i = tid; i < n; i += NT) {
+            ds[i] = p.d[p.offN[w] + i];
+            es[i] = i < n - 1 ? p.e[p.offN[w] + i] : R(0);
+        }
+        // rows [r0, r0 + nr) of the window; steps i staged by chunks of IC
+        auto stage = [&](int c, int buf) {
+            R* dst = yb + (size_t)buf * IC * RB;
+            for (int idx = tid; idx < IC * RB; idx += NT) {
+                const int ic = idx / RB, row = idx % RB;
+                const int i = c * IC + ic;
+                if (row < nr && i < n) cp_async4(dst + idx, Yw + row + (long long)i * m);
+                else dst[idx] = R(0);
+            }
+            cp_commit();
+        };
+        const int nch = (n + IC - 1) / IC;
+        stage(0, 0);
+
+        const C z = p.shifts[k < P ? k : 0];
+        C gp = C{R(0), R(0)};                       // 1 / D_{i-1}
+        C uc[RR], pr[RR];
+        double2 acc[RR];
+#pragma unroll
+        for (int u = 0; u < RR; ++u) {
+            uc[u] = C{R(0), R(0)};
+            pr[u] = C{R(0), R(0)};
+            acc[u] = make_double2(0.0, 0.0);
+        }
+        for (int c = 0; c < nch; ++c) {
+            if (c + 1 < nch) {
+                stage(c + 1, (c + 1) & 1);
+                cp_wait<1>();
+            } else {
+                cp_wait<0>();
+            }
+            __syncthreads();                          // chunk c (and d, e) visible
+            const R* yc = yb + (size_t)(c & 1) * IC * RB + g * RR;
+            const int i0 = c * IC, i1 = min(n, i0 + IC);
+            if (on) {
+                for (int i = i0; i < i1; ++i) {
+                    const R di = ds[i];
+                    C t, D;
+                    if (i == 0) {
+                        t = C{R(0), R(0)};
+                        D = C{z.x - di, z.y};
+                    } else {
+                        const R ei = es[i - 1];
+                        t = C{ei * gp.x, ei * gp.y};
+                        D = C{z.x - di - ei * t.x, z.y - ei * t.y};
+                    }
+                    const R inv = R(1) / (D.x * D.x + D.y * D.y);
+                    gp = C{D.x * inv, -D.y * inv};
+                    const R* yi = yc + (size_t)(i - i0) * RB;
+#pragma unroll
+                    for (int u = 0; u < RR; ++u) {
+                        const R y = yi[u];
+                        const R ur = fma(t.x, uc[u].x, fma(-t.y, uc[u].y, y));
+                        const R ui = fma(t.x, uc[u].y, t.y * uc[u].x);
+                        uc[u] = C{ur, ui};
+                        const R sr = fma(ur, ur, -ui * ui);
+                        const R si = R(2) * ur * ui;
+                        pr[u].x = fma(sr, gp.x, fma(-si, gp.y, pr[u].x));
+                        pr[u].y = fma(sr, gp.y, fma(si, gp.x, pr[u].y));
+                    }
+                }
+                // each chunk's sum is formed from zero and added in FP64
+#pragma unroll
+                for (int u = 0; u < RR; ++u) {
+                    acc[u].x += (double)pr[u].x;
+                    acc[u].y += (double)pr[u].y;
+                    pr[u] = C{R(0), R(0)};
+                }
+            }
+            __syncthreads();                          // buffer c & 1 is free for chunk c + 2
+        }
+        // pole sums: n(r) = 4 Re sum_k w_k d_k(r), e(r) = 4 Re sum_k w_k z_k d_k(r)
+        if (on) {
+            const double2 a = p.wq[k], b = p.wzq[k];
+#pragma unroll
+            for (int u = 0; u < RR; ++u) {
+                const double qx = acc[u].x, qy = acc[u].y;
+                red[(size_t)(g * RR + u) * P + k] = make_double2(a.x * qx - a.y * qy, b.x * qx - b.y * qy);
+            }
+        }
+        __syncthreads();
+        double tn = 0.0, te = 0.0;
+        for (int row = tid; row < nr; row += NT) {
+            double sn = 0.0, se = 0.0;
+            for (int kk = 0; kk < P; ++kk) {
+                const double2 v = red[(size_t)row * P + kk];
+                sn += v.x;
+                se += v.y;
+            }
+            const double nrow = 4.0 * sn, erow = 4.0 * se;
+            if (!isfinite(nrow) || !isfinite(erow)) atomicOr(p.status, ST_ZERO_PIVOT);
+            if (p.dens) p.dens[p.Oflat[p.offQ[w] + r0 + row]] = nrow;
+            tn += nrow;
+            te += erow;
+        }
+        tn = block_sum<NT>(tn, sred);
+        te = block_sum<NT>(te, sred);
+        if (tid == 0) {
+            p.part[2 * (size_t)it] = tn;
+            p.part[2 * (size_t)it + 1] = te;
+        }
+        __syncthreads();
+    }
+}
+
+// per-window totals from the items of each window (contiguous, fixed order)
+__global__ void tri_window_sums_kernel(int nwin, const int* first, const int* count, const double* part, double dV,
+                                       double* nw, double* ew) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nwin) return;
+    double sn = 0.0, se = 0.0;
+    for (int i = first[w]; i < first[w] + count[w]; ++i) {
+        sn += part[2 * (size_t)i];
+        se += part[2 * (size_t)i + 1];
+    }
+    nw[w] = sn * dV;
+    ew[w] = se * dV;
+}
+
+// ---------------------------------------------------------------------------
+// Sturm counts on T (FP64 arithmetic)
+// ---------------------------------------------------------------------------
+
+// Eigenvalues of the tridiagonal (d, e) below sigma = negative pivots of T - sigma I.
+template <class R>
+__device__ int sturm_count(int n, const R* d, const R* e, double sigma) {
+    constexpr double pivmin = 1e-290;
+    int cnt = 0;
+    double q = (double)d[0] - sigma;
+    if (fabs(q) < pivmin) q = -pivmin;
+    if (q < 0.0) ++cnt;
+    for (int i = 1; i < n; ++i) {
+        const double ee = (double)e[i - 1];
+        q = ((double)d[i] - sigma) - ee * ee / q;
+        if (fabs(q) < pivmin) q = -pivmin;
+        if (q < 0.0) ++cnt;
+    }
+    return cnt;
+}
+
+template <class R>
+__global__ void tri_sturm_kernel(int nwin, const int* n_w, const long long* offN, const R* d, const R* e,
+                                 double sigma, int* below) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nwin) return;
+    below[w] = sturm_count(n_w[w], d + offN[w], e + offN[w], sigma);
+}
+
+// Smallest eigenvalue of every window: bisection on the Sturm count from the Gershgorin
+// interval down to width tol; lam[w] = midpoint of the last bracket.
+template <class R>
+__global__ void tri_mineig_kernel(int nwin, const int* n_w, const long long* offN, const R* d, const R* e,
+                                  double tol, double* lam) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nwin) return;
+    const int n = n_w[w];
+    const R* dw = d + offN[w];
+    const R* ew = e + offN[w];
+    double lo = 1e300, hi = -1e300;
+    for (int i = 0; i < n; ++i) {
+        const double r = (i > 0 ? fabs((double)ew[i - 1]) : 0.0) + (i < n - 1 ? fabs((double)ew[i]) : 0.0);
+        lo = fmin(lo, (double)dw[i] - r);
+        hi = fmax(hi, (double)dw[i] + r);
+    }
+    const double pad = 1e-12 * fmax(1.0, fmax(fabs(lo), fabs(hi)));
+    double a = lo - pad, b = hi + pad;
+    for (int iter = 0; iter < 200 && b - a > tol; ++iter) {
+        const double mid = 0.5 * (a + b);
+        if (sturm_count(n, dw, ew, mid) >= 1) b = mid;
+        else a = mid;
+    }
+    lam[w] = 0.5 * (a + b);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host launchers
+// ---------------------------------------------------------------------------
+
+int tri_pick_nb(bool fp32, int nmax, size_t smem_budget, int* nb, int* ldv) {
+    const int el = fp32 ? 4 : 8;
+    *ldv = (std::max(nmax, 1) + 31) / 32 * 32;
+    for (int b : {32, 16, 8, 4}) {
+        const size_t red = reduce_smem_elems(b, *ldv) * el;
+        const size_t app = (size_t)el * ((size_t)*ldv * b + 2 * b * b);
+        if (red <= smem_budget && app <= smem_budget) {
+            *nb = b;
+            return LRES_OK;
+        }
+    }
+    lres_set_error("windows of %d functions exceed the shared memory of the tridiagonal reduction", nmax);
+    return LRES_EINVAL;
+}
+
+template <class R>
+static int launch_reduce(const TriReduceParams<R>& p, size_t smem_budget, cudaStream_t s) {
+    const size_t smem = reduce_smem_elems(p.nb, p.ldv) * sizeof(R);
+    if (smem > smem_budget) {
+        lres_set_error("tridiagonal reduction needs %zu B of shared memory", smem);
+        return LRES_EINVAL;
+    }
+    int per_sm = 0;
+    if (int rc = prepare_kernel<tri_reduce_kernel<R, kRedNT>>(kRedNT, smem, &per_sm)) return rc;
+    const int grid = std::min(p.nwin, std::max(1, per_sm) * device_sms());
+    tri_reduce_kernel<R, kRedNT><<<grid, kRedNT, smem, s>>>(p);
+    LRES_CUDA_TRY(cudaGetLastError());
+    return LRES_OK;
+}
+
+int tri_reduce(bool fp32, int nwin, const int* order, int* counter, const int* n_w, const long long* offC,
+               const long long* offA, const long long* offN, const void* H, void* A, void* d, void* e, void* tau,
+               int* status, int nb, int ldv, size_t smem_budget, cudaStream_t s) {
+    if (!nwin) return LRES_OK;
+    LRES_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), s));
+    if (fp32) {
+        TriReduceParams<float> p{nwin, order, counter, n_w, offC, offA, offN, (const float*)H, (float*)A,
+                                 (float*)d, (float*)e, (float*)tau, status, nb, ldv};
+        return launch_reduce(p, smem_budget, s);
+    }
+    TriReduceParams<double> p{nwin, order, counter, n_w, offC, offA, offN, (const double*)H, (double*)A,
+                              (double*)d, (double*)e, (double*)tau, status, nb, ldv};
+    return launch_reduce(p, smem_budget, s);
+}
+
+template <class R, int NB>
+static int launch_apply(const TriApplyParams<R>& p, cudaStream_t s) {
+    const size_t smem = sizeof(R) * ((size_t)p.ldv * NB + 2 * NB * NB);
+    int per_sm = 0;
+    if (int rc = prepare_kernel<tri_apply_kernel<R, kAppNT, NB>>(kAppNT, smem, &per_sm)) return rc;
+    tri_apply_kernel<R, kAppNT, NB><<<p.nitems, kAppNT, smem, s>>>(p);
+    LRES_CUDA_TRY(cudaGetLastError());
+    return LRES_OK;
+}
+
+template <class R>
+static int dispatch_apply(const TriApplyParams<R>& p, int nb, cudaStream_t s) {
+    switch (nb) {
+        case 32: return launch_apply<R, 32>(p, s);
+        case 16: return launch_apply<R, 16>(p, s);
+        case 8: return launch_apply<R, 8>(p, s);
+        case 4: return launch_apply<R, 4>(p, s);
+        default:
+            lres_set_error("tridiagonal panel width %d not compiled", nb);
+            return LRES_EINVAL;
+    }
+}
+
+int tri_apply(bool fp32, int nitems, const int4* items, const int* n_w, const int* m_w, const long long* offA,
+              const long long* offN, const long long* offF, const void* A, const void* tau, const void* F, void* Y,
+              int nb, int ldv, cudaStream_t s) {
+    if (!nitems) return LRES_OK;
+    if (fp32) {
+        TriApplyParams<float> p{nitems, items, n_w, m_w, offA, offN, offF, (const float*)A, (const float*)tau,
+                                (const float*)F, (float*)Y, ldv};
+        return dispatch_apply(p, nb, s);
+    }
+    TriApplyParams<double> p{nitems, items, n_w, m_w, offA, offN, offF, (const double*)A, (const double*)tau,
+                             (const double*)F, (double*)Y, ldv};
+    return dispatch_apply(p, nb, s);
+}
+
+int tri_rows_per_item(bool fp32, int P) {
+    const int RR = fp32 ? 8 : 4;
+    return pass_groups(std::max(P, 1), RR) * RR;
+}
+
+template <class R, int RR>
+static int launch_pass(const TriPassParams<R>& p, size_t smem_budget, cudaStream_t s) {
+    const size_t smem = pass_smem_bytes(sizeof(R), p.P, RR, p.ldv);
+    if (smem > smem_budget) {
+        lres_set_error("pole pass needs %zu B of shared memory (P = %d, windows up to %d)", smem, p.P, p.ldv);
+        return LRES_EINVAL;
+    }
+    int per_sm = 0;
+    if (int rc = prepare_kernel<tri_pass_kernel<R, kPassNT, RR>>(kPassNT, smem, &per_sm)) return rc;
+    const int grid = std::min(p.nitems, std::max(1, per_sm) * device_sms());
+    tri_pass_kernel<R, kPassNT, RR><<<grid, kPassNT, smem, s>>>(p);
+    LRES_CUDA_TRY(cudaGetLastError());
+    return LRES_OK;
+}
+
+int tri_pass(bool fp32, int nitems, const int4* items, int* counter, const int* n_w, const int* m_w,
+             const long long* offN, const long long* offF, const long long* offQ, const long long* Oflat,
+             const void* Y, const void* d, const void* e, int P, const void* shifts, const double2* wq,
+             const double2* wzq, double* dens, double* part, int* status, int ldv, size_t smem_budget,
+             cudaStream_t s) {
+    if (!nitems) return LRES_OK;
+    if (P < 1 || P > kPassNT) {
+        lres_set_error("pole pass supports 1..%d poles per half plane (got %d)", kPassNT, P);
+        return LRES_EINVAL;
+    }
+    LRES_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), s));
+    if (fp32) {
+        TriPassParams<float> p{nitems, items, counter, n_w, m_w, offN, offF, offQ, Oflat, (const float*)Y,
+                               (const float*)d, (const float*)e, P, (const float2*)shifts, wq, wzq, dens, part,
+                               status, ldv};
+        return launch_pass<float, 8>(p, smem_budget, s);
+    }
+    TriPassParams<double> p{nitems, items, counter, n_w, m_w, offN, offF, offQ, Oflat, (const double*)Y,
+                            (const double*)d, (const double*)e, P, (const double2*)shifts, wq, wzq, dens, part,
+                            status, ldv};
+    return launch_pass<double, 4>(p, smem_budget, s);
+}
+
+int tri_window_sums(int nwin, const int* first, const int* count, const double* part, double dV, double* nw,
+                    double* ew, cudaStream_t s) {
+    if (!nwin) return LRES_OK;
+    tri_window_sums_kernel<<<(nwin + 127) / 128, 128, 0, s>>>(nwin, first, count, part, dV, nw, ew);
+    LRES_CUDA_TRY(cudaGetLastError());
+    return LRES_OK;
+}
+
+int tri_sturm(bool fp32, int nwin, const int* n_w, const long long* offN, const void* d, const void* e,
+              double sigma, int* below, cudaStream_t s) {
+    if (!nwin) return LRES_OK;
+    const int grid = (nwin + 63) / 64;
+    if (fp32) tri_sturm_kernel<float><<<grid, 64, 0, s>>>(nwin, n_w, offN, (const float*)d, (const float*)e, sigma, below);
+    else tri_sturm_kernel<double><<<grid, 64, 0, s>>>(nwin, n_w, offN, (const double*)d, (const double*)e, sigma, below);
+    LRES_CUDA_TRY(cudaGetLastError());
+    return LRES_OK;
+}
+
+int tri_min_eig(bool fp32, int nwin, const int* n_w, const long long* offN, const void* d, const void* e,
+                double tol, double* lam, cudaStream_t s) {
+    if (!nwin) return LRES_OK;
+    const int grid = (nwin + 31) / 32;
+    if (fp32) tri_mineig_kernel<float><<<grid, 32, 0, s>>>(nwin, n_w, offN, (const float*)d, (const float*)e, tol, lam);
+    else tri_mineig_kernel<double><<<grid, 32, 0, s>>>(nwin, n_w, offN, (const double*)d, (const double*)e, tol, lam);
+    LRES_CUDA_TRY(cudaGetLastError());
+    return LRES_OK;
+}
+
+}  // namespace lres

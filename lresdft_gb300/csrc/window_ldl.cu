@@ -31,6 +31,7 @@
 // (32/3) n^3 real flops of a complex LU + full inverse): about
 // (2/3) n^3 + 2 n^2 m real FMAs (complex case: 4 real FMAs per complex MAC).
 #include "common.cuh"
+#include "launch.cuh"
 #include "lres_internal.h"
 
 #include <algorithm>
@@ -75,42 +76,6 @@ struct LdlParams {
     const int* c0;              // per window (nullable): F is zero in the columns before c0[w], so
                                 // its rows of G are zero there too and are not computed
 };
-
-// Dynamic shared memory attribute and occupancy of a kernel, set/queried only when the
-// request grows, so that launches enqueued during CUDA-graph capture issue no attribute
-// calls (the first, eager launch of each instantiation on each device does).  Cached per
-// device (up to kMaxDevices devices in one process).
-constexpr int kMaxDevices = 16;
-
-static int current_device() {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    return dev < 0 ? 0 : (dev >= kMaxDevices ? kMaxDevices - 1 : dev);
-}
-
-template <auto Kern>
-static int prepare_kernel(int threads, size_t smem, int* per_sm) {
-    static size_t set_smem[kMaxDevices] = {};     // one cache per kernel instantiation and device
-    static int cached_per_sm[kMaxDevices] = {};
-    const int dev = current_device();
-    if (smem > set_smem[dev]) {
-        LRES_CUDA_TRY(cudaFuncSetAttribute(Kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        // prefer the largest shared-memory carveout, so that the occupancy below is the maximum
-        LRES_CUDA_TRY(cudaFuncSetAttribute(Kern, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                           (int)cudaSharedmemCarveoutMaxShared));
-        LRES_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cached_per_sm[dev], Kern, threads, smem));
-        set_smem[dev] = smem;
-    }
-    *per_sm = cached_per_sm[dev];
-    return LRES_OK;
-}
-
-static int device_sms() {
-    static int nsm[kMaxDevices] = {};
-    const int dev = current_device();
-    if (!nsm[dev]) cudaDeviceGetAttribute(&nsm[dev], cudaDevAttrMultiProcessorCount, dev);
-    return nsm[dev];
-}
 
 template <class T, int NB, int TR, int TC, int NT>
 __global__ void __launch_bounds__(NT) ldl_aug_kernel(LdlParams<T> p) {
@@ -1551,7 +1516,7 @@ struct NoallocDevice {
     int smem_budget = 0;
 };
 std::mutex g_noalloc_mu;
-NoallocDevice g_noalloc_dev[64];
+NoallocDevice g_noalloc_dev[kMaxDevices];
 
 __global__ void noalloc_init_kernel(unsigned char* base, int nwin, double sigma) {
     int* counter = reinterpret_cast<int*>(base);
@@ -1571,8 +1536,8 @@ __global__ void noalloc_init_kernel(unsigned char* base, int nwin, double sigma)
 int noalloc_device(NoallocDevice** out) {
     int dev = 0;
     LRES_CUDA_TRY(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 64) {
-        lres_set_error("device index %d out of range", dev);
+    if (dev < 0 || dev >= kMaxDevices) {
+        lres_set_error("device index %d outside the supported range 0..%d", dev, kMaxDevices - 1);
         return LRES_EINVAL;
     }
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
@@ -1652,6 +1617,12 @@ extern "C" int lres_inertia_noalloc(int32_t nwin, const int32_t* n_w, const int6
     if (st & ST_BAD_SHAPE) {
         lres_set_error("lres_inertia_noalloc: a window is larger than nmax = %d", nmax);
         return LRES_EINVAL;
+    }
+    if (st & ST_ZERO_PIVOT) {
+        // a zero or non-finite pivot (NaN/Inf in H or S, or sigma on an eigenvalue): the
+        // counts of that window are meaningless
+        lres_set_error("lres_inertia_noalloc: zero or non-finite pivot in a window factorisation");
+        return LRES_ENUMERIC;
     }
     return LRES_OK;
 }

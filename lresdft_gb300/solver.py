@@ -21,8 +21,12 @@ warm/cold decisions:
   (the count is monotone in mu, so the root is the same), else from
   [max(lambda_min, e_lo+1e-6), +1] widened by 0.5 (lrft/lcao3d.py:387-398).
 
-Each N(mu) evaluation is a full pole pass (the poles move with mu), so mu is found
-by Brent's method on pass results; the last pass at the accepted mu is the density.
+Each N(mu) evaluation is a pole pass (the poles move with mu), so mu is found by
+Brent's method on pass results; the last pass at the accepted mu is the density.  On
+the default tridiagonal route (liblres_gb300, LRES_ROUTE_TRIDIAG) every window's
+standard form is reduced once per Hamiltonian to tridiagonal form, so each pass costs
+O(M/2 x rows x n_W) instead of M/2 dense factorisations; the inertia counts of the mu
+logic are then Sturm counts of those tridiagonal matrices.
 With trace rows installed (fine grids) the trial passes run over them and produce no
 density; the accepted mu then gets one density pass over the owned points.
 """
@@ -149,13 +153,15 @@ def trace_factor(K, rtol=1e-14):
 class LResGPU:
     """GPU pole-route LRes window solver with the LRFTLCAOCpp interface.
 
-    Extra keyword ``precision``: "fp64" (complex128 factor/solve throughout) or
+    Extra keywords: ``precision`` "fp64" (complex128 factor/solve throughout) or
     "mixed" (complex64 factor/solve of the standard-form windows
     L^-1 (z S - H) L^-T, FP64 Cholesky/orthogonalisation, FP64 pole sums, electron
-    count and energies)."""
+    count and energies); ``route`` "auto" (the library's choice: tridiagonal unless the
+    context has fewer than 4 windows or windows too large for it), "tridiag" or "ldl"
+    (one dense LDL^T per window and pole)."""
 
     def __init__(self, basis, cells, R_w=12.1, M=64, margin=0.3, nthreads=1, lag_mu=False, reuse_vectors=True,
-                 precision="fp64", tile_config=None, trace_rows="auto", merge_windows="auto"):
+                 precision="fp64", tile_config=None, trace_rows="auto", merge_windows="auto", route="auto"):
         if M % 2 or M < 2:
             raise ValueError(f"M must be even and >= 2 (got {M})")
         if precision not in ("fp64", "mixed"):
@@ -164,6 +170,8 @@ class LResGPU:
             raise ValueError(f"R_w must be positive (got {R_w})")
         if not (tile_config is None or tile_config == "auto" or tile_config in range(6)):
             raise ValueError(f"tile_config must be None, 'auto' or 0..5 (got {tile_config!r})")
+        if route not in ("auto", "tridiag", "ldl"):
+            raise ValueError(f"route must be 'auto', 'tridiag' or 'ldl' (got {route!r})")
         self.b, self.M, self.margin = basis, M, margin
         self.lag_mu, self.reuse_vectors, self.nthreads = lag_mu, reuse_vectors, nthreads
         self.precision = precision
@@ -213,10 +221,14 @@ class LResGPU:
         _lib.check(_lib.lib.lres_ctx_create(C.byref(ctx), C.byref(d), prec, M, None))
         self._ctx = ctx
         self._keep = (X, S, T, cWflat, cWoff, cOflat, cOoff)   # referenced by the descriptor
+        if route != "auto":
+            self.set_route(route)
         # tile configuration of the pole kernel: an index, or "auto" to time all of them on
         # the first Hamiltonian (see autotune); None keeps the library default
         self.tile_config = tile_config
-        self._tuned = not (tile_config == "auto")
+        # the tile configurations belong to the LDL^T route (and the adjoint, which always
+        # factors by LDL^T): autotuned on the first Hamiltonian only when that route solves
+        self._tuned = not (tile_config == "auto" and self.route == "ldl")
         if isinstance(tile_config, int):
             self.autotune(0.0, -1.0, config=tile_config)
         self._out = np.zeros(3)
@@ -242,6 +254,18 @@ class LResGPU:
             pass
 
     # ------------------------------------------------------------------ GPU calls
+    @property
+    def route(self):
+        """Route of the pole solves: "tridiag" or "ldl"."""
+        r = C.c_int32()
+        _lib.check(_lib.lib.lres_get_route(self._ctx, C.byref(r)))
+        return "tridiag" if r.value == _lib.LRES_ROUTE_TRIDIAG else "ldl"
+
+    def set_route(self, route):
+        """Switch the route of the pole solves ("tridiag" or "ldl")."""
+        code = {"tridiag": _lib.LRES_ROUTE_TRIDIAG, "ldl": _lib.LRES_ROUTE_LDL}[route]
+        _lib.check(_lib.lib.lres_set_route(self._ctx, code, None))
+
     def set_potential(self, v):
         """H(v) for all windows: assembled on the GPU from v, or (for bases with extra
         terms in H) built by basis.H on the host and gathered on the GPU."""
@@ -433,10 +457,12 @@ class LResGPU:
 
     def timings(self):
         """Device milliseconds of the last launches: pole kernel, pole sums, H(v)
-        assembly, window gather, standard-form transform, inertia kernel (-1 = none)."""
-        ms = np.empty(6)
-        _lib.check(_lib.lib.lres_timings(self._ctx, _lib.ptrd(ms), 6))
-        return dict(zip(("pole_kernel", "pole_sums", "assemble_h", "gather", "transform", "inertia"), ms))
+        assembly, window gather, standard-form transform, inertia kernel, tridiagonal
+        reduction, rows through its reflectors (-1 = none)."""
+        ms = np.empty(8)
+        _lib.check(_lib.lib.lres_timings(self._ctx, _lib.ptrd(ms), 8))
+        return dict(zip(("pole_kernel", "pole_sums", "assemble_h", "gather", "transform", "inertia",
+                         "tri_reduce", "tri_rows"), ms))
 
     def window_sums(self):
         nw = np.empty(len(self.ctx_windows))
