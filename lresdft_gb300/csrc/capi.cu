@@ -318,9 +318,15 @@ int window_transform(lres_ctx* c, cudaStream_t s) {
         TRY(batched_gemm_df64(c->nwin, c->d_n, c->d_offC, c->nmax, true, 2, c->d_LinvT_df, c->d_Y_df, nullptr,
                               c->d_Hhat32, s));
     } else {
-        // FP64 (the FP64 tridiagonal route)
-        TRY(batched_gemm(c->nwin, c->d_n, c->d_offC, c->nmax, false, c->d_HW, c->d_LinvT, c->d_Y, s, 1));
-        TRY(batched_gemm(c->nwin, c->d_n, c->d_offC, c->nmax, true, c->d_LinvT, c->d_Y, c->d_Hhat, s, 2));
+        // FP64 (the FP64 tridiagonal route); the product H LinvT lives in the working blocks of
+        // the reduction (at least sizeC elements), which the reduction overwrites afterwards
+        double* Y = static_cast<double*>(c->d_triA);
+        if (!Y || c->sizeA < c->sizeC) {
+            lres_set_error("FP64 standard form without the tridiagonal buffers");
+            return LRES_ESTATE;
+        }
+        TRY(batched_gemm(c->nwin, c->d_n, c->d_offC, c->nmax, false, c->d_HW, c->d_LinvT, Y, s, 1));
+        TRY(batched_gemm(c->nwin, c->d_n, c->d_offC, c->nmax, true, c->d_LinvT, Y, c->d_Hhat, s, 2));
     }
     return LRES_OK;
 }
@@ -374,6 +380,37 @@ int trace_standard_form(lres_ctx* c, cudaStream_t s) {
     return LRES_OK;
 }
 
+// Every window overlap S_W positive definite: all n_w pivots of its LDL^T positive (the
+// factorisation that filled d_npos, one item per window).  The reference's dsygvx reports the
+// same failure as info > n (src/lrft_cpp.cpp:94,110).
+int check_positive_pivots(lres_ctx* c, cudaStream_t s) {
+    std::vector<int> npos(c->nwin);
+    LRES_CUDA_TRY(cudaMemcpyAsync(npos.data(), c->d_npos, sizeof(int) * c->nwin, cudaMemcpyDeviceToHost, s));
+    LRES_CUDA_TRY(cudaStreamSynchronize(s));
+    for (int w = 0; w < c->nwin; ++w)
+        if (npos[w] != c->n_w[w]) {
+            lres_set_error("overlap S_W of window %d is not positive definite (%d of %d pivots positive)", w,
+                           npos[w], c->n_w[w]);
+            return LRES_ENUMERIC;
+        }
+    return LRES_OK;
+}
+
+// Positive definiteness of the current S_W alone (the FP64 LDL^T route has no standard form).
+int check_overlaps(lres_ctx* c, cudaStream_t s) {
+    double* one = nullptr;
+    TRY(dalloc(&one, 1));
+    const double h_one = 1.0;
+    int rc = LRES_OK;
+    cudaError_t e = cudaMemcpyAsync(one, &h_one, sizeof(double), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) rc = LRES_ECUDA;
+    if (!rc) rc = ldl_launch(c, LdlJob::R64, c->nwin, c->d_items_win, nullptr, c->d_SW, nullptr, c->d_m, c->d_offF,
+                             one, nullptr, nullptr, c->nmax, 0, s);
+    if (!rc) rc = check_positive_pivots(c, s);
+    cudaFree(one);
+    return rc;
+}
+
 // Standard form from the current S_W: L_c^-1 (stored as L^-T in FP64; for the mixed path also
 // as double-float pairs) and F^ = L_c^-1 F (FP32 for the mixed path, FP64 for the FP64
 // tridiagonal route).  Allocates on the first call.
@@ -388,7 +425,6 @@ int setup_standard_form(lres_ctx* c, cudaStream_t s) {
             TRY(dalloc(&c->d_Hhat32, c->sizeC));
             TRY(dalloc(&c->d_Fhat32, c->sizeF));
         } else {
-            TRY(dalloc(&c->d_Y, c->sizeC));
             TRY(dalloc(&c->d_Hhat, c->sizeC));
             TRY(dalloc(&c->d_Fhat64, c->sizeF));
         }
@@ -426,7 +462,7 @@ int setup_standard_form(lres_ctx* c, cudaStream_t s) {
         lres_set_error("Cholesky of a window overlap S_W failed (status %d)", st);
         return LRES_ENUMERIC;
     }
-    return LRES_OK;
+    return check_positive_pivots(c, s);
 }
 
 // Work items over the rows of every window, windows in the order of c->order (most
@@ -1461,6 +1497,7 @@ extern "C" int lres_set_windows(lres_ctx* c, const double* HW, const double* SW,
     if (SW) {
         LRES_CUDA_TRY(cudaMemcpyAsync(c->d_SW, SW, sizeof(double) * c->sizeC, kind, s));
         if (needs_standard_form(c)) TRY(setup_standard_form(c, s));
+        else TRY(check_overlaps(c, s));
     }
     if (needs_standard_form(c)) TRY(window_transform(c, s));
     if (c->route == LRES_ROUTE_TRIDIAG) TRY(tri_prepare(c, s));

@@ -73,6 +73,55 @@ def test_single_pass_matches_reference_density(systems, name, hpath):
 
 
 @pytest.mark.parametrize("name", CASES)
+def test_routes_agree(systems, name):
+    """The tridiagonal route (the default) and the LDL^T route evaluate the same resolvent
+    quadratic forms: FP64 densities within 1e-12, band energies within 1e-11, inertia counts
+    equal; mixed precision: both within the 2e-7 Ha/electron gate of the reference, and the
+    mixed density within 1e-6 of FP64 in L2 per electron."""
+    g, cr, b = systems[name]
+    v = g["v"].reshape(cr.shape)
+    mu, e_lo = float(g["cold_mu"]), float(g["cold_elo"])
+    sig = float(g["lam_min"].min()) + 0.05
+    for precision in ("fp64", "mixed"):
+        out = {}
+        for route in ("ldl", "tridiag"):
+            s = _solver(b, cr, g, precision, route=route)
+            assert s.route == route
+            s.set_potential(v)
+            dens, N, eb = s.pole_pass(mu, e_lo)
+            out[route] = (dens, N, eb, s.inertia(sig, per_window=True))
+            s.close()
+        a, t = out["ldl"], out["tridiag"]
+        assert np.array_equal(a[3], t[3])
+        if precision == "fp64":
+            assert np.max(np.abs(a[0] - t[0])) < 1e-12 and abs(a[2] - t[2]) < 1e-11 and abs(a[1] - t[1]) < 1e-11
+        else:
+            for r in (a, t):
+                assert abs(r[2] - g["cold_eband"]) / cr.n_elec < 2e-7
+                assert np.sqrt(np.sum((r[0] - g["cold_dens"]) ** 2) * cr.dV) / cr.n_elec < 1e-6
+
+
+def test_route_switch_keeps_results(systems):
+    """lres_set_route on a context with a Hamiltonian: the tridiagonal form is rebuilt on the
+    switch, and switching back and forth gives the same pass bit for bit."""
+    g, cr, b = systems["cubic3"]
+    mu, e_lo = float(g["cold_mu"]), float(g["cold_elo"])
+    s = _solver(b, cr, g, "fp64", route="ldl")
+    s.set_potential(g["v"].reshape(cr.shape))
+    d0, N0, E0 = s.pole_pass(mu, e_lo)
+    s.set_route("tridiag")
+    d1, N1, E1 = s.pole_pass(mu, e_lo)
+    s.set_route("ldl")
+    d2, N2, E2 = s.pole_pass(mu, e_lo)
+    s.set_route("tridiag")
+    d3, N3, E3 = s.pole_pass(mu, e_lo)
+    assert np.array_equal(d0, d2) and E0 == E2
+    assert np.array_equal(d1, d3) and E1 == E3
+    assert np.max(np.abs(d1 - g["cold_dens"])) < 1e-10
+    s.close()
+
+
+@pytest.mark.parametrize("name", CASES)
 def test_pass_is_bitwise_reproducible(systems, name):
     g, cr, b = systems[name]
     s = _solver(b, cr, g)
@@ -176,13 +225,13 @@ def test_scf_energy_matches_reference(systems, name):
 @pytest.mark.parametrize("name", CASES)
 @pytest.mark.parametrize("config", [0, 1, 2, 3, 4, 5])
 def test_every_tile_configuration_matches_reference(systems, name, config):
-    """Each compiled tile configuration of the pole kernel, forced: FP64 to 1e-10 in
+    """Each compiled tile configuration of the LDL^T pole kernel, forced: FP64 to 1e-10 in
     density, mixed within the 2e-7 Ha/electron gate (configuration 4 of the mixed path runs
     the chunk products on the tensor cores with a 3xTF32 split)."""
     g, cr, b = systems[name]
     v = g["v"].reshape(cr.shape)
     for precision in ("fp64", "mixed"):
-        s = _solver(b, cr, g, precision)
+        s = _solver(b, cr, g, precision, route="ldl")
         s.autotune(0.0, -1.0, config=config)
         s.set_potential(v)
         dens, N, eb = s.pole_pass(float(g["cold_mu"]), float(g["cold_elo"]))
