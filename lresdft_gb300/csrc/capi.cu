@@ -86,6 +86,8 @@ struct lres_ctx {
     double *d_LinvT = nullptr, *d_Y = nullptr, *d_Hhat = nullptr;
     float2 *d_LinvT_df = nullptr, *d_H_df = nullptr, *d_Y_df = nullptr;   // double-float operands
     float *d_Hhat32 = nullptr, *d_Fhat32 = nullptr;
+    float *d_LinvT32 = nullptr, *d_Linv32 = nullptr;   // L^-T and L^-1 in FP32 (mixed tridiagonal route)
+    bool hhat_df = false;                // d_Hhat32 holds the double-float transform of the current H_W
     double *d_Fhat64 = nullptr, *d_FhatT64 = nullptr;   // FP64 standard-form rows (FP64 tridiagonal route)
     long long sizeC = 0, sizeF = 0;
     // multi-shift tridiagonal route (tridiag.cu): T = Q^T H^ Q per window once per Hamiltonian,
@@ -170,7 +172,7 @@ lres_ctx::~lres_ctx() {
                     d_Hhat32, d_Fhat32, d_LinvT_df, d_H_df, d_Y_df, d_items, d_items_win, d_items_sub, d_counter, d_status, d_npos, d_ws, d_shifts,
                     d_wq, d_wzq, d_q, d_dens, d_nw, d_ew, d_v, d_fftwork, d_adjA[0], d_adjA[1], d_adjA[2],
                     d_dHW, d_dSW, d_gH, d_adjdv, d_adju, d_cw, d_order, d_eoff, d_poff, d_ent, d_pent, d_adjws,
-                    d_mT, d_offFT, d_offQT, d_FT, d_FhatT32, d_qT, d_Fhat64, d_FhatT64, d_offN, d_offA, d_order_w,
+                    d_mT, d_offFT, d_offQT, d_FT, d_FhatT32, d_qT, d_Fhat64, d_FhatT64, d_offN, d_offA, d_order_w, d_LinvT32, d_Linv32,
                     d_tstatus, d_triA, d_trid, d_trie, d_tritau, d_Yown, d_Ytr, d_lam};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -307,27 +309,56 @@ __global__ void window_total_kernel(int nwin, const double* nw, const double* ew
     out[1] = E;
 }
 
-int window_transform(lres_ctx* c, cudaStream_t s) {
-    // H^_W = L^-1 H_W L^-T with LinvT = L^-T (upper triangular) stored column-major:
-    // Y = H LinvT (k <= column), then the lower triangle of H^ = LinvT^T Y (k <= row)
-    if (c->precision == LRES_MIXED) {
-        // both in double-float arithmetic on the FP32 pipes, H^ rounded to FP32 at the end
-        TRY(split_f64(c->d_HW, c->d_H_df, c->sizeC, s));
-        TRY(batched_gemm_df64(c->nwin, c->d_n, c->d_offC, c->nmax, false, 1, c->d_H_df, c->d_LinvT_df, c->d_Y_df,
-                              nullptr, s));
-        TRY(batched_gemm_df64(c->nwin, c->d_n, c->d_offC, c->nmax, true, 2, c->d_LinvT_df, c->d_Y_df, nullptr,
-                              c->d_Hhat32, s));
-    } else {
-        // FP64 (the FP64 tridiagonal route); the product H LinvT lives in the working blocks of
-        // the reduction (at least sizeC elements), which the reduction overwrites afterwards
-        double* Y = static_cast<double*>(c->d_triA);
-        if (!Y || c->sizeA < c->sizeC) {
-            lres_set_error("FP64 standard form without the tridiagonal buffers");
-            return LRES_ESTATE;
-        }
-        TRY(batched_gemm(c->nwin, c->d_n, c->d_offC, c->nmax, false, c->d_HW, c->d_LinvT, Y, s, 1));
-        TRY(batched_gemm(c->nwin, c->d_n, c->d_offC, c->nmax, true, c->d_LinvT, Y, c->d_Hhat, s, 2));
+// H^_W = L^-1 H_W L^-T with LinvT = L^-T (upper triangular) stored column-major:
+// Y = H LinvT (k <= column), then the lower triangle of H^ = LinvT^T Y (k <= row).
+
+// Double-float arithmetic on the FP32 pipes, H^ rounded to FP32 at the end (the mixed LDL^T
+// route and the mixed adjoint, whose FP32 factorisations are more accurate than FP32 input).
+int transform_df64(lres_ctx* c, cudaStream_t s) {
+    TRY(split_f64(c->d_HW, c->d_H_df, c->sizeC, s));
+    TRY(batched_gemm_df64(c->nwin, c->d_n, c->d_offC, c->nmax, false, 1, c->d_H_df, c->d_LinvT_df, c->d_Y_df,
+                          nullptr, s));
+    TRY(batched_gemm_df64(c->nwin, c->d_n, c->d_offC, c->nmax, true, 2, c->d_LinvT_df, c->d_Y_df, nullptr,
+                          c->d_Hhat32, s));
+    c->hhat_df = true;
+    return LRES_OK;
+}
+
+// Standard form of the mixed tridiagonal route: FP32 with blocked sums (measured as accurate
+// as the double-float form there, whose FP32 Householder reduction sets the error).  Both
+// products live in the double-float scratch: Y in its first sizeC floats, H^ in the next.
+float* tri_hhat32(lres_ctx* c) { return reinterpret_cast<float*>(c->d_Y_df) + c->sizeC; }
+
+int transform_f32(lres_ctx* c, cudaStream_t s) {
+    float* Y = reinterpret_cast<float*>(c->d_Y_df);
+    TRY(batched_gemm_f32(c->nwin, c->d_n, c->d_offC, c->nmax, 1, c->d_HW, true, c->d_LinvT32, Y, s));
+    TRY(batched_gemm_f32(c->nwin, c->d_n, c->d_offC, c->nmax, 2, c->d_Linv32, false, Y, tri_hhat32(c), s));
+    c->hhat_df = false;                  // d_Hhat32 no longer follows H_W
+    return LRES_OK;
+}
+
+// FP64 (the FP64 tridiagonal route); the product H LinvT lives in the working blocks of the
+// reduction (at least sizeC elements), which the reduction overwrites afterwards.
+int transform_fp64(lres_ctx* c, cudaStream_t s) {
+    double* Y = static_cast<double*>(c->d_triA);
+    if (!Y || c->sizeA < c->sizeC) {
+        lres_set_error("FP64 standard form without the tridiagonal buffers");
+        return LRES_ESTATE;
     }
+    TRY(batched_gemm(c->nwin, c->d_n, c->d_offC, c->nmax, false, c->d_HW, c->d_LinvT, Y, s, 1));
+    TRY(batched_gemm(c->nwin, c->d_n, c->d_offC, c->nmax, true, c->d_LinvT, Y, c->d_Hhat, s, 2));
+    return LRES_OK;
+}
+
+int window_transform(lres_ctx* c, cudaStream_t s) {
+    if (c->precision == LRES_MIXED)
+        return c->route == LRES_ROUTE_TRIDIAG ? transform_f32(c, s) : transform_df64(c, s);
+    return transform_fp64(c, s);
+}
+
+// The double-float standard form for the LDL^T consumers (passes on that route, the adjoint).
+int ensure_hhat_df(lres_ctx* c, cudaStream_t s) {
+    if (c->precision == LRES_MIXED && !c->hhat_df) return transform_df64(c, s);
     return LRES_OK;
 }
 
@@ -424,6 +455,8 @@ int setup_standard_form(lres_ctx* c, cudaStream_t s) {
             TRY(dalloc(&c->d_Y_df, c->sizeC));
             TRY(dalloc(&c->d_Hhat32, c->sizeC));
             TRY(dalloc(&c->d_Fhat32, c->sizeF));
+            TRY(dalloc(&c->d_LinvT32, c->sizeC));
+            TRY(dalloc(&c->d_Linv32, c->sizeC));
         } else {
             TRY(dalloc(&c->d_Hhat, c->sizeC));
             TRY(dalloc(&c->d_Fhat64, c->sizeF));
@@ -452,6 +485,9 @@ int setup_standard_form(lres_ctx* c, cudaStream_t s) {
     if (!rc && mixed) rc = convert_f64_f32(Fhat, c->d_Fhat32, c->sizeF, s);
     if (!rc && c->have_trace) rc = trace_standard_form(c, s);
     if (!rc && mixed) rc = split_f64(c->d_LinvT, c->d_LinvT_df, c->sizeC, s);
+    if (!rc && mixed) rc = convert_f64_f32(c->d_LinvT, c->d_LinvT32, c->sizeC, s);
+    if (!rc && mixed) rc = batched_transpose_f32(c->nwin, c->d_n, c->d_offC, c->nmax, c->d_LinvT32, c->d_Linv32, s);
+    c->hhat_df = false;                  // the standard form changed
     int st = 0;
     if (!rc) rc = read_status(c, s, &st);
     cudaFree(I);
@@ -533,7 +569,7 @@ int tri_prepare(lres_ctx* c, cudaStream_t s) {
     LRES_CUDA_TRY(cudaMemsetAsync(c->d_tstatus, 0, sizeof(int), s));
     TRY(mark(c, 6, 0, s));
     TRY(tri_reduce(fp32, c->nwin, c->d_order_w, c->d_counter, c->d_n, c->d_offC, c->d_offA, c->d_offN,
-                   fp32 ? (const void*)c->d_Hhat32 : (const void*)c->d_Hhat, c->d_triA, c->d_trid, c->d_trie,
+                   fp32 ? (const void*)tri_hhat32(c) : (const void*)c->d_Hhat, c->d_triA, c->d_trid, c->d_trie,
                    c->d_tritau, c->d_tstatus, c->tri_nb, c->tri_ldv, c->smem_budget, s));
     TRY(mark(c, 6, 1, s));
     TRY(mark(c, 7, 0, s));
@@ -542,6 +578,13 @@ int tri_prepare(lres_ctx* c, cudaStream_t s) {
     TRY(mark(c, 7, 1, s));
     c->tri_ready = true;
     return LRES_OK;
+}
+
+// Standard form and tridiagonal form of the current H_W (when the route was switched after it
+// was set).
+int tri_refresh(lres_ctx* c, cudaStream_t s) {
+    TRY(window_transform(c, s));
+    return tri_prepare(c, s);
 }
 
 // The pole pass of the tridiagonal route over one row set (nodes and weights already set):
@@ -1065,10 +1108,11 @@ extern "C" int lres_pass(lres_ctx* c, double mu, double e_lo, double* dens, int 
     // no density requested and trace rows installed: the pass over the trace rows
     const bool trace = !dens && c->have_trace;
     if (c->route == LRES_ROUTE_TRIDIAG) {
-        if (!c->tri_ready) TRY(tri_prepare(c, s));
+        if (!c->tri_ready) TRY(tri_refresh(c, s));
         TRY(tri_run_pass(c, trace, s));
     } else {
         const Rows rw = select_rows(c, trace);
+        TRY(ensure_hhat_df(c, s));
         TRY(mark(c, 0, 0, s));
         if (mixed)
             TRY(ldl_launch(c, LdlJob::C64, c->nitems, c->d_items, c->d_Hhat32, nullptr, rw.F, rw.m, rw.offF,
@@ -1176,7 +1220,7 @@ extern "C" int lres_set_route(lres_ctx* c, int32_t route, void* stream) {
     if (c->precision != LRES_MIXED && !c->d_LinvT) rc = setup_standard_form(c, s);
     if (!rc) rc = tri_setup(c, s);
     if (!rc && c->have_h) {
-        if (c->precision != LRES_MIXED) rc = window_transform(c, s);   // H^ (FP64) of the current H
+        rc = window_transform(c, s);           // the route's standard form of the current H
         if (!rc) rc = tri_prepare(c, s);
     }
     if (rc) {
@@ -1234,9 +1278,10 @@ extern "C" int lres_pass_async(lres_ctx* c, double mu, double e_lo, double* d_ou
     LRES_CUDA_TRY(cudaGetLastError());
     LRES_CUDA_TRY(cudaMemsetAsync(c->d_status, 0, sizeof(int), s));
     if (c->route == LRES_ROUTE_TRIDIAG) {
-        if (!c->tri_ready) TRY(tri_prepare(c, s));
+        if (!c->tri_ready) TRY(tri_refresh(c, s));
         TRY(tri_run_pass(c, false, s));
     } else {
+        TRY(ensure_hhat_df(c, s));
         if (mixed)
             TRY(ldl_launch(c, LdlJob::C64, c->nitems, c->d_items, c->d_Hhat32, nullptr, c->d_Fhat32, c->d_m,
                            c->d_offF, c->d_shifts, c->d_q, nullptr, c->nmax + c->mmax, c->mmax, s));
@@ -1293,7 +1338,7 @@ extern "C" int lres_inertia(lres_ctx* c, double sigma, int32_t* below, int64_t* 
     cudaStream_t s = (cudaStream_t)stream;
     if (c->route == LRES_ROUTE_TRIDIAG) {
         // Sturm counts of T - sigma: T is congruent to the pencil (H_W, S_W)
-        if (!c->tri_ready) TRY(tri_prepare(c, s));
+        if (!c->tri_ready) TRY(tri_refresh(c, s));
         TRY(mark(c, 5, 0, s));
         TRY(tri_sturm(c->precision == LRES_MIXED, c->nwin, c->d_n, c->d_offN, c->d_trid, c->d_trie, sigma,
                       c->d_npos, s));
@@ -1347,7 +1392,7 @@ extern "C" int lres_min_eig(lres_ctx* c, double lo, double hi, double tol, doubl
     cudaStream_t s = (cudaStream_t)stream;
     if (c->route == LRES_ROUTE_TRIDIAG) {
         // every window's smallest eigenvalue by Sturm bisection on T, to width tol
-        if (!c->tri_ready) TRY(tri_prepare(c, s));
+        if (!c->tri_ready) TRY(tri_refresh(c, s));
         TRY(tri_min_eig(c->precision == LRES_MIXED, c->nwin, c->d_n, c->d_offN, c->d_trid, c->d_trie, tol,
                         c->d_lam, s));
         std::vector<double> lam(c->nwin);
@@ -1592,6 +1637,7 @@ extern "C" int lres_adjoint(lres_ctx* c, double mu, double e_lo, double* dv, int
         return LRES_EINVAL;
     }
     cudaStream_t s = (cudaStream_t)stream;
+    TRY(ensure_hhat_df(c, s));                 // the adjoint factors the double-float standard form
     TRY(adj_prepare(c, s));
     const bool mixed = c->precision == LRES_MIXED;
     const int P = c->npoles;

@@ -635,6 +635,126 @@ __global__ void __launch_bounds__(256) gemm_df64_kernel(const int* n_w, const lo
         }
 }
 
+// ---------------------------------------------------------------------------
+// batched FP32 GEMM with blocked sums  C_w = A_w B_w  (n_w x n_w, column-major, offsets off)
+// ---------------------------------------------------------------------------
+// KLIM as gemm_f64_kernel (1: B upper triangular, k <= column; 2: A lower triangular, k <= row,
+// lower triangle of C only).  A is FP64 (converted on load) or FP32, B and C FP32.  Each
+// 32-term block of the k sum is formed from zero and added to the running value, so the
+// rounding grows with the number of blocks rather than the number of terms.  64 x 64 tiles,
+// 4 x 4 outputs per thread; A staged k-major (16-byte reads of 4 rows), B column-major with a
+// padded row so that both the staging stores and the reads are free of bank conflicts.
+template <int KLIM, bool AF64>
+__global__ void __launch_bounds__(256) gemm_f32blk_kernel(const int* n_w, const long long* off, const void* Av,
+                                                          const float* B, float* C) {
+    constexpr int BM = 64, BN = 64, BK = 32;
+    const int w = blockIdx.z;
+    const int n = n_w[w];
+    const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+    if (m0 >= n || n0 >= n) return;
+    if (KLIM == 2 && m0 + BM - 1 < n0) return;
+    const int kend = KLIM == 1 ? min(n, n0 + BN) : KLIM == 2 ? min(n, m0 + BM) : n;
+    const double* A64 = AF64 ? static_cast<const double*>(Av) + off[w] : nullptr;
+    const float* A32 = AF64 ? nullptr : static_cast<const float*>(Av) + off[w];
+    const float* Bw = B + off[w];
+    __shared__ __align__(16) float As[BK][BM];
+    __shared__ float Bs[BN][BK + 1];
+    const int tid = threadIdx.x;
+    const int tx = tid % 16, ty = tid / 16;
+    float acc[4][4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = 0.f;
+    for (int k0 = 0; k0 < kend; k0 += BK) {
+        for (int idx = tid; idx < BK * BM; idx += 256) {
+            const int kk = idx / BM, i = idx % BM;
+            const int gi = m0 + i, gk = k0 + kk;
+            float a = 0.f;
+            if (gi < n && gk < n) a = AF64 ? (float)A64[gi + (long long)gk * n] : A32[gi + (long long)gk * n];
+            As[kk][i] = a;
+        }
+        for (int idx = tid; idx < BK * BN; idx += 256) {
+            const int j = idx / BK, kk = idx % BK;
+            const int gj = n0 + j, gk = k0 + kk;
+            Bs[j][kk] = (gj < n && gk < n) ? Bw[gk + (long long)gj * n] : 0.f;
+        }
+        __syncthreads();
+        float blk[4][4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) blk[u][v] = 0.f;
+#pragma unroll 8
+        for (int kk = 0; kk < BK; ++kk) {
+            const float4 a = *reinterpret_cast<const float4*>(&As[kk][4 * tx]);
+            const float av[4] = {a.x, a.y, a.z, a.w};
+            float bv[4];
+#pragma unroll
+            for (int v = 0; v < 4; ++v) bv[v] = Bs[4 * ty + v][kk];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) blk[u][v] = fmaf(av[u], bv[v], blk[u][v]);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) acc[u][v] += blk[u][v];
+        __syncthreads();
+    }
+    float* Cw = C + off[w];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const int gi = m0 + 4 * tx + u, gj = n0 + 4 * ty + v;
+            if (gi < n && gj < n) Cw[gi + (long long)gj * n] = acc[u][v];
+        }
+}
+
+int batched_gemm_f32(int nwin, const int* n_w, const long long* off, int nmax, int klim, const void* A, bool a_f64,
+                     const float* B, float* C, cudaStream_t s) {
+    if (!nwin) return LRES_OK;
+    dim3 grid((nmax + 63) / 64, (nmax + 63) / 64, nwin);
+    if (klim == 1 && a_f64) gemm_f32blk_kernel<1, true><<<grid, 256, 0, s>>>(n_w, off, A, B, C);
+    else if (klim == 2 && !a_f64) gemm_f32blk_kernel<2, false><<<grid, 256, 0, s>>>(n_w, off, A, B, C);
+    else {
+        lres_set_error("unsupported FP32 GEMM variant");
+        return LRES_EINVAL;
+    }
+    LRES_CUDA_TRY(cudaGetLastError());
+    return LRES_OK;
+}
+
+// B_w = A_w^T for every window block (FP32, one 32 x 32 tile per CTA through shared memory).
+__global__ void transpose_f32_kernel(const int* n_w, const long long* off, const float* A, float* B) {
+    __shared__ float t[32][33];
+    const int w = blockIdx.z, n = n_w[w];
+    const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
+    if (i0 >= n || j0 >= n) return;
+    const float* Aw = A + off[w];
+    float* Bw = B + off[w];
+    for (int c = threadIdx.y; c < 32; c += blockDim.y) {
+        const int i = i0 + threadIdx.x, j = j0 + c;
+        t[c][threadIdx.x] = (i < n && j < n) ? Aw[i + (long long)j * n] : 0.f;
+    }
+    __syncthreads();
+    for (int c = threadIdx.y; c < 32; c += blockDim.y) {
+        const int j = j0 + threadIdx.x, i = i0 + c;     // B[j, i] = A[i, j]
+        if (i < n && j < n) Bw[j + (long long)i * n] = t[threadIdx.x][c];
+    }
+}
+
+int batched_transpose_f32(int nwin, const int* n_w, const long long* off, int nmax, const float* A, float* B,
+                          cudaStream_t s) {
+    if (!nwin) return LRES_OK;
+    dim3 grid((nmax + 31) / 32, (nmax + 31) / 32, nwin);
+    transpose_f32_kernel<<<grid, dim3(32, 8), 0, s>>>(n_w, off, A, B);
+    LRES_CUDA_TRY(cudaGetLastError());
+    return LRES_OK;
+}
+
 int batched_gemm_df64(int nwin, const int* n_w, const long long* off, int nmax, bool transA, int klim,
                       const float2* A, const float2* B, float2* C, float* C32, cudaStream_t s) {
     if (!nwin) return LRES_OK;

@@ -99,6 +99,10 @@ int convert_f64_f32(const double* a, float* b, long long n, cudaStream_t s);
 int split_f64(const double* a, float2* b, long long n, cudaStream_t s);
 int batched_gemm_df64(int nwin, const int* n_w, const long long* off, int nmax, bool transA, int klim,
                       const float2* A, const float2* B, float2* C, float* C32, cudaStream_t s);
+int batched_gemm_f32(int nwin, const int* n_w, const long long* off, int nmax, int klim, const void* A, bool a_f64,
+                     const float* B, float* C, cudaStream_t s);
+int batched_transpose_f32(int nwin, const int* n_w, const long long* off, int nmax, const float* A, float* B,
+                          cudaStream_t s);
 int pole_sums(int nwin, const long long* offQ, const int* m_w, const long long* Oflat, bool fp32,
               const void* q, long long qstride, int npoles, const double2* wq, const double2* wzq, double dV,
               double* dens, double* n_w, double* e_w, cudaStream_t s);
