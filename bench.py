@@ -8,16 +8,18 @@ Gaussian basis (6144 functions), one window per atom with R_w = 8 bohr (1024 win
 n_W 264-312), M = 64 poles (32 upper-half-plane solves per window).  Inputs are
 synthetic (seeded geometry; potential = that of the uniform starting density).
 
-One step = one density evaluation at fixed (mu, e_lo): H(v) assembly by atom pairs,
-gather of the 1024 dense window blocks, the standard-form transform (mixed), the
-fused pole kernel over all 1024 x 32 window-pole items, and the pole sums to
-density / electron count / band energy.  Metric: window-pole solves per second
-(1024 * 32 per step).  `value` is measured with the potential resident on the GPU and
-the density left there; `e2e` goes through the public drop-in API with a host
-potential in and a host density out every step.  Inputs (window blocks ~0.6 GB) are
-larger than L2, so no L2 flush is needed between steps.
+One step = one density evaluation at fixed (mu, e_lo) from the potential: H(v) assembly by
+atom pairs, gather of the 1024 dense window blocks, the standard-form transform, and then on
+the default tridiagonal route the Householder reduction of every window, the owned rows
+through its reflectors and the fused shifted-solve + pole-sum kernel over all 1024 x 32
+window-pole pairs (on the LDL^T route: one fused LDL^T per window-pole item and the pole
+sums).  Metric: window-pole solves per second (1024 * 32 per step).  `value` is measured
+with the potential resident on the GPU and the density left there; `e2e` goes through the
+public drop-in API with a host potential in and a host density out every step.  Inputs
+(window blocks ~0.7 GB) are larger than L2, so no L2 flush is needed between steps.
 
-    python bench.py [--steps K] [--warmup W] [--precision mixed|fp64] [--impl ours|reference]
+    python bench.py [--steps K] [--warmup W] [--precision mixed|fp64] [--route auto|tridiag|ldl]
+                    [--impl ours|reference]
 """
 from __future__ import annotations
 
@@ -36,7 +38,8 @@ sys.path.insert(0, ROOT)
 
 WORKLOAD = dict(workload="8x8x8 H2 crystal, 1024 electrons, a=4.5, jitter U(+-0.1), R_w=8, M=64, 64^3 grid",
                 natoms=1024, nwin=1024, poles_per_window=32, M=64, R_w=8.0, basis_functions=6144,
-                grid="64^3", l2="inputs larger than L2 (no flush)")
+                grid="64^3", l2="inputs larger than L2 (no flush)", parallelism="single GPU")
+SCF_ITERS = 4           # the fixed SCF window of the GPU and CPU s/iter figures
 
 
 def build_system(cells=8, assembly="native"):
@@ -88,6 +91,56 @@ class Clocks:
 def algorithmic_flops(nW, npoles):
     """(32/3) n^3 real flops per window-pole solve (complex LU + full inverse), fixed."""
     return float(npoles * (32.0 / 3.0) * np.sum(np.asarray(nW, float) ** 3))
+
+
+def kernel_work(name, nW, mW, P, nnz_h):
+    """Algorithmic work of one launch (per step) of each kernel, with the roofline that bounds
+    it: ("flop", F) for compute kernels, ("byte", B) for bandwidth kernels."""
+    n = np.asarray(nW, float)
+    m = np.asarray(mW, float)
+    if name == "tri_reduce":          # Householder tridiagonalisation: (4/3) n^3 per window
+        return "flop", float(np.sum(4.0 / 3.0 * n ** 3))
+    if name == "tri_rows":            # Y = F^ Q: 2 m n^2 per window
+        return "flop", float(np.sum(2.0 * m * n ** 2))
+    if name == "transform":           # L^-1 H L^-T: n^3/2 + n^3/6 multiply-adds per window
+        return "flop", float(np.sum(4.0 / 3.0 * n ** 3))
+    if name == "pole_kernel_tri":     # per (pole, row, step): complex multiply-add + u^2/D (20 flops)
+        return "flop", float(P * np.sum(20.0 * m * n))
+    if name == "pole_kernel_ldl":     # the fixed unit: (32/3) n^3 per window-pole solve
+        return "flop", algorithmic_flops(nW, P)
+    if name == "assemble_h":          # read the common-point slots, v and basis values, write H
+        return "byte", float(nnz_h * 8 * 2 + 0.3e9)
+    if name == "gather":              # window blocks written (FP64) and the atom-pair blocks read
+        return "byte", float(np.sum(n ** 2) * 8 * 2)
+    return None, None
+
+
+def roofline_of(name, ms, nW, mW, P, nnz_h, peaks):
+    kind, work = kernel_work(name, nW, mW, P, nnz_h)
+    if kind is None:
+        return None
+    if kind == "flop":
+        achieved = work / (ms / 1e3) / 1e12
+        peak = peaks.get("bf16_tflops_sustained") if peaks else 1700.0
+        return {"bound": "tensor", "achieved": round(achieved, 3), "peak": peak, "unit": "TFLOP/s",
+                "frac": round(achieved / peak, 5), "traffic": None, "kernel_ms": round(ms, 3),
+                "algorithmic_flop_per_launch": work,
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (of measured)" if peaks else "fallback"}
+    achieved = work / (ms / 1e3) / 1e9
+    peak = peaks.get("hbm_gbs") if peaks else 6800.0
+    return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 5), "traffic": None, "kernel_ms": round(ms, 3),
+            "algorithmic_bytes_per_launch": work,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback"}
+
+
+def launches_per_step(route, precision):
+    """Our kernels in one step (H(v) + window blocks + standard form + pass)."""
+    if route == "tridiag":
+        # assemble_h, gather, 2 standard-form GEMMs, reduction, rows, pole nodes, pass, window sums
+        return 9
+    # assemble_h, gather, [split + 2 double-float GEMMs], pole nodes, LDL^T kernel, pole sums
+    return 8 if precision == "mixed" else 5
 
 
 def cpu_leg(b, v, s, mu, e_lo, workers=None):
@@ -166,8 +219,11 @@ def run_ours(args):
     if args.cells != 8:
         WORKLOAD.update(workload=f"{args.cells}^3 H2 crystal (profiling size), {cr.n_elec} electrons",
                         natoms=len(cr.pos), nwin=len(cr.pos), basis_functions=6 * len(cr.pos), grid=f"{cr.shape[0]}^3")
-    s = LResGPU(b, cr.pos, R_w=8.0, M=64, precision=args.precision,
+    if world > 1:
+        WORKLOAD.update(parallelism=f"{world} replicas")
+    s = LResGPU(b, cr.pos, R_w=8.0, M=64, precision=args.precision, route=args.route,
                 tile_config="auto" if args.tile_config is None else args.tile_config)
+    route = s.route
     go = GridOps(s)
     vion = go.ion_potential()
     d0 = np.full(cr.shape, cr.n_elec / (cr.ng * cr.dV))
@@ -188,12 +244,11 @@ def run_ours(args):
 
     dev = torch.device("cuda", local)
     v_dev = torch.from_numpy(np.ascontiguousarray(v.ravel())).to(dev)
-    nW = s.nW
+    nW = s.ctx_nW
+    mW = np.array([len(o) for o in s.ctx_own])
     P = s.M // 2
-    units = len(nW) * P
-    # kernels per step: H(v) assembly, window gather, [split + 2 double-float GEMMs], pole nodes,
-    # pole kernel, pole sums
-    launches_per_step = 8 if args.precision == "mixed" else 5
+    units = len(s.nW) * P
+    lps = launches_per_step(route, args.precision)
 
     def step():
         s.set_potential_device(v_dev.data_ptr())
@@ -202,7 +257,8 @@ def run_ours(args):
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
-    kern_ms, assemble_ms, gather_ms, transform_ms, sums_ms = [], [], [], [], []
+    names = ("pole_kernel", "pole_sums", "assemble_h", "gather", "transform", "tri_reduce", "tri_rows")
+    per = {k: [] for k in names}
     clocks = Clocks()
     if dist:
         dist.barrier()
@@ -213,11 +269,8 @@ def run_ours(args):
     for _ in range(args.steps):
         step()
         t = s.timings()
-        kern_ms.append(t["pole_kernel"])
-        sums_ms.append(t["pole_sums"])
-        assemble_ms.append(t["assemble_h"])
-        gather_ms.append(t["gather"])
-        transform_ms.append(t["transform"])
+        for k in names:
+            per[k].append(t[k])
     e1.record()
     torch.cuda.synchronize()
     clk = clocks.stop()
@@ -228,6 +281,7 @@ def run_ours(args):
         ms_total = float(tt.item())
     ms_step = ms_total / args.steps
     value = units * world / (ms_step / 1e3)
+    breakdown = {k: round(float(np.mean(x)), 3) for k, x in per.items() if np.mean(x) >= 0}
 
     # e2e through the drop-in API: host potential in, host density out, every step
     for _ in range(max(1, args.warmup // 2)):
@@ -242,6 +296,14 @@ def run_ours(args):
     e2e_ms = (time.perf_counter() - t) * 1e3 / args.steps
     h2d = cr.ng * 8 + 3 * 16 * P
     d2h = cr.ng * 8 + 2 * 8 * len(nW) + 4
+
+    # one more mu trial on the same Hamiltonian (what each extra pass of a density call costs)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for k in range(args.steps):
+        s.pole_pass_device(mu + 1e-4 * (k % 3), e_lo)
+    torch.cuda.synchronize()
+    pass_ms = (time.perf_counter() - t) * 1e3 / args.steps
 
     # the same step as one CUDA graph (H(v) from device v + capturable pass, N and E_band
     # left on the device): replayed K times, timed on the replay stream
@@ -271,58 +333,70 @@ def run_ours(args):
         torch.cuda.synchronize()
         g_ms = g0.elapsed_time(g1) / args.steps
         gN = float(out_dev[0].item())
-        if s.status() != 0 or abs(gN - cr.n_elec) > 1e-4:
+        if s.status() != 0 or abs(gN - cr.n_elec) > 1e-3:
             raise RuntimeError(f"graph replay gave N={gN}, status {s.status()}")
         graph_leg = {"value": round(units / (g_ms / 1e3), 1), "unit": "window-pole solves/s",
-                     "ms_per_step": round(g_ms, 3), "launches_per_step": launches_per_step + 1}
+                     "ms_per_step": round(g_ms, 3), "launches_per_step": lps + 1}
         del graph
     except Exception as exc:          # reported, never silently replaced
         graph_leg = {"error": str(exc)[:200]}
 
-    # roofline of the dominant kernel (the fused pole kernel)
+    # roofline of the dominant kernel of the step (largest device time), with its own
+    # algorithmic work; the fixed (32/3) n^3 unit of the whole step beside it
     peaks = read_peaks()
-    kern = float(np.mean(kern_ms))
-    flops = algorithmic_flops(nW, P)
-    achieved = flops / (kern / 1e3) / 1e12
-    peak = peaks.get("bf16_tflops_sustained") if peaks else 1700.0
-    roof = {"bound": "tensor", "achieved": round(achieved, 3), "peak": peak, "unit": "TFLOP/s",
-            "frac": round(achieved / peak, 5), "traffic": None,
-            "kernel": {4: "ldl_left_tc_kernel", 5: "ldl_left_bulk_kernel"}.get(s.tile_config, "ldl_left_kernel")
-                      + " (fused complex LDL^T + owned-point quadratic forms)",
-            "algorithmic": "(32/3) n_W^3 real flops per window-pole solve",
-            "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (of measured)" if peaks else "fallback",
-            "kernel_ms": round(kern, 3)}
+    nnz_h = float(b.S.nnz)
+    cand = {k: breakdown[k] for k in ("pole_kernel", "transform", "tri_reduce", "tri_rows", "assemble_h", "gather")
+            if k in breakdown}
+    kernel_names = {"pole_kernel": "tri_pass_kernel" if route == "tridiag" else "ldl_left_kernel",
+                    "transform": "gemm_f32blk_kernel" if (route == "tridiag" and args.precision == "mixed")
+                    else ("gemm_f64_kernel" if args.precision == "fp64" else "gemm_df64_kernel"),
+                    "tri_reduce": "tri_reduce_kernel", "tri_rows": "tri_apply_kernel",
+                    "assemble_h": "assemble_h_kernel", "gather": "gather_windows_kernel"}
+
+    def work_name(k):
+        return {"pole_kernel": "pole_kernel_tri" if route == "tridiag" else "pole_kernel_ldl"}.get(k, k)
+    dom = max(cand, key=cand.get)
+    roof = roofline_of(work_name(dom), cand[dom], nW, mW, P, nnz_h, peaks)
+    roof["kernel"] = kernel_names[dom]
     try:
         tr = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
-        roof["traffic"] = tr.get(args.precision)
+        roof["traffic"] = tr.get(f"{args.precision}/{route}/{roof['kernel']}")
     except Exception:
         pass
+    others = {}
+    for k in cand:
+        if k != dom:
+            r = roofline_of(work_name(k), cand[k], nW, mW, P, nnz_h, peaks)
+            if r:
+                others[kernel_names[k]] = {x: r[x] for x in ("bound", "achieved", "unit", "frac", "kernel_ms")}
+    flops_step = algorithmic_flops(nW, P)
 
     line = {
         "metric": "window-pole solves/s", "value": round(value, 1), "unit": "window-pole solves/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "c64 (FP64 set-up/sums)" if args.precision == "mixed" else "c128",
+        "dtype": "c64 (FP32 reduction, FP64 sums)" if args.precision == "mixed" else "c128",
+        "precision": args.precision, "route": route,
         "data": "synthetic (seeded H2 crystal, potential of the uniform starting density)",
-        "config": dict(WORKLOAD, precision=args.precision, parallelism="replicas" if world > 1 else "single GPU"),
+        "config": dict(WORKLOAD),
         "e2e": {"value": round(units / (e2e_ms / 1e3), 1), "unit": "window-pole solves/s",
                 "ms_per_step": round(e2e_ms, 3), "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-        "gpu_launches": launches_per_step * args.steps,
+        "gpu_launches": lps * args.steps,
         "roofline": roof,
+        "roofline_other_kernels": others,
+        "equivalent_work": {"unit": "(32/3) n_W^3 real flops per window-pole solve (fixed)",
+                            "flop_per_step": flops_step,
+                            "tflops_per_s": round(flops_step / (ms_step / 1e3) / 1e12, 2)},
         "clocks": clk,
-        "breakdown_ms": {"pole_kernel": round(kern, 3), "pole_sums": round(float(np.mean(sums_ms)), 3),
-                         "assemble_h": round(float(np.mean(assemble_ms)), 3),
-                         "gather": round(float(np.mean(gather_ms)), 3),
-                         "transform": round(float(np.mean(transform_ms)), 3)},
+        "breakdown_ms": breakdown,
+        "extra_pass_ms": round(pass_ms, 3),
         "cuda_graph": graph_leg,
         "setup_s": round(setup_s, 2), "basis_s": round(basis_s, 2), "accuracy": err,
-        "tile_config": {"chosen": s.tile_config,
-                        "pole_kernel_ms_per_config": [round(float(x), 2) for x in getattr(s, "tune_ms", [])]},
     }
 
     # FP64 path on the same potential (the target ratio is mixed vs FP64)
     if args.precision == "mixed" and args.fp64_steps > 0:
-        s64 = LResGPU(b, cr.pos, R_w=8.0, M=64, precision="fp64", tile_config=3)
+        s64 = LResGPU(b, cr.pos, R_w=8.0, M=64, precision="fp64", route=args.route, tile_config=3)
         s64.set_potential_device(v_dev.data_ptr())
         s64.pole_pass_device(mu, e_lo)
         torch.cuda.synchronize()
@@ -334,24 +408,31 @@ def run_ours(args):
         a1.record()
         torch.cuda.synchronize()
         ms64 = a0.elapsed_time(a1) / args.fp64_steps
+        t64 = s64.timings()
         _, N32, E32 = s.pole_pass(mu, e_lo)
-        line["fp64"] = {"value": round(units / (ms64 / 1e3), 1), "ms_per_step": round(ms64, 2),
+        line["fp64"] = {"route": s64.route, "value": round(units / (ms64 / 1e3), 1), "ms_per_step": round(ms64, 2),
                         "mixed_speedup": round(ms64 / ms_step, 2),
+                        "breakdown_ms": {k: round(float(t64[k]), 3) for k in names if t64[k] >= 0},
                         "mixed_eband_err_per_e": abs(E32 - E64) / cr.n_elec,
                         "mixed_count_err": abs(N32 - N64)}
-        # the tensor-core configuration (tcgen05, 3xTF32) on the same pass, against FP64
-        try:
-            s.autotune(mu, e_lo, config=4)
-            s.pole_pass(mu, e_lo)
-            _, Ntc, Etc = s.pole_pass(mu, e_lo)
-            line["tensor_core"] = {"tile_config": 4, "kernel_ms": round(s.timings()["pole_kernel"], 2),
-                                   "eband_err_per_e_vs_fp64": abs(Etc - E64) / cr.n_elec,
-                                   "count_err_vs_fp64": abs(Ntc - N64),
-                                   "note": "tcgen05.mma kind::tf32, 3xTF32 split; forced only (not auto-selected)"}
-        except Exception as exc:
-            line["tensor_core"] = {"error": str(exc)[:200]}
-        finally:
-            s.autotune(mu, e_lo, config=s.tile_config if isinstance(s.tile_config, int) else 1)
+        # the LDL^T route on the same potential (SIMT tile configuration 1 and the tensor-core
+        # configuration 4), for comparison with the default route
+        if route == "tridiag" and args.ldl_leg:
+            ldl = {}
+            try:
+                s.set_route("ldl")
+                for cfg in (1, 4):
+                    s.autotune(mu, e_lo, config=cfg)
+                    s.pole_pass(mu, e_lo)
+                    _, Nl, El = s.pole_pass(mu, e_lo)
+                    ldl[f"config{cfg}"] = {"pole_kernel_ms": round(s.timings()["pole_kernel"], 2),
+                                           "eband_err_per_e_vs_fp64": abs(El - E64) / cr.n_elec}
+                ldl["note"] = "LDL^T route (one fused factorisation per window-pole item); config4 = tcgen05 3xTF32"
+            except Exception as exc:
+                ldl["error"] = str(exc)[:200]
+            finally:
+                s.set_route("tridiag")
+            line["ldl_route"] = ldl
         if args.adjoint:
             line["adjoint"] = adjoint_leg(s, s64, mu, e_lo)
         s64.close()
@@ -364,10 +445,9 @@ def run_ours(args):
         scf = {}
         for prec in ("mixed", "fp64") if args.precision == "mixed" and args.fp64_scf else (args.precision,):
             st = []
-            cfg = "auto" if prec == "mixed" else 3
-            s_scf = LResGPU(b, cr.pos, R_w=8.0, M=64, precision=prec, tile_config=cfg)
+            s_scf = LResGPU(b, cr.pos, R_w=8.0, M=64, precision=prec, route=args.route)
             r = scf_lcao(cr, s_scf, tol=1e-12, maxiter=args.scf_iters, vion=vion, step_times=st)
-            scf[prec] = {"s_per_iter": round(float(np.median(st[2:])) if len(st) > 2 else float(np.median(st)), 3),
+            scf[prec] = {"s_per_iter": round(float(np.median(st[2:])) if len(st) > 2 else float(np.median(st)), 4),
                          "iterations": len(st), "passes": s_scf.passes, "first_iter_s": round(st[0], 3),
                          "energy": r["energy"]}
             s_scf.close()
@@ -393,6 +473,15 @@ def run_ours(args):
                                               f"({c['eig_wall']:.2f} s wall), dsygvx below c+1.5R per window",
                                     "pole_route_value": round(c["pole_rate"], 1),
                                     "pole_route_sample": f"scipy solve per window-pole on {c['pole_windows']} windows"}
+            if args.cpu_scf and args.scf_iters > 0:
+                from oracle import cpu_baseline
+                cs = cpu_baseline.scf_window(cr, b, vion, 8.0, 64, args.scf_iters)
+                line["cpu_baseline"]["scf"] = dict(cs, unit="s/iter", iterations=args.scf_iters,
+                                                   note="reference SCF (eigen route, reuse_vectors=False) over the "
+                                                        "same fixed iteration window, window passes on all cores")
+                if "scf" in line and "mixed" in line["scf"]:
+                    line["cpu_baseline"]["scf"]["gpu_mixed_speedup_per_iter"] = round(
+                        cs["s_per_iter"] / line["scf"]["mixed"]["s_per_iter"], 1)
         except Exception as ex:   # the CPU leg must not hide the GPU result
             line["cpu_baseline"] = {"value": None, "error": repr(ex)}
     s.close()
@@ -403,21 +492,23 @@ def run_ours(args):
 
 
 def run_reference(args):
+    """The reference's CPU algorithm for the path (the eigen route of _lrft_cpp.lrft_windows,
+    restated in oracle/, windows spread over all host cores), timed on the same workload and
+    metric; nothing of the GPU library is imported."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    from oracle import cpu_baseline
     from oracle import lrft_oracle as orc
     cr, b = build_system(assembly="scipy")      # the reference's own scipy assembly
     # the potential and (mu, e_lo) of the reference's own cold call (tests/golden/jit8.npz)
     g = np.load(os.path.join(ROOT, "tests", "golden", "jit8.npz"))
     vion = orc.ion_potential(cr)
     v = orc.guess_potential(cr, vion)
+    windows, own, _ = orc.window_setup(b, cr.pos, 8.0)
 
     class W:
         pass
-    from lresdft_gb300.solver import _groups  # noqa: F401  (host-side window set-up only)
-    from oracle.lrft_oracle import window_setup
-    windows, own, _ = window_setup(b, cr.pos, 8.0)
     s = W()
     s.M = 64
     s.Wflat = np.concatenate(windows).astype(np.int64)
@@ -434,13 +525,21 @@ def run_reference(args):
             "unit": "window-pole solves/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1024 * 32 / val * 1e3, 2),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "precision": "fp64 eigen route (reference algorithm)",
             "data": "synthetic (seeded H2 crystal, potential of the uniform starting density)",
-            "config": dict(WORKLOAD, precision="fp64 eigen route (reference algorithm)"),
+            "config": dict(WORKLOAD),
             "cpu_baseline": {"value": round(val, 1), "unit": "window-pole solves/s (equivalent)",
                              "cores": c["workers"], "kind": "port",
                              "sample": f"full eigen-route window pass over {c['nwin']} windows per step"},
             "e2e": {"value": round(val, 1), "unit": "window-pole solves/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
+    iters = getattr(args, "scf_iters", SCF_ITERS)
+    if getattr(args, "cpu_scf", True) and iters > 0:
+        try:
+            cs = cpu_baseline.scf_window(cr, b, vion, 8.0, 64, iters)
+            line["cpu_baseline"]["scf"] = dict(cs, unit="s/iter", iterations=iters)
+        except Exception as ex:
+            line["cpu_baseline"]["scf"] = {"error": repr(ex)}
     print(json.dumps(line), flush=True)
 
 
@@ -452,7 +551,12 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
     ap.add_argument("--fp64-steps", type=int, default=2)
-    ap.add_argument("--scf-iters", type=int, default=4)
+    ap.add_argument("--scf-iters", type=int, default=SCF_ITERS)
+    ap.add_argument("--route", choices=["auto", "tridiag", "ldl"], default="auto")
+    ap.add_argument("--no-ldl-leg", dest="ldl_leg", action="store_false",
+                    help="skip the LDL^T-route comparison passes")
+    ap.add_argument("--no-cpu-scf", dest="cpu_scf", action="store_false",
+                    help="skip the reference SCF s/iter on the host cores (about a minute at 1024 electrons)")
     ap.add_argument("--no-fp64-scf", dest="fp64_scf", action="store_false",
                     help="skip the FP64 SCF window (about a minute at 1024 electrons)")
     ap.add_argument("--no-cpu", action="store_true")

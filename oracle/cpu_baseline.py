@@ -12,6 +12,12 @@ with one OpenBLAS thread each.  The result is expressed in the GPU metric's unit
 (windows x M/2) / wall time, i.e. window-pole solves per second that the eigen route
 replaces.  The reference's own pole route (benchmarks/window_resolvent_vs_eig.py:58-65,
 one scipy.linalg.solve per window and pole) is timed on a small sample as well.
+
+``scf_window`` times the reference's SCF (lrft/lcao3d.py:237-284 with the LRFTLCAOCpp
+solver protocol, lrft/lcao3d.py:340-456, restated by oracle.lrft_oracle) over a fixed number
+of iterations, wrapping the solver like the reference's ``Timed`` helper
+(benchmarks/scf3d_large.py:35-45): H(v) by scipy in the main process (single-threaded, as in
+the reference), every window pass spread over worker processes.
 """
 from __future__ import annotations
 
@@ -119,3 +125,160 @@ def run(H, S, X, Wflat, Woff, Oflat, Ooff, mu, e_lo, M, dV, workers=None, pole_s
         eig_rate=nwin * P / t_eig, eig_wall=t_eig, nwin=nwin, workers=workers,
         pole_rate=len(samp) * P / t_pole, pole_wall=t_pole, pole_windows=len(samp),
     )
+
+
+# ---------------------------------------------------------------------------
+# SCF seconds per iteration of the reference algorithm on the host cores
+# ---------------------------------------------------------------------------
+
+_S = {}
+
+
+def _init_scf(path):
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    from scipy import sparse
+    ld = lambda n: np.load(os.path.join(path, n + ".npy"), mmap_mode="r")  # noqa: E731
+    nb, ng = int(ld("dims")[0]), int(ld("dims")[1])
+    _S["path"], _S["nb"] = path, nb
+    _S["S"] = sparse.csr_matrix((ld("Sv"), ld("Si"), ld("Sp")), shape=(nb, nb))
+    _S["X"] = sparse.csr_matrix((ld("Xv"), ld("Xi"), ld("Xp")), shape=(ng, nb))
+    for k in ("Wflat", "Woff", "Oflat", "Ooff", "dV"):
+        _S[k] = np.asarray(ld(k))
+
+
+def _scf_windows(args):
+    """Eigen route over some windows (src/lrft_cpp.cpp:148-196): owned densities (no spin
+    factor), eigenvalues and owned weights."""
+    from scipy import linalg, sparse
+    ws, tag, mu, e_lo, M, upper, want = args
+    if _S.get("Htag") != tag:
+        ld = lambda n: np.load(os.path.join(_S["path"], f"{n}_{tag}.npy"), mmap_mode="r")  # noqa: E731
+        nb = _S["nb"]
+        _S["H"] = sparse.csr_matrix((np.asarray(ld("Hv")), np.asarray(ld("Hi")), np.asarray(ld("Hp"))),
+                                    shape=(nb, nb))
+        _S["Htag"] = tag
+    H, S, X = _S["H"], _S["S"], _S["X"]
+    Wf, Wo, Of, Oo, dV = _S["Wflat"], _S["Woff"], _S["Oflat"], _S["Ooff"], float(_S["dV"][0])
+    c0, R = 0.5 * (mu + e_lo), 0.5 * (mu - e_lo)
+    out = []
+    for w in ws:
+        W = Wf[Wo[w]:Wo[w + 1]]
+        own = Of[Oo[w]:Oo[w + 1]]
+        HW, SW = H[W][:, W].toarray(), S[W][:, W].toarray()
+        if np.isfinite(upper):
+            lam, U = linalg.eigh(HW, SW, subset_by_value=(-np.inf, upper), driver="gvx")
+        else:
+            lam, U = linalg.eigh(HW, SW, driver="gvd")
+        Y = X[own][:, W] @ U
+        c = np.sum(Y * Y, axis=0) * dV
+        d = None
+        if want:
+            with np.errstate(over="ignore"):
+                occ = 1.0 / (1.0 + ((lam - c0) / R) ** M)
+            d = (Y * Y) @ occ
+        out.append((w, d, lam, c))
+    return out
+
+
+class EigenPool:
+    """``window_pass`` of the eigen route over worker processes (spawn start method, one
+    single-threaded BLAS each), for oracle.lrft_oracle.LResEigenOracle(pool=...)."""
+
+    def __init__(self, basis, windows, own, workers=None):
+        from scipy import sparse
+        self.workers = workers or len(os.sched_getaffinity(0))
+        self.ng = basis.cr.ng
+        self.dir = tempfile.TemporaryDirectory(prefix="lres_scf_")
+        S, X = sparse.csr_matrix(basis.S), sparse.csr_matrix(basis.Xr)
+        Woff = np.concatenate([[0], np.cumsum([len(W) for W in windows])]).astype(np.int64)
+        Ooff = np.concatenate([[0], np.cumsum([len(o) for o in own])]).astype(np.int64)
+        self.Oflat = np.concatenate(own).astype(np.int64)
+        self.Ooff = Ooff
+        arrs = dict(dims=np.array([S.shape[0], X.shape[0]]), Sp=S.indptr, Si=S.indices, Sv=S.data, Xp=X.indptr,
+                    Xi=X.indices, Xv=X.data, Wflat=np.concatenate(windows).astype(np.int64), Woff=Woff,
+                    Oflat=self.Oflat, Ooff=Ooff, dV=np.array([basis.cr.dV]))
+        for k, a in arrs.items():
+            np.save(os.path.join(self.dir.name, k + ".npy"), np.ascontiguousarray(a))
+        order = np.argsort(-np.diff(Woff), kind="stable")
+        self.chunks = [order[i::self.workers * 4].tolist() for i in range(self.workers * 4)]
+        self.nwin = len(windows)
+        self.calls = 0
+        self.pool = mp.get_context("spawn").Pool(self.workers, initializer=_init_scf, initargs=(self.dir.name,))
+
+    def window_pass(self, H, mu, e_lo, M, upper, want_density):
+        from scipy import sparse
+        H = sparse.csr_matrix(H)
+        self.calls += 1
+        tag = self.calls
+        for k, a in (("Hp", H.indptr), ("Hi", H.indices), ("Hv", H.data)):
+            np.save(os.path.join(self.dir.name, f"{k}_{tag}.npy"), np.ascontiguousarray(a))
+        res = self.pool.map(_scf_windows, [(ch, tag, mu, e_lo, M, upper, want_density) for ch in self.chunks])
+        per = {w: (d, lam, c) for part in res for (w, d, lam, c) in part}
+        dens = np.zeros(self.ng) if want_density else None
+        lams, cs = [], []
+        for w in range(self.nwin):
+            d, lam, c = per[w]
+            if want_density:
+                dens[self.Oflat[self.Ooff[w]:self.Ooff[w + 1]]] = d
+            lams.append(lam)
+            cs.append(c)
+        for k in ("Hp", "Hi", "Hv"):
+            os.unlink(os.path.join(self.dir.name, f"{k}_{tag}.npy"))
+        return dens, np.concatenate(lams), np.concatenate(cs)
+
+    def close(self):
+        self.pool.close()
+        self.pool.join()
+        self.dir.cleanup()
+
+
+class Timed:
+    """Records the wall time of every density call of a solver (the reference's
+    benchmarks/scf3d_large.py:35-45 wrapper)."""
+
+    def __init__(self, solver):
+        self.s, self.times = solver, []
+
+    def density(self, v):
+        t = time.perf_counter()
+        out = self.s.density(v)
+        self.times.append(time.perf_counter() - t)
+        return out
+
+
+def scf_window(cr, basis, vion, R_w, M, iters, workers=None):
+    """The reference's SCF (Pulay mixer, mix 0.4, ndiis 6) over a fixed window of `iters`
+    iterations from the uniform start, eigen-route solver with its window passes on
+    `workers` processes.  Returns s/iter (median of iterations 3..end, the whole iteration:
+    LDA + Hartree + H(v) + density call + mixing), the density-call times, passes, energy."""
+    from . import lrft_oracle as orc
+    pool = None
+    try:
+        t = time.perf_counter()
+        solver = orc.LResEigenOracle(basis, cr.pos, R_w=R_w, M=M)
+        pool = EigenPool(basis, solver.windows, solver.own, workers)
+        solver.pool = pool
+        setup = time.perf_counter() - t
+        timed = Timed(solver)
+        # whole iterations: each density call starts at a mark, the driver's own work (LDA,
+        # Hartree, mixing) sits between consecutive marks
+        marks = []
+        inner = timed.density
+
+        class _Marked:
+            def density(self, v):
+                marks.append(time.perf_counter())
+                return inner(v)
+        t0 = time.perf_counter()
+        r = orc.scf_lcao(cr, _Marked(), tol=1e-12, maxiter=iters, vion=vion)
+        t_end = time.perf_counter()
+        marks.append(t_end)
+        it_times = [marks[i + 1] - marks[i] for i in range(len(marks) - 1)]
+        sel = it_times[2:] if len(it_times) > 2 else it_times
+        return dict(s_per_iter=float(np.median(sel)), iteration_s=[round(x, 3) for x in it_times],
+                    density_call_s=[round(x, 3) for x in timed.times], passes=solver.passes,
+                    energy=float(r["energy"]), workers=pool.workers, setup_s=round(setup, 2),
+                    wall_s=round(t_end - t0, 2))
+    finally:
+        if pool is not None:
+            pool.close()

@@ -22,7 +22,7 @@ def test_reference_arm_line(monkeypatch, capsys):
         return cr, system.LCAOBasis(cr, assembly=assembly)
 
     monkeypatch.setattr(bench, "build_system", small_system)
-    bench.run_reference(types.SimpleNamespace(steps=1, warmup=3))
+    bench.run_reference(types.SimpleNamespace(steps=1, warmup=3, scf_iters=3, cpu_scf=True))
     line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
     assert seen["assembly"] == "scipy"          # the reference's own basis assembly
     assert all(k in line for k in KEYS) and line["impl"] == "reference"
@@ -31,6 +31,31 @@ def test_reference_arm_line(monkeypatch, capsys):
     assert line["cpu_baseline"]["value"] == line["value"] == line["e2e"]["value"]
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
     assert "workload" in line["config"]
+    scf = line["cpu_baseline"]["scf"]
+    assert scf["s_per_iter"] > 0 and len(scf["iteration_s"]) == 3 and scf["workers"] >= 1
+
+
+def test_reference_arm_config_equals_ours():
+    """Both arms print the same config object (the precision is a key of its own)."""
+    import bench
+    assert "precision" not in bench.WORKLOAD and bench.WORKLOAD["parallelism"] == "single GPU"
+
+
+def test_reference_arm_loads_no_product_library():
+    """The reference arm runs in a process that never maps liblres_gb300.so."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = ("import sys, types; sys.path.insert(0, %r); import bench\n"
+            "from lresdft_gb300 import system\n"
+            "cr = system.jittered_h2((2, 2, 2), a=4.5, bond=1.4, pts_per_cell=8, jitter=0.1, seed=0)\n"
+            "bench.build_system = lambda cells=8, assembly='native': (cr, system.LCAOBasis(cr, assembly=assembly))\n"
+            "bench.run_reference(types.SimpleNamespace(steps=1, warmup=3, scf_iters=0, cpu_scf=False))\n"
+            "print('MAPPED', any('liblres_gb300' in l for l in open('/proc/self/maps')))\n") % root
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    assert "MAPPED False" in out.stdout
 
 
 def test_clock_samples_parsed():
