@@ -131,12 +131,15 @@ int lres_status(lres_ctx* ctx, int32_t* status, void* stream);
 /* Device address of the context's density array (ng doubles, valid until destroy). */
 int lres_density_ptr(lres_ctx* ctx, const double** d_dens);
 
-/* Tile configuration of the fused pole kernel: force_config in [0, 5] selects one
- * (LRES_MIXED configuration 4 runs the chunk products on the tensor cores, tcgen05 with a
- * 3xTF32 split; it is timed but kept only when forced, its error being ~5x that of the FP32
- * configurations); -1 times every configuration with full passes at (mu, e_lo) on the
- * current Hamiltonian and keeps the fastest eligible one for this context.  *chosen (may be
- * NULL) receives the choice, ms_per_config[6] (may be NULL) the measured kernel times. */
+/* Tile configuration of the pole solves, force_config in [0, 5]; -1 times every
+ * configuration on the current Hamiltonian and keeps the fastest eligible one for this context.
+ * On the LDL^T route it is the tile configuration of the fused pole kernel, timed with full
+ * passes at (mu, e_lo) (LRES_MIXED configuration 4 runs the chunk products on the tensor cores,
+ * tcgen05 with a 3xTF32 split; it is timed but kept only when forced, its error being ~5x that
+ * of the FP32 configurations).  On the tridiagonal route it is the pair of panel widths of the
+ * reduction and of the row application ((32,16), (32,32), (16,16), (32,8), (16,32), (16,8),
+ * each capped by the shared memory), timed as reduction + rows (mu, e_lo unused).
+ * *chosen (may be NULL) receives the choice, ms_per_config[6] (may be NULL) the measured times. */
 int lres_autotune(lres_ctx* ctx, double mu, double e_lo, int32_t force_config, int32_t* chosen,
                   double* ms_per_config, void* stream);
 

@@ -94,7 +94,7 @@ struct lres_ctx {
     // rows Y = F^ Q, then each pass is one fused shifted-solve + pole-sum kernel
     int route = LRES_ROUTE_LDL;
     bool tri_alloc = false, tri_ready = false;
-    int tri_nb = 0, tri_ldv = 0;
+    int tri_nb = 0, tri_nb_apply = 0, tri_ldv = 0, tri_cfg = 0;   // panel widths (tile configuration tri_cfg)
     std::vector<long long> offN;                 // window vectors (sum of n)
     long long sizeN = 0, sizeA = 0;
     long long* d_offN = nullptr;
@@ -531,7 +531,7 @@ int tri_setup(lres_ctx* c, cudaStream_t s) {
     if (c->tri_alloc) return LRES_OK;
     const bool fp32 = c->precision == LRES_MIXED;
     const size_t el = fp32 ? sizeof(float) : sizeof(double);
-    TRY(tri_pick_nb(fp32, c->nmax, c->smem_budget, &c->tri_nb, &c->tri_ldv));
+    TRY(tri_pick_nb(fp32, c->nmax, c->smem_budget, c->tri_cfg, &c->tri_nb, &c->tri_nb_apply, &c->tri_ldv));
     TRY(dalloc((char**)&c->d_triA, el * (size_t)c->sizeA));
     TRY(dalloc((char**)&c->d_trid, el * (size_t)c->sizeN));
     TRY(dalloc((char**)&c->d_trie, el * (size_t)c->sizeN));
@@ -559,7 +559,7 @@ int tri_rows(lres_ctx* c, bool trace, cudaStream_t s) {
                           : (fp32 ? (const void*)c->d_Fhat32 : (const void*)c->d_Fhat64);
     return tri_apply(fp32, ri.napply, ri.apply, c->d_n, trace ? c->d_mT : c->d_m, c->d_offA, c->d_offN,
                      trace ? c->d_offFT : c->d_offF, c->d_triA, c->d_tritau, F, trace ? c->d_Ytr : c->d_Yown,
-                     c->tri_nb, c->tri_ldv, s);
+                     c->tri_nb_apply, c->tri_ldv, s);
 }
 
 // Tridiagonal form of the current standard-form windows and the rows through its reflectors
@@ -1008,8 +1008,8 @@ extern "C" int lres_ctx_create(lres_ctx** out, const lres_system_desc* d, int pr
     }
     TRY(upload(&c->d_order_w, c->order, s));
     {
-        int nb = 0, ldv = 0;
-        const bool fits = tri_pick_nb(precision == LRES_MIXED, c->nmax, c->smem_budget, &nb, &ldv) == LRES_OK;
+        int nb = 0, nba = 0, ldv = 0;
+        const bool fits = tri_pick_nb(precision == LRES_MIXED, c->nmax, c->smem_budget, 0, &nb, &nba, &ldv) == LRES_OK;
         lres_set_error("");
         c->route = (fits && c->nwin >= 4) ? LRES_ROUTE_TRIDIAG : LRES_ROUTE_LDL;
     }
@@ -1162,6 +1162,46 @@ extern "C" int lres_autotune(lres_ctx* c, double mu, double e_lo, int32_t force_
         lres_set_error("configuration %d out of range (0..%d)", force_config, kLeftConfigs - 1);
         return LRES_EINVAL;
     }
+    cudaStream_t s = (cudaStream_t)stream;
+    if (c->route == LRES_ROUTE_TRIDIAG) {
+        // panel widths of the reduction and the row application, timed on the current
+        // Hamiltonian (reduction + rows per configuration)
+        auto apply_cfg = [&](int cfg) -> int {
+            c->tri_cfg = cfg;
+            TRY(tri_pick_nb(c->precision == LRES_MIXED, c->nmax, c->smem_budget, cfg, &c->tri_nb, &c->tri_nb_apply,
+                            &c->tri_ldv));
+            if (c->have_h) TRY(tri_refresh(c, s));
+            return LRES_OK;
+        };
+        if (force_config >= 0) {
+            TRY(apply_cfg(force_config));
+            if (chosen) *chosen = force_config;
+            return LRES_OK;
+        }
+        if (!c->have_h) {
+            lres_set_error("lres_autotune before a Hamiltonian was set");
+            return LRES_ESTATE;
+        }
+        double best = 1e300;
+        int arg = 0;
+        for (int cfg = 0; cfg < kLeftConfigs; ++cfg) {
+            double ms = 0.0;
+            for (int rep = 0; rep < 2; ++rep) {          // first repetition warms up
+                TRY(apply_cfg(cfg));
+                double t[8];
+                TRY(lres_timings(c, t, 8));
+                ms = t[6] + t[7];
+            }
+            if (ms_per_config) ms_per_config[cfg] = ms;
+            if (ms < best) {
+                best = ms;
+                arg = cfg;
+            }
+        }
+        TRY(apply_cfg(arg));
+        if (chosen) *chosen = arg;
+        return LRES_OK;
+    }
     if (force_config >= 0) {
         c->config = force_config;
         if (chosen) *chosen = force_config;
@@ -1170,13 +1210,6 @@ extern "C" int lres_autotune(lres_ctx* c, double mu, double e_lo, int32_t force_
     double out[3];
     double best = 1e300;
     int arg = 0;
-    // the tile configurations belong to the LDL^T kernel: time them on that route
-    struct RouteGuard {
-        lres_ctx* c;
-        int saved;
-        ~RouteGuard() { c->route = saved; }
-    } guard{c, c->route};
-    c->route = LRES_ROUTE_LDL;
     for (int cfg = 0; cfg < kLeftConfigs; ++cfg) {
         // the tensor-core variant (3xTF32) is timed but chosen only when forced: its
         // measured error is about 5x that of the FP32 SIMT configurations
@@ -1212,8 +1245,8 @@ extern "C" int lres_set_route(lres_ctx* c, int32_t route, void* stream) {
         c->tri_ready = false;               // T no longer follows the Hamiltonian
         return LRES_OK;
     }
-    int nb = 0, ldv = 0;
-    TRY(tri_pick_nb(c->precision == LRES_MIXED, c->nmax, c->smem_budget, &nb, &ldv));
+    int nb = 0, nba = 0, ldv = 0;
+    TRY(tri_pick_nb(c->precision == LRES_MIXED, c->nmax, c->smem_budget, c->tri_cfg, &nb, &nba, &ldv));
     const int old = c->route;
     c->route = route;
     int rc = LRES_OK;

@@ -307,42 +307,40 @@ __global__ void __launch_bounds__(NT) tri_reduce_kernel(TriReduceParams<R> p) {
                     Ws[jj * ldv + i] = (i > j && i < n) ? pv[i] - K * Vs[jj * ldv + i] : R(0);
                 __syncthreads();
             }
-            // ---- trailing update of both triangles: A -= V W^T + W V^T on rows, columns >= t0,
-            //      one quad of rows x TC columns per thread (rows below t0 left unchanged)
+            // ---- trailing update of both triangles: A -= V W^T + W V^T on rows, columns >= t0.
+            //      One quad of rows x one aligned quad of columns per thread: the v, w values of
+            //      both quads come from shared memory as 16-byte vectors (4 loads per 32 FMAs);
+            //      rows and columns below t0 are left unchanged.
             const int t0 = j0 + nbp;
             if (t0 < n) {
-                constexpr int TC = 4;
                 const int q0 = t0 & ~3;
                 const int nq = (ld - q0) >> 2;
-                const int ncb = (n - t0 + TC - 1) / TC;
+                const int ncb = (ld - q0) >> 2;
                 for (int tile = tid; tile < nq * ncb; tile += NT) {
                     const int q = tile % nq, cb = tile / nq;
-                    const int i = q0 + 4 * q, c0 = t0 + cb * TC;
-                    R acc[TC][4];
+                    const int i = q0 + 4 * q, c0 = q0 + 4 * cb;
+                    R acc[4][4];
 #pragma unroll
-                    for (int c = 0; c < TC; ++c)
+                    for (int c = 0; c < 4; ++c)
 #pragma unroll
                         for (int r = 0; r < 4; ++r) acc[c][r] = R(0);
                     for (int l = 0; l < nbp; ++l) {
-                        R vi[4], wi[4];
+                        R vi[4], wi[4], vk[4], wk[4];
+                        ld4(Vs + (size_t)l * ldv + i, vi);
+                        ld4(Ws + (size_t)l * ldv + i, wi);
+                        ld4(Vs + (size_t)l * ldv + c0, vk);
+                        ld4(Ws + (size_t)l * ldv + c0, wk);
 #pragma unroll
-                        for (int r = 0; r < 4; ++r) {
-                            vi[r] = Vs[l * ldv + i + r];
-                            wi[r] = Ws[l * ldv + i + r];
-                        }
+                        for (int c = 0; c < 4; ++c)
 #pragma unroll
-                        for (int c = 0; c < TC; ++c) {
-                            const int col = min(c0 + c, ldv - 1);     // reads stay inside the vectors
-                            const R wk = Ws[l * ldv + col], vk = Vs[l * ldv + col];
-#pragma unroll
-                            for (int r = 0; r < 4; ++r) acc[c][r] = fma(vi[r], wk, fma(wi[r], vk, acc[c][r]));
-                        }
+                            for (int r = 0; r < 4; ++r) acc[c][r] = fma(vi[r], wk[c], fma(wi[r], vk[c], acc[c][r]));
                     }
 #pragma unroll
-                    for (int c = 0; c < TC; ++c) {
-                        if (c0 + c >= n) continue;
+                    for (int c = 0; c < 4; ++c) {
+                        const int col = c0 + c;
+                        if (col < t0 || col >= n) continue;
                         R x[4];
-                        R* dst = A + i + (long long)(c0 + c) * ld;
+                        R* dst = A + i + (long long)col * ld;
                         ld4(dst, x);
 #pragma unroll
                         for (int r = 0; r < 4; ++r)
@@ -392,10 +390,37 @@ struct TriApplyParams {
     int ldv;
 };
 
+// Index of v_l[k] in the staged panel: rows of NB values, 16-byte groups of each row permuted
+// by XOR with the row index, so that the staging stores (consecutive k, one l) spread over the
+// banks while each row is still read as aligned 16-byte vectors.
+template <class R, int NB>
+__device__ __forceinline__ int panel_index(int k, int l) {
+    constexpr int GW = 16 / (int)sizeof(R) < NB ? 16 / (int)sizeof(R) : NB;   // elements per group
+    constexpr int NG = NB / GW;                                                 // groups per row
+    return k * NB + (((l / GW) ^ (k % NG)) * GW) + (l % GW);
+}
+
+// One 16-byte group of a staged row (4 floats or 2 doubles; a narrower panel row whole).
+template <class R, int GW>
+__device__ __forceinline__ void ld_group(const R* src, R (&x)[GW]) {
+    if constexpr (sizeof(R) == 4 && GW == 4) {
+        const float4 v = *reinterpret_cast<const float4*>(src);
+        x[0] = v.x; x[1] = v.y; x[2] = v.z; x[3] = v.w;
+    } else if constexpr (sizeof(R) == 8 && GW == 2) {
+        const double2 v = *reinterpret_cast<const double2*>(src);
+        x[0] = v.x; x[1] = v.y;
+    } else {
+#pragma unroll
+        for (int e = 0; e < GW; ++e) x[e] = src[e];
+    }
+}
+
 template <class R, int NT, int NB>
 __global__ void __launch_bounds__(NT) tri_apply_kernel(TriApplyParams<R> p) {
+    constexpr int GW = 16 / (int)sizeof(R) < NB ? 16 / (int)sizeof(R) : NB;
+    constexpr int NG = NB / GW;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    R* const Vs = reinterpret_cast<R*>(smem_raw);         // [ldv][NB]: v_l[k] at Vs[k*NB + l]
+    R* const Vs = reinterpret_cast<R*>(smem_raw);         // [ldv][NB], panel_index layout
     R* const Tm = Vs + (size_t)p.ldv * NB;                 // [NB][NB] upper triangular factor
     R* const Gm = Tm + NB * NB;                            // [NB][NB] V^T V (above the diagonal)
     const int4 item = p.items[blockIdx.x];
@@ -417,24 +442,39 @@ __global__ void __launch_bounds__(NT) tri_apply_kernel(TriApplyParams<R> p) {
 
     for (int j0 = 0; j0 < n - 2; j0 += NB) {
         const int nbp = min(NB, n - 2 - j0);
+        const int nk = n - j0 - 1;                         // rows j0+1 .. n-1
         __syncthreads();                                   // the previous panel is consumed
-        for (int idx = tid; idx < (n - j0) * NB; idx += NT) {
-            const int k = j0 + idx / NB, l = idx % NB;
+        // v_l (l < nbp) lives on rows j0+l+1 .. n-1 (v_l[j0+l+1] = 1); reads run down the
+        // columns of the reflector storage (coalesced)
+        for (int idx = tid; idx < nk * NB; idx += NT) {
+            const int l = idx / nk, k = j0 + 1 + idx % nk;
             R v = R(0);
             if (l < nbp) {
                 const int j = j0 + l;
                 if (k == j + 1) v = R(1);
                 else if (k > j + 1) v = Aw[k + j * ld];
             }
-            Vs[(size_t)k * NB + l] = v;
+            Vs[panel_index<R, NB>(k, l)] = v;
         }
         __syncthreads();
-        for (int q = tid; q < NB * NB; q += NT) {
-            const int a = q / NB, b = q % NB;
-            R g = R(0);
-            if (a < b && b < nbp)
-                for (int k = j0 + b + 1; k < n; ++k) g += Vs[(size_t)k * NB + a] * Vs[(size_t)k * NB + b];
-            Gm[q] = g;
+        // G = V^T V by 2 x 2 blocks per thread (entries above the diagonal are used)
+        for (int q = tid; q < NB * NB / 4; q += NT) {
+            const int a0 = 2 * (q / (NB / 2)), b0 = 2 * (q % (NB / 2));
+            R g00 = R(0), g01 = R(0), g10 = R(0), g11 = R(0);
+            if (b0 + 1 > a0) {
+                for (int k = j0 + 1; k < n; ++k) {
+                    const R va0 = Vs[panel_index<R, NB>(k, a0)], va1 = Vs[panel_index<R, NB>(k, a0 + 1)];
+                    const R vb0 = Vs[panel_index<R, NB>(k, b0)], vb1 = Vs[panel_index<R, NB>(k, b0 + 1)];
+                    g00 = fma(va0, vb0, g00);
+                    g01 = fma(va0, vb1, g01);
+                    g10 = fma(va1, vb0, g10);
+                    g11 = fma(va1, vb1, g11);
+                }
+            }
+            Gm[a0 * NB + b0] = g00;
+            Gm[a0 * NB + b0 + 1] = g01;
+            Gm[(a0 + 1) * NB + b0] = g10;
+            Gm[(a0 + 1) * NB + b0 + 1] = g11;
         }
         __syncthreads();
         // T (forward, columnwise): T_ll = tau_l, T[0:l, l] = -tau_l T[0:l, 0:l] (V^T V)[0:l, l]
@@ -444,9 +484,9 @@ __global__ void __launch_bounds__(NT) tri_apply_kernel(TriApplyParams<R> p) {
                 for (int a = tid; a < NB; a += 32) {
                     R val = R(0);
                     if (a < l) {
-                        R s = R(0);
-                        for (int b = a; b < l; ++b) s += Tm[a * NB + b] * Gm[b * NB + l];
-                        val = -tl * s;
+                        R sacc = R(0);
+                        for (int b = a; b < l; ++b) sacc = fma(Tm[a * NB + b], Gm[b * NB + l], sacc);
+                        val = -tl * sacc;
                     } else if (a == l) {
                         val = tl;
                     }
@@ -460,12 +500,17 @@ __global__ void __launch_bounds__(NT) tri_apply_kernel(TriApplyParams<R> p) {
             R sv[NB];
 #pragma unroll
             for (int l = 0; l < NB; ++l) sv[l] = R(0);
-#pragma unroll 8
+#pragma unroll 4
             for (int k = j0 + 1; k < n; ++k) {
                 const R y = Yw[r + (long long)k * m];
-                const R* vk = Vs + (size_t)k * NB;
+                const R* row = Vs + (size_t)k * NB;
 #pragma unroll
-                for (int l = 0; l < NB; ++l) sv[l] = fma(y, vk[l], sv[l]);
+                for (int g = 0; g < NG; ++g) {
+                    R x[GW];
+                    ld_group<R, GW>(row + ((g ^ (k % NG)) * GW), x);
+#pragma unroll
+                    for (int e = 0; e < GW; ++e) sv[g * GW + e] = fma(y, x[e], sv[g * GW + e]);
+                }
             }
             // s <- s T in place (T upper triangular: column b needs s_0..s_b, so b descends)
 #pragma unroll
@@ -475,12 +520,17 @@ __global__ void __launch_bounds__(NT) tri_apply_kernel(TriApplyParams<R> p) {
                 for (int a = 0; a <= b; ++a) acc = fma(sv[a], Tm[a * NB + b], acc);
                 sv[b] = acc;
             }
-#pragma unroll 8
+#pragma unroll 4
             for (int k = j0 + 1; k < n; ++k) {
-                const R* vk = Vs + (size_t)k * NB;
+                const R* row = Vs + (size_t)k * NB;
                 R acc = R(0);
 #pragma unroll
-                for (int l = 0; l < NB; ++l) acc = fma(sv[l], vk[l], acc);
+                for (int g = 0; g < NG; ++g) {
+                    R x[GW];
+                    ld_group<R, GW>(row + ((g ^ (k % NG)) * GW), x);
+#pragma unroll
+                    for (int e = 0; e < GW; ++e) acc = fma(sv[g * GW + e], x[e], acc);
+                }
                 Yw[r + (long long)k * m] -= acc;
             }
         }
@@ -756,19 +806,25 @@ __global__ void tri_mineig_kernel(int nwin, const int* n_w, const long long* off
 // host launchers
 // ---------------------------------------------------------------------------
 
-int tri_pick_nb(bool fp32, int nmax, size_t smem_budget, int* nb, int* ldv) {
+// Panel widths of the reduction and of the row application for tile configuration cfg
+// (0..kLeftConfigs-1), each capped by what fits the shared memory at windows of nmax.
+static const int kTriCfg[6][2] = {{32, 16}, {32, 32}, {16, 16}, {32, 8}, {16, 32}, {16, 8}};
+
+int tri_pick_nb(bool fp32, int nmax, size_t smem_budget, int cfg, int* nb, int* nb_apply, int* ldv) {
     const int el = fp32 ? 4 : 8;
     *ldv = (std::max(nmax, 1) + 31) / 32 * 32;
-    for (int b : {32, 16, 8, 4}) {
-        const size_t red = reduce_smem_elems(b, *ldv) * el;
-        const size_t app = (size_t)el * ((size_t)*ldv * b + 2 * b * b);
-        if (red <= smem_budget && app <= smem_budget) {
-            *nb = b;
-            return LRES_OK;
-        }
+    if (cfg < 0 || cfg >= 6) cfg = 0;
+    *nb = *nb_apply = 0;
+    for (int b : {32, 16, 8, 4})
+        if (b <= kTriCfg[cfg][0] && !*nb && reduce_smem_elems(b, *ldv) * el <= smem_budget) *nb = b;
+    for (int b : {32, 16, 8, 4})
+        if (b <= kTriCfg[cfg][1] && !*nb_apply && (size_t)el * ((size_t)*ldv * b + 2 * b * b) <= smem_budget)
+            *nb_apply = b;
+    if (!*nb || !*nb_apply) {
+        lres_set_error("windows of %d functions exceed the shared memory of the tridiagonal reduction", nmax);
+        return LRES_EINVAL;
     }
-    lres_set_error("windows of %d functions exceed the shared memory of the tridiagonal reduction", nmax);
-    return LRES_EINVAL;
+    return LRES_OK;
 }
 
 template <class R>

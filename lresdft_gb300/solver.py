@@ -226,9 +226,9 @@ class LResGPU:
         # tile configuration of the pole kernel: an index, or "auto" to time all of them on
         # the first Hamiltonian (see autotune); None keeps the library default
         self.tile_config = tile_config
-        # the tile configurations belong to the LDL^T route (and the adjoint, which always
-        # factors by LDL^T): autotuned on the first Hamiltonian only when that route solves
-        self._tuned = not (tile_config == "auto" and self.route == "ldl")
+        # tile configurations: of the LDL^T kernel on that route, of the reduction and row panels
+        # on the tridiagonal route; "auto" times them on the first Hamiltonian
+        self._tuned = not (tile_config == "auto")
         if isinstance(tile_config, int):
             self.autotune(0.0, -1.0, config=tile_config)
         self._out = np.zeros(3)
@@ -447,8 +447,9 @@ class LResGPU:
         return (dens.copy() if want_density else None), float(self._out[0]), float(self._out[1])
 
     def autotune(self, mu, e_lo, config=-1):
-        """Pick the tile configuration of the pole kernel (-1: time all six with full
-        passes at (mu, e_lo) and keep the fastest).  Returns (chosen, ms per config)."""
+        """Pick the tile configuration of the route (-1: time all six on the current
+        Hamiltonian and keep the fastest; on the LDL^T route with full passes at (mu, e_lo)).
+        Returns (chosen, ms per config)."""
         chosen = C.c_int32()
         ms = np.full(6, -1.0)
         _lib.check(_lib.lib.lres_autotune(self._ctx, float(mu), float(e_lo), int(config), C.byref(chosen),
