@@ -6,13 +6,17 @@
 # image has none, so the LAPACK symbols are mapped onto the copies exported by
 # scipy's bundled OpenBLAS (exported names only, nothing is disassembled).
 #
-# Usage: sh oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: sh oracle/build_ref.sh REFERENCE_ROOT   (or LRES_REFERENCE_ROOT in the environment)
 # Needs pybind11 (present in the x86 build container only); on machines without
 # it or without the reference tree the script exits 0 and builds nothing.
 set -e
-REF=${1:-/root/reference}
+REF=${1:-${LRES_REFERENCE_ROOT:-}}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
+if [ -z "$REF" ]; then
+    echo "build_ref: no reference root given (argument or LRES_REFERENCE_ROOT); skipped"
+    exit 0
+fi
 if [ ! -f "$REF/src/lrft_cpp.cpp" ]; then
     echo "build_ref: no reference tree at $REF; skipped"
     exit 0

@@ -16,17 +16,22 @@ import os
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-DEFAULT_ROOT = os.environ.get("LRES_REFERENCE_ROOT", "/root/reference")
+def reference_root():
+    """The reference source tree: the LRES_REFERENCE_ROOT environment variable (no default)."""
+    return os.environ.get("LRES_REFERENCE_ROOT")
 
 
-def available(root: str = DEFAULT_ROOT) -> bool:
-    return os.path.isfile(os.path.join(root, "lrft", "lcao3d.py"))
+def available(root=None) -> bool:
+    root = root or reference_root()
+    return bool(root) and os.path.isfile(os.path.join(root, "lrft", "lcao3d.py"))
 
 
-def load(root: str = DEFAULT_ROOT, need_cpp: bool = True):
-    """Return the reference modules (three_d, lcao3d); registers lrft._lrft_cpp."""
+def load(root=None, need_cpp: bool = True):
+    """Return the reference modules (three_d, lcao3d); registers lrft._lrft_cpp.  The tree is
+    `root`, else LRES_REFERENCE_ROOT."""
+    root = root or reference_root()
     if not available(root):
-        raise ImportError(f"reference tree not found at {root}")
+        raise ImportError(f"reference tree not found (root {root!r}; set LRES_REFERENCE_ROOT)")
     if root not in sys.path:
         sys.path.insert(0, root)
     import lrft  # noqa: F401

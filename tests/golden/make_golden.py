@@ -1,8 +1,9 @@
 """Generate the golden vectors under tests/golden/ by running the REFERENCE's own code
 (albert-hzbn/LResDFT: lrft.three_d, lrft.lcao3d and the C++ back end src/lrft_cpp.cpp
-compiled by oracle/build_ref.sh).  Needs the reference tree, so it only runs in the
-build container:
+compiled by oracle/build_ref.sh).  Needs the reference's source tree, named by the
+LRES_REFERENCE_ROOT environment variable:
 
+    export LRES_REFERENCE_ROOT=<reference tree>
     sh oracle/build_ref.sh && python tests/golden/make_golden.py
 
 Geometries are produced by lresdft_gb300.system (identical conventions to the
