@@ -137,7 +137,7 @@ int lres_density_ptr(lres_ctx* ctx, const double** d_dens);
  * passes at (mu, e_lo) (LRES_MIXED configuration 4 runs the chunk products on the tensor cores,
  * tcgen05 with a 3xTF32 split; it is timed but kept only when forced, its error being ~5x that
  * of the FP32 configurations).  On the tridiagonal route it is the pair of panel widths of the
- * reduction and of the row application ((32,16), (32,32), (16,16), (32,8), (16,32), (16,8),
+ * reduction and of the row application with their thread layouts (six measured variants,
  * each capped by the shared memory), timed as reduction + rows (mu, e_lo unused).
  * *chosen (may be NULL) receives the choice, ms_per_config[6] (may be NULL) the measured times. */
 int lres_autotune(lres_ctx* ctx, double mu, double e_lo, int32_t force_config, int32_t* chosen,

@@ -94,7 +94,7 @@ struct lres_ctx {
     // rows Y = F^ Q, then each pass is one fused shifted-solve + pole-sum kernel
     int route = LRES_ROUTE_LDL;
     bool tri_alloc = false, tri_ready = false;
-    int tri_nb = 0, tri_nb_apply = 0, tri_ldv = 0, tri_cfg = 0;   // panel widths (tile configuration tri_cfg)
+    int tri_nb = 0, tri_nt = 0, tri_nb_apply = 0, tri_rpt = 1, tri_ldv = 0, tri_cfg = 0;   // tile configuration
     std::vector<long long> offN;                 // window vectors (sum of n)
     long long sizeN = 0, sizeA = 0;
     long long* d_offN = nullptr;
@@ -531,7 +531,8 @@ int tri_setup(lres_ctx* c, cudaStream_t s) {
     if (c->tri_alloc) return LRES_OK;
     const bool fp32 = c->precision == LRES_MIXED;
     const size_t el = fp32 ? sizeof(float) : sizeof(double);
-    TRY(tri_pick_nb(fp32, c->nmax, c->smem_budget, c->tri_cfg, &c->tri_nb, &c->tri_nb_apply, &c->tri_ldv));
+    TRY(tri_pick_nb(fp32, c->nmax, c->smem_budget, c->tri_cfg, &c->tri_nb, &c->tri_nt, &c->tri_nb_apply, &c->tri_rpt,
+                    &c->tri_ldv));
     TRY(dalloc((char**)&c->d_triA, el * (size_t)c->sizeA));
     TRY(dalloc((char**)&c->d_trid, el * (size_t)c->sizeN));
     TRY(dalloc((char**)&c->d_trie, el * (size_t)c->sizeN));
@@ -559,7 +560,7 @@ int tri_rows(lres_ctx* c, bool trace, cudaStream_t s) {
                           : (fp32 ? (const void*)c->d_Fhat32 : (const void*)c->d_Fhat64);
     return tri_apply(fp32, ri.napply, ri.apply, c->d_n, trace ? c->d_mT : c->d_m, c->d_offA, c->d_offN,
                      trace ? c->d_offFT : c->d_offF, c->d_triA, c->d_tritau, F, trace ? c->d_Ytr : c->d_Yown,
-                     c->tri_nb_apply, c->tri_ldv, s);
+                     c->tri_nb_apply, c->tri_rpt, c->tri_ldv, s);
 }
 
 // Tridiagonal form of the current standard-form windows and the rows through its reflectors
@@ -570,7 +571,7 @@ int tri_prepare(lres_ctx* c, cudaStream_t s) {
     TRY(mark(c, 6, 0, s));
     TRY(tri_reduce(fp32, c->nwin, c->d_order_w, c->d_counter, c->d_n, c->d_offC, c->d_offA, c->d_offN,
                    fp32 ? (const void*)tri_hhat32(c) : (const void*)c->d_Hhat, c->d_triA, c->d_trid, c->d_trie,
-                   c->d_tritau, c->d_tstatus, c->tri_nb, c->tri_ldv, c->smem_budget, s));
+                   c->d_tritau, c->d_tstatus, c->tri_nb, c->tri_nt, c->tri_ldv, c->smem_budget, s));
     TRY(mark(c, 6, 1, s));
     TRY(mark(c, 7, 0, s));
     TRY(tri_rows(c, false, s));
@@ -1008,8 +1009,9 @@ extern "C" int lres_ctx_create(lres_ctx** out, const lres_system_desc* d, int pr
     }
     TRY(upload(&c->d_order_w, c->order, s));
     {
-        int nb = 0, nba = 0, ldv = 0;
-        const bool fits = tri_pick_nb(precision == LRES_MIXED, c->nmax, c->smem_budget, 0, &nb, &nba, &ldv) == LRES_OK;
+        int nb = 0, nt = 0, nba = 0, rpt = 0, ldv = 0;
+        const bool fits =
+            tri_pick_nb(precision == LRES_MIXED, c->nmax, c->smem_budget, 0, &nb, &nt, &nba, &rpt, &ldv) == LRES_OK;
         lres_set_error("");
         c->route = (fits && c->nwin >= 4) ? LRES_ROUTE_TRIDIAG : LRES_ROUTE_LDL;
     }
@@ -1168,8 +1170,8 @@ extern "C" int lres_autotune(lres_ctx* c, double mu, double e_lo, int32_t force_
         // Hamiltonian (reduction + rows per configuration)
         auto apply_cfg = [&](int cfg) -> int {
             c->tri_cfg = cfg;
-            TRY(tri_pick_nb(c->precision == LRES_MIXED, c->nmax, c->smem_budget, cfg, &c->tri_nb, &c->tri_nb_apply,
-                            &c->tri_ldv));
+            TRY(tri_pick_nb(c->precision == LRES_MIXED, c->nmax, c->smem_budget, cfg, &c->tri_nb, &c->tri_nt,
+                            &c->tri_nb_apply, &c->tri_rpt, &c->tri_ldv));
             if (c->have_h) TRY(tri_refresh(c, s));
             return LRES_OK;
         };
@@ -1245,8 +1247,8 @@ extern "C" int lres_set_route(lres_ctx* c, int32_t route, void* stream) {
         c->tri_ready = false;               // T no longer follows the Hamiltonian
         return LRES_OK;
     }
-    int nb = 0, nba = 0, ldv = 0;
-    TRY(tri_pick_nb(c->precision == LRES_MIXED, c->nmax, c->smem_budget, c->tri_cfg, &nb, &nba, &ldv));
+    int nb = 0, nt = 0, nba = 0, rpt = 0, ldv = 0;
+    TRY(tri_pick_nb(c->precision == LRES_MIXED, c->nmax, c->smem_budget, c->tri_cfg, &nb, &nt, &nba, &rpt, &ldv));
     const int old = c->route;
     c->route = route;
     int rc = LRES_OK;

@@ -108,13 +108,14 @@ int pole_sums(int nwin, const long long* offQ, const int* m_w, const long long* 
               double* dens, double* n_w, double* e_w, cudaStream_t s);
 
 // Multi-shift tridiagonal route (tridiag.cu): R = float (fp32) or double.
-int tri_pick_nb(bool fp32, int nmax, size_t smem_budget, int cfg, int* nb, int* nb_apply, int* ldv);
+int tri_pick_nb(bool fp32, int nmax, size_t smem_budget, int cfg, int* nb, int* nt, int* nb_apply, int* rpt,
+                int* ldv);
 int tri_reduce(bool fp32, int nwin, const int* order, int* counter, const int* n_w, const long long* offC,
                const long long* offA, const long long* offN, const void* H, void* A, void* d, void* e, void* tau,
-               int* status, int nb, int ldv, size_t smem_budget, cudaStream_t s);
+               int* status, int nb, int nt, int ldv, size_t smem_budget, cudaStream_t s);
 int tri_apply(bool fp32, int nitems, const int4* items, const int* n_w, const int* m_w, const long long* offA,
               const long long* offN, const long long* offF, const void* A, const void* tau, const void* F, void* Y,
-              int nb, int ldv, cudaStream_t s);
+              int nb, int rpt, int ldv, cudaStream_t s);
 int tri_rows_per_item(bool fp32, int P);
 int tri_pass(bool fp32, int nitems, const int4* items, int* counter, const int* n_w, const int* m_w,
              const long long* offN, const long long* offF, const long long* offQ, const long long* Oflat,

@@ -73,8 +73,7 @@ __device__ __forceinline__ R block_sum(R x, R* red) {
     return s;
 }
 
-constexpr int kRedNT = 512;                   // threads of the reduction kernel
-constexpr int kAppNT = 256;                   // threads (rows) of the apply kernel
+constexpr int kAppRows = 256;                 // rows of one item of the apply kernel
 
 // ---------------------------------------------------------------------------
 // Householder tridiagonalisation
@@ -117,9 +116,9 @@ struct TriReduceParams {
 };
 
 // Shared memory of the reduction, in elements of R.
-inline size_t reduce_smem_elems(int nb, int ldv) {
-    const size_t big = std::max((size_t)2 * nb * ldv, (size_t)(kRedNT / 32) * 32 * 33);
-    return big + 2 * (size_t)ldv + 4 * (size_t)kRedNT + 64 + kRedNT / 32;
+inline size_t reduce_smem_elems(int nb, int ldv, int nt) {
+    const size_t big = std::max((size_t)2 * nb * ldv, (size_t)(nt / 32) * 32 * 33);
+    return big + 2 * (size_t)ldv + 4 * (size_t)nt + 64 + nt / 32;
 }
 
 template <class R, int NT>
@@ -415,7 +414,9 @@ __device__ __forceinline__ void ld_group(const R* src, R (&x)[GW]) {
     }
 }
 
-template <class R, int NT, int NB>
+// NT threads handle the item's rows (at most NT * RPT), RPT rows each (rows tid + u NT), so
+// that every staged reflector value feeds RPT multiply-adds.
+template <class R, int NT, int NB, int RPT>
 __global__ void __launch_bounds__(NT) tri_apply_kernel(TriApplyParams<R> p) {
     constexpr int GW = 16 / (int)sizeof(R) < NB ? 16 / (int)sizeof(R) : NB;
     constexpr int NG = NB / GW;
@@ -433,12 +434,20 @@ __global__ void __launch_bounds__(NT) tri_apply_kernel(TriApplyParams<R> p) {
     const R* Fw = p.F + p.offF[w];
     R* Yw = p.Y + p.offF[w];
     const int tid = threadIdx.x;
-    const bool act = tid < nr && r0 + tid < m;
-    const long long r = r0 + tid;
-    if (act) {
-#pragma unroll 8
-        for (int k = 0; k < n; ++k) Yw[r + (long long)k * m] = Fw[r + (long long)k * m];
+    bool act[RPT];
+    long long rr[RPT];
+#pragma unroll
+    for (int u = 0; u < RPT; ++u) {
+        const int t = tid + u * NT;
+        act[u] = t < nr && r0 + t < m;
+        rr[u] = act[u] ? r0 + t : 0;
     }
+#pragma unroll
+    for (int u = 0; u < RPT; ++u)
+        if (act[u]) {
+#pragma unroll 8
+            for (int k = 0; k < n; ++k) Yw[rr[u] + (long long)k * m] = Fw[rr[u] + (long long)k * m];
+        }
 
     for (int j0 = 0; j0 < n - 2; j0 += NB) {
         const int nbp = min(NB, n - 2 - j0);
@@ -496,43 +505,60 @@ __global__ void __launch_bounds__(NT) tri_apply_kernel(TriApplyParams<R> p) {
             }
         }
         __syncthreads();
-        if (act) {
-            R sv[NB];
+        R sv[RPT][NB];
 #pragma unroll
-            for (int l = 0; l < NB; ++l) sv[l] = R(0);
-#pragma unroll 4
-            for (int k = j0 + 1; k < n; ++k) {
-                const R y = Yw[r + (long long)k * m];
-                const R* row = Vs + (size_t)k * NB;
+        for (int u = 0; u < RPT; ++u)
 #pragma unroll
-                for (int g = 0; g < NG; ++g) {
-                    R x[GW];
-                    ld_group<R, GW>(row + ((g ^ (k % NG)) * GW), x);
+            for (int l = 0; l < NB; ++l) sv[u][l] = R(0);
+#pragma unroll 2
+        for (int k = j0 + 1; k < n; ++k) {
+            R y[RPT];
 #pragma unroll
-                    for (int e = 0; e < GW; ++e) sv[g * GW + e] = fma(y, x[e], sv[g * GW + e]);
-                }
+            for (int u = 0; u < RPT; ++u) y[u] = act[u] ? Yw[rr[u] + (long long)k * m] : R(0);
+            const R* row = Vs + (size_t)k * NB;
+#pragma unroll
+            for (int g = 0; g < NG; ++g) {
+                R x[GW];
+                ld_group<R, GW>(row + ((g ^ (k % NG)) * GW), x);
+#pragma unroll
+                for (int u = 0; u < RPT; ++u)
+#pragma unroll
+                    for (int e = 0; e < GW; ++e) sv[u][g * GW + e] = fma(y[u], x[e], sv[u][g * GW + e]);
             }
-            // s <- s T in place (T upper triangular: column b needs s_0..s_b, so b descends)
+        }
+        // s <- s T in place (T upper triangular: column b needs s_0..s_b, so b descends)
 #pragma unroll
-            for (int b = NB - 1; b >= 0; --b) {
-                R acc = R(0);
+        for (int b = NB - 1; b >= 0; --b) {
+            R acc[RPT];
 #pragma unroll
-                for (int a = 0; a <= b; ++a) acc = fma(sv[a], Tm[a * NB + b], acc);
-                sv[b] = acc;
+            for (int u = 0; u < RPT; ++u) acc[u] = R(0);
+#pragma unroll
+            for (int a = 0; a <= b; ++a) {
+                const R t = Tm[a * NB + b];
+#pragma unroll
+                for (int u = 0; u < RPT; ++u) acc[u] = fma(sv[u][a], t, acc[u]);
             }
-#pragma unroll 4
-            for (int k = j0 + 1; k < n; ++k) {
-                const R* row = Vs + (size_t)k * NB;
-                R acc = R(0);
 #pragma unroll
-                for (int g = 0; g < NG; ++g) {
-                    R x[GW];
-                    ld_group<R, GW>(row + ((g ^ (k % NG)) * GW), x);
+            for (int u = 0; u < RPT; ++u) sv[u][b] = acc[u];
+        }
+#pragma unroll 2
+        for (int k = j0 + 1; k < n; ++k) {
+            const R* row = Vs + (size_t)k * NB;
+            R acc[RPT];
 #pragma unroll
-                    for (int e = 0; e < GW; ++e) acc = fma(sv[g * GW + e], x[e], acc);
-                }
-                Yw[r + (long long)k * m] -= acc;
+            for (int u = 0; u < RPT; ++u) acc[u] = R(0);
+#pragma unroll
+            for (int g = 0; g < NG; ++g) {
+                R x[GW];
+                ld_group<R, GW>(row + ((g ^ (k % NG)) * GW), x);
+#pragma unroll
+                for (int u = 0; u < RPT; ++u)
+#pragma unroll
+                    for (int e = 0; e < GW; ++e) acc[u] = fma(sv[u][g * GW + e], x[e], acc[u]);
             }
+#pragma unroll
+            for (int u = 0; u < RPT; ++u)
+                if (act[u]) Yw[rr[u] + (long long)k * m] -= acc[u];
         }
     }
 }
@@ -806,20 +832,30 @@ __global__ void tri_mineig_kernel(int nwin, const int* n_w, const long long* off
 // host launchers
 // ---------------------------------------------------------------------------
 
-// Panel widths of the reduction and of the row application for tile configuration cfg
-// (0..kLeftConfigs-1), each capped by what fits the shared memory at windows of nmax.
-static const int kTriCfg[6][2] = {{32, 16}, {32, 32}, {16, 16}, {32, 8}, {16, 32}, {16, 8}};
+// Tile configurations of the tridiagonal route: reduction panel width and threads, row
+// application panel width and rows per thread.  Panel widths are capped by what fits the
+// shared memory at windows of nmax.
+struct TriCfg {
+    int nb, nt, nba, rpt;
+};
+// Measured at 1024 electrons (reduction + rows, mixed): (16, 512, 32, 1) 12.5 ms, (32, 512, 32, 1)
+// 13.0-13.9 ms, the 256-thread reductions and the two-rows-per-thread applications 14-18 ms.
+static const TriCfg kTriCfg[6] = {{16, 512, 32, 1}, {32, 512, 32, 1}, {16, 512, 16, 1},
+                                  {16, 512, 16, 4}, {16, 256, 32, 1}, {16, 512, 32, 2}};
 
-int tri_pick_nb(bool fp32, int nmax, size_t smem_budget, int cfg, int* nb, int* nb_apply, int* ldv) {
+int tri_pick_nb(bool fp32, int nmax, size_t smem_budget, int cfg, int* nb, int* nt, int* nb_apply, int* rpt,
+                int* ldv) {
     const int el = fp32 ? 4 : 8;
     *ldv = (std::max(nmax, 1) + 31) / 32 * 32;
     if (cfg < 0 || cfg >= 6) cfg = 0;
+    const TriCfg& t = kTriCfg[cfg];
+    *nt = t.nt;
     *nb = *nb_apply = 0;
     for (int b : {32, 16, 8, 4})
-        if (b <= kTriCfg[cfg][0] && !*nb && reduce_smem_elems(b, *ldv) * el <= smem_budget) *nb = b;
+        if (b <= t.nb && !*nb && reduce_smem_elems(b, *ldv, t.nt) * el <= smem_budget) *nb = b;
     for (int b : {32, 16, 8, 4})
-        if (b <= kTriCfg[cfg][1] && !*nb_apply && (size_t)el * ((size_t)*ldv * b + 2 * b * b) <= smem_budget)
-            *nb_apply = b;
+        if (b <= t.nba && !*nb_apply && (size_t)el * ((size_t)*ldv * b + 2 * b * b) <= smem_budget) *nb_apply = b;
+    *rpt = *nb_apply >= 16 ? t.rpt : 1;
     if (!*nb || !*nb_apply) {
         lres_set_error("windows of %d functions exceed the shared memory of the tridiagonal reduction", nmax);
         return LRES_EINVAL;
@@ -827,53 +863,57 @@ int tri_pick_nb(bool fp32, int nmax, size_t smem_budget, int cfg, int* nb, int* 
     return LRES_OK;
 }
 
-template <class R>
+template <class R, int NT>
 static int launch_reduce(const TriReduceParams<R>& p, size_t smem_budget, cudaStream_t s) {
-    const size_t smem = reduce_smem_elems(p.nb, p.ldv) * sizeof(R);
+    const size_t smem = reduce_smem_elems(p.nb, p.ldv, NT) * sizeof(R);
     if (smem > smem_budget) {
         lres_set_error("tridiagonal reduction needs %zu B of shared memory", smem);
         return LRES_EINVAL;
     }
     int per_sm = 0;
-    if (int rc = prepare_kernel<tri_reduce_kernel<R, kRedNT>>(kRedNT, smem, &per_sm)) return rc;
+    if (int rc = prepare_kernel<tri_reduce_kernel<R, NT>>(NT, smem, &per_sm)) return rc;
     const int grid = std::min(p.nwin, std::max(1, per_sm) * device_sms());
-    tri_reduce_kernel<R, kRedNT><<<grid, kRedNT, smem, s>>>(p);
+    tri_reduce_kernel<R, NT><<<grid, NT, smem, s>>>(p);
     LRES_CUDA_TRY(cudaGetLastError());
     return LRES_OK;
 }
 
 int tri_reduce(bool fp32, int nwin, const int* order, int* counter, const int* n_w, const long long* offC,
                const long long* offA, const long long* offN, const void* H, void* A, void* d, void* e, void* tau,
-               int* status, int nb, int ldv, size_t smem_budget, cudaStream_t s) {
+               int* status, int nb, int nt, int ldv, size_t smem_budget, cudaStream_t s) {
     if (!nwin) return LRES_OK;
     LRES_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), s));
     if (fp32) {
         TriReduceParams<float> p{nwin, order, counter, n_w, offC, offA, offN, (const float*)H, (float*)A,
                                  (float*)d, (float*)e, (float*)tau, status, nb, ldv};
-        return launch_reduce(p, smem_budget, s);
+        return nt == 512 ? launch_reduce<float, 512>(p, smem_budget, s) : launch_reduce<float, 256>(p, smem_budget, s);
     }
     TriReduceParams<double> p{nwin, order, counter, n_w, offC, offA, offN, (const double*)H, (double*)A,
                               (double*)d, (double*)e, (double*)tau, status, nb, ldv};
-    return launch_reduce(p, smem_budget, s);
+    return nt == 512 ? launch_reduce<double, 512>(p, smem_budget, s) : launch_reduce<double, 256>(p, smem_budget, s);
 }
 
-template <class R, int NB>
+template <class R, int NB, int RPT>
 static int launch_apply(const TriApplyParams<R>& p, cudaStream_t s) {
+    constexpr int NT = kAppRows / RPT;
     const size_t smem = sizeof(R) * ((size_t)p.ldv * NB + 2 * NB * NB);
     int per_sm = 0;
-    if (int rc = prepare_kernel<tri_apply_kernel<R, kAppNT, NB>>(kAppNT, smem, &per_sm)) return rc;
-    tri_apply_kernel<R, kAppNT, NB><<<p.nitems, kAppNT, smem, s>>>(p);
+    if (int rc = prepare_kernel<tri_apply_kernel<R, NT, NB, RPT>>(NT, smem, &per_sm)) return rc;
+    tri_apply_kernel<R, NT, NB, RPT><<<p.nitems, NT, smem, s>>>(p);
     LRES_CUDA_TRY(cudaGetLastError());
     return LRES_OK;
 }
 
 template <class R>
-static int dispatch_apply(const TriApplyParams<R>& p, int nb, cudaStream_t s) {
+static int dispatch_apply(const TriApplyParams<R>& p, int nb, int rpt, cudaStream_t s) {
+    if (nb == 32 && rpt == 2) return launch_apply<R, 32, 2>(p, s);
+    if (nb == 16 && rpt == 4) return launch_apply<R, 16, 4>(p, s);
+    if (nb == 16 && rpt == 2) return launch_apply<R, 16, 2>(p, s);
     switch (nb) {
-        case 32: return launch_apply<R, 32>(p, s);
-        case 16: return launch_apply<R, 16>(p, s);
-        case 8: return launch_apply<R, 8>(p, s);
-        case 4: return launch_apply<R, 4>(p, s);
+        case 32: return launch_apply<R, 32, 1>(p, s);
+        case 16: return launch_apply<R, 16, 1>(p, s);
+        case 8: return launch_apply<R, 8, 1>(p, s);
+        case 4: return launch_apply<R, 4, 1>(p, s);
         default:
             lres_set_error("tridiagonal panel width %d not compiled", nb);
             return LRES_EINVAL;
@@ -882,16 +922,16 @@ static int dispatch_apply(const TriApplyParams<R>& p, int nb, cudaStream_t s) {
 
 int tri_apply(bool fp32, int nitems, const int4* items, const int* n_w, const int* m_w, const long long* offA,
               const long long* offN, const long long* offF, const void* A, const void* tau, const void* F, void* Y,
-              int nb, int ldv, cudaStream_t s) {
+              int nb, int rpt, int ldv, cudaStream_t s) {
     if (!nitems) return LRES_OK;
     if (fp32) {
         TriApplyParams<float> p{nitems, items, n_w, m_w, offA, offN, offF, (const float*)A, (const float*)tau,
                                 (const float*)F, (float*)Y, ldv};
-        return dispatch_apply(p, nb, s);
+        return dispatch_apply(p, nb, rpt, s);
     }
     TriApplyParams<double> p{nitems, items, n_w, m_w, offA, offN, offF, (const double*)A, (const double*)tau,
                              (const double*)F, (double*)Y, ldv};
-    return dispatch_apply(p, nb, s);
+    return dispatch_apply(p, nb, rpt, s);
 }
 
 int tri_rows_per_item(bool fp32, int P) {
