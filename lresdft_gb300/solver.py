@@ -233,6 +233,8 @@ class LResGPU:
             self.autotune(0.0, -1.0, config=tile_config)
         self._out = np.zeros(3)
         self.dens_buf = np.zeros(cr.ng)
+        self._device_out = False
+        self._v_keep = None
         # trace rows (passes that need N and E only): installed when the owned points
         # outnumber the window functions clearly (fine grids)
         self._trace = False
@@ -267,8 +269,17 @@ class LResGPU:
         _lib.check(_lib.lib.lres_set_route(self._ctx, code, None))
 
     def set_potential(self, v):
-        """H(v) for all windows: assembled on the GPU from v, or (for bases with extra
-        terms in H) built by basis.H on the host and gathered on the GPU."""
+        """H(v) for all windows: assembled on the GPU from v (a host array or a CUDA tensor of
+        ng float64), or (for bases with extra terms in H) built by basis.H on the host and
+        gathered on the GPU."""
+        if hasattr(v, "is_cuda") and v.is_cuda:
+            if self._gpu_h:
+                import torch
+                vd = v.detach().reshape(-1).to(torch.float64).contiguous()
+                self._v_keep = vd                     # alive until the kernels have read it
+                self.set_potential_device(vd.data_ptr(), torch.cuda.current_stream().cuda_stream)
+                return
+            v = v.detach().cpu().numpy()
         if self._gpu_h:
             v = _lib.f64(v).ravel()
             _lib.check(_lib.lib.lres_set_potential(self._ctx, v.ctypes.data, 0, None))
@@ -437,14 +448,23 @@ class LResGPU:
         _lib.check(_lib.lib.lres_set_hamiltonian_csr(self._ctx, _lib.ptr64(Hp), _lib.ptr64(Hi), _lib.ptrd(Hv), None))
 
     def pole_pass(self, mu, e_lo, want_density=True):
-        """One pole pass: returns (density or None, N(mu), E_band)."""
+        """One pole pass: returns (density or None, N(mu), E_band); the density is a host
+        array, or a CUDA tensor while a density_device call runs."""
         self.passes += 1
-        dens = self.dens_buf if want_density else None
-        ptr = dens.ctypes.data if want_density else None
-        _lib.check(_lib.lib.lres_pass(self._ctx, float(mu), float(e_lo), ptr, 0, _lib.ptrd(self._out), None))
+        if want_density and self._device_out:
+            import torch
+            dens = torch.empty(self.b.cr.ng, dtype=torch.float64, device="cuda")
+            torch.cuda.synchronize()               # the device copy below runs on the legacy stream
+            _lib.check(_lib.lib.lres_pass(self._ctx, float(mu), float(e_lo), dens.data_ptr(), 1,
+                                          _lib.ptrd(self._out), None))
+        else:
+            dens = self.dens_buf if want_density else None
+            ptr = dens.ctypes.data if want_density else None
+            _lib.check(_lib.lib.lres_pass(self._ctx, float(mu), float(e_lo), ptr, 0, _lib.ptrd(self._out), None))
+            dens = dens.copy() if want_density else None
         if self.trace is not None:
             self.trace.append((float(mu), float(self._out[0])))
-        return (dens.copy() if want_density else None), float(self._out[0]), float(self._out[1])
+        return dens, float(self._out[0]), float(self._out[1])
 
     def autotune(self, mu, e_lo, config=-1):
         """Pick the tile configuration of the route (-1: time all six on the current
@@ -625,6 +645,15 @@ class LResGPU:
         return b
 
     # ------------------------------------------------------------------ protocol
+    def density_device(self, v, N=None):
+        """density() with device tensors: v a CUDA tensor of ng float64 values, the returned
+        density a CUDA tensor of the grid's shape (the same protocol and passes)."""
+        self._device_out = True
+        try:
+            return self.density(v, N)
+        finally:
+            self._device_out = False
+
     def density(self, v, N=None):
         try:
             return self._density(v, N)
