@@ -417,7 +417,7 @@ __device__ __forceinline__ void ld_group(const R* src, R (&x)[GW]) {
 // NT threads handle the item's rows (at most NT * RPT), RPT rows each (rows tid + u NT), so
 // that every staged reflector value feeds RPT multiply-adds.
 template <class R, int NT, int NB, int RPT>
-__global__ void __launch_bounds__(NT) tri_apply_kernel(TriApplyParams<R> p) {
+__global__ void __launch_bounds__(NT, RPT == 1 && NB <= 16 ? 3 : 1) tri_apply_kernel(TriApplyParams<R> p) {
     constexpr int GW = 16 / (int)sizeof(R) < NB ? 16 / (int)sizeof(R) : NB;
     constexpr int NG = NB / GW;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -510,7 +510,7 @@ __global__ void __launch_bounds__(NT) tri_apply_kernel(TriApplyParams<R> p) {
         for (int u = 0; u < RPT; ++u)
 #pragma unroll
             for (int l = 0; l < NB; ++l) sv[u][l] = R(0);
-#pragma unroll 2
+#pragma unroll 4
         for (int k = j0 + 1; k < n; ++k) {
             R y[RPT];
 #pragma unroll
@@ -541,7 +541,7 @@ __global__ void __launch_bounds__(NT) tri_apply_kernel(TriApplyParams<R> p) {
 #pragma unroll
             for (int u = 0; u < RPT; ++u) sv[u][b] = acc[u];
         }
-#pragma unroll 2
+#pragma unroll 4
         for (int k = j0 + 1; k < n; ++k) {
             const R* row = Vs + (size_t)k * NB;
             R acc[RPT];
@@ -668,12 +668,13 @@ __global__ void __launch_bounds__(NT) tri_pass_kernel(TriPassParams<R> p) {
 
         const C z = p.shifts[k < P ? k : 0];
         C gp = C{R(0), R(0)};                       // 1 / D_{i-1}
-        C uc[RR], pr[RR];
+        C uc[RR], pr[RR], pc[RR];
         double2 acc[RR];
 #pragma unroll
         for (int u = 0; u < RR; ++u) {
             uc[u] = C{R(0), R(0)};
             pr[u] = C{R(0), R(0)};
+            pc[u] = C{R(0), R(0)};
             acc[u] = make_double2(0.0, 0.0);
         }
         for (int c = 0; c < nch; ++c) {
@@ -713,12 +714,21 @@ __global__ void __launch_bounds__(NT) tri_pass_kernel(TriPassParams<R> p) {
                         pr[u].y = fma(sr, gp.y, fma(si, gp.x, pr[u].y));
                     }
                 }
-                // each chunk's sum is formed from zero and added in FP64
+                // each chunk's sum is formed from zero; chunk sums are added in the working
+                // precision over 8 chunks, those sums in FP64 (GB300's FP64 rate is 1/64 of FP32)
 #pragma unroll
                 for (int u = 0; u < RR; ++u) {
-                    acc[u].x += (double)pr[u].x;
-                    acc[u].y += (double)pr[u].y;
+                    pc[u].x += pr[u].x;
+                    pc[u].y += pr[u].y;
                     pr[u] = C{R(0), R(0)};
+                }
+                if ((c & 7) == 7 || c + 1 == nch) {
+#pragma unroll
+                    for (int u = 0; u < RR; ++u) {
+                        acc[u].x += (double)pc[u].x;
+                        acc[u].y += (double)pc[u].y;
+                        pc[u] = C{R(0), R(0)};
+                    }
                 }
             }
             __syncthreads();                          // buffer c & 1 is free for chunk c + 2
