@@ -4,6 +4,7 @@
 #include "lres_internal.h"
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <complex>
 #include <memory>
@@ -75,6 +76,10 @@ struct lres_ctx {
     bool skip_rows = false;              // owned-point rows start late enough to skip panels
     long long *d_offC = nullptr, *d_offF = nullptr, *d_offQ = nullptr, *d_Oflat = nullptr;
     int *d_wgrp_off = nullptr, *d_wgrp = nullptr, *d_wgrp_lo = nullptr, *d_gloc = nullptr;
+    // gather tables: per window function (local atom, function in atom, atom size), per
+    // window pair of local atoms the value offset of the stored block (h, g) or -1
+    int *d_gfn = nullptr, *d_gbtab = nullptr, *d_gnlg = nullptr;
+    long long *d_gfnoff = nullptr, *d_gbtoff = nullptr;
     // block storage
     BlockPattern bp;
     Supports sp;
@@ -94,7 +99,10 @@ struct lres_ctx {
     // rows Y = F^ Q, then each pass is one fused shifted-solve + pole-sum kernel
     int route = LRES_ROUTE_LDL;
     bool tri_alloc = false, tri_ready = false;
-    int tri_nb = 0, tri_nt = 0, tri_nb_apply = 0, tri_rpt = 1, tri_ldv = 0, tri_cfg = 0;   // tile configuration
+    TriPick tri;                                 // tile configuration (tri_pick)
+    int tri_cfg = 0;
+    float* d_triT = nullptr;                     // T factors of the resident row application
+    long long triT_size = 0;
     std::vector<long long> offN;                 // window vectors (sum of n)
     long long sizeN = 0, sizeA = 0;
     long long* d_offN = nullptr;
@@ -105,7 +113,8 @@ struct lres_ctx {
     void *d_Yown = nullptr, *d_Ytr = nullptr;
     double* d_lam = nullptr;                     // per-window smallest eigenvalue
     struct RowItems {                            // work items over the rows of every window
-        int4* apply = nullptr;                   // (window, first row, rows <= 256)
+        int4* apply = nullptr;                   // (window, first row, rows <= rows per application item)
+        int arows = 0;                           // rows per application item the items were built for
         int napply = 0;
         int4* pass = nullptr;                    // (window, first row, rows <= rows per pass item)
         int npass = 0;
@@ -167,13 +176,14 @@ struct lres_ctx {
 
 lres_ctx::~lres_ctx() {
     void* ptrs[] = {d_n, d_m, d_c0, d_offC, d_offF, d_offQ, d_Oflat, d_wgrp_off, d_wgrp, d_wgrp_lo, d_gloc,
+                    d_gfn, d_gbtab, d_gnlg, d_gfnoff, d_gbtoff,
                     bp.gptr, bp.bptr, bp.bcol, bp.brow, bp.boff, bp.btrans, bp.pair_blk, sp.soff, sp.sgrid,
-                    sp.sval, sp.coff, sp.cslot, d_Sblk, d_Tblk, d_Hblk, d_SW, d_HW, d_F, d_LinvT, d_Y, d_Hhat,
+                    sp.sval, sp.sval32, sp.vslot, sp.coff, sp.cslot, d_Sblk, d_Tblk, d_Hblk, d_SW, d_HW, d_F, d_LinvT, d_Y, d_Hhat,
                     d_Hhat32, d_Fhat32, d_LinvT_df, d_H_df, d_Y_df, d_items, d_items_win, d_items_sub, d_counter, d_status, d_npos, d_ws, d_shifts,
                     d_wq, d_wzq, d_q, d_dens, d_nw, d_ew, d_v, d_fftwork, d_adjA[0], d_adjA[1], d_adjA[2],
                     d_dHW, d_dSW, d_gH, d_adjdv, d_adju, d_cw, d_order, d_eoff, d_poff, d_ent, d_pent, d_adjws,
                     d_mT, d_offFT, d_offQT, d_FT, d_FhatT32, d_qT, d_Fhat64, d_FhatT64, d_offN, d_offA, d_order_w, d_LinvT32, d_Linv32,
-                    d_tstatus, d_triA, d_trid, d_trie, d_tritau, d_Yown, d_Ytr, d_lam};
+                    d_tstatus, d_triA, d_trid, d_trie, d_tritau, d_Yown, d_Ytr, d_lam, d_triT};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     ri_own.release();
@@ -381,9 +391,8 @@ int tri_prepare(lres_ctx* c, cudaStream_t s);
 
 int after_h_blocks(lres_ctx* c, cudaStream_t s) {
     TRY(mark(c, 3, 0, s));
-    LRES_CUDA_TRY(cudaMemsetAsync(c->d_HW, 0, sizeof(double) * c->sizeC, s));
-    TRY(gather_windows(c->bp, c->nwin, c->d_wgrp_off, c->d_wgrp, c->d_wgrp_lo, c->d_gloc, c->d_offC, c->d_n, c->nmax,
-                       c->d_Hblk, c->d_HW, s));
+    TRY(gather_windows(c->nwin, c->nmax, c->d_gfn, c->d_gfnoff, c->d_gbtab, c->d_gbtoff, c->d_gnlg, c->d_offC,
+                       c->d_n, c->d_Hblk, c->d_HW, s));
     TRY(mark(c, 3, 1, s));
     if (needs_standard_form(c)) {
         TRY(mark(c, 4, 0, s));
@@ -502,20 +511,23 @@ int setup_standard_form(lres_ctx* c, cudaStream_t s) {
 }
 
 // Work items over the rows of every window, windows in the order of c->order (most
-// expensive first): blocks of 256 rows for the reflector application, batches of the pass
-// kernel's rows per item for the pole passes (each window's batches contiguous).
+// expensive first): blocks of the application's rows per item for the reflector application,
+// batches of the pass kernel's rows per item for the pole passes (each window's batches
+// contiguous).
 int build_row_items(lres_ctx* c, const std::vector<int>& m, lres_ctx::RowItems& ri, cudaStream_t s) {
     ri.release();
     const int rb = tri_rows_per_item(c->precision == LRES_MIXED, c->npoles);
+    const int ar = c->tri.arows;
     std::vector<int4> ap, pa;
     std::vector<int> first(c->nwin, 0), count(c->nwin, 0);
     for (int w : c->order) {
-        for (int r0 = 0; r0 < m[w]; r0 += 256) ap.push_back(make_int4(w, r0, std::min(256, m[w] - r0), 0));
+        for (int r0 = 0; r0 < m[w]; r0 += ar) ap.push_back(make_int4(w, r0, std::min(ar, m[w] - r0), 0));
         first[w] = (int)pa.size();
         for (int r0 = 0; r0 < m[w]; r0 += rb) pa.push_back(make_int4(w, r0, std::min(rb, m[w] - r0), 0));
         count[w] = (int)pa.size() - first[w];
     }
     ri.napply = (int)ap.size();
+    ri.arows = ar;
     ri.npass = (int)pa.size();
     TRY(upload(&ri.apply, ap, s));
     TRY(upload(&ri.pass, pa, s));
@@ -526,13 +538,25 @@ int build_row_items(lres_ctx* c, const std::vector<int>& m, lres_ctx::RowItems& 
     return LRES_OK;
 }
 
+// T-factor buffer of the resident row application (grown on a configuration change).
+int ensure_tfactors(lres_ctx* c) {
+    const long long need = (long long)c->nwin * c->tri.tstride;
+    if (need <= c->triT_size) return LRES_OK;
+    if (c->d_triT) cudaFree(c->d_triT);
+    c->d_triT = nullptr;
+    c->triT_size = 0;
+    TRY(dalloc(&c->d_triT, need));
+    c->triT_size = need;
+    return LRES_OK;
+}
+
 // Buffers of the tridiagonal route (once per context).
 int tri_setup(lres_ctx* c, cudaStream_t s) {
     if (c->tri_alloc) return LRES_OK;
     const bool fp32 = c->precision == LRES_MIXED;
     const size_t el = fp32 ? sizeof(float) : sizeof(double);
-    TRY(tri_pick_nb(fp32, c->nmax, c->smem_budget, c->tri_cfg, &c->tri_nb, &c->tri_nt, &c->tri_nb_apply, &c->tri_rpt,
-                    &c->tri_ldv));
+    TRY(tri_pick(fp32, c->nmax, c->smem_budget, c->tri_cfg, &c->tri));
+    TRY(ensure_tfactors(c));
     TRY(dalloc((char**)&c->d_triA, el * (size_t)c->sizeA));
     TRY(dalloc((char**)&c->d_trid, el * (size_t)c->sizeN));
     TRY(dalloc((char**)&c->d_trie, el * (size_t)c->sizeN));
@@ -558,9 +582,10 @@ int tri_rows(lres_ctx* c, bool trace, cudaStream_t s) {
     const lres_ctx::RowItems& ri = trace ? c->ri_tr : c->ri_own;
     const void* F = trace ? (fp32 ? (const void*)c->d_FhatT32 : (const void*)c->d_FhatT64)
                           : (fp32 ? (const void*)c->d_Fhat32 : (const void*)c->d_Fhat64);
+    // the T factors depend on the reflectors only: formed with the owned rows
     return tri_apply(fp32, ri.napply, ri.apply, c->d_n, trace ? c->d_mT : c->d_m, c->d_offA, c->d_offN,
                      trace ? c->d_offFT : c->d_offF, c->d_triA, c->d_tritau, F, trace ? c->d_Ytr : c->d_Yown,
-                     c->tri_nb_apply, c->tri_rpt, c->tri_ldv, s);
+                     c->tri, c->nwin, !trace, c->d_triT, c->smem_budget, s);
 }
 
 // Tridiagonal form of the current standard-form windows and the rows through its reflectors
@@ -571,7 +596,7 @@ int tri_prepare(lres_ctx* c, cudaStream_t s) {
     TRY(mark(c, 6, 0, s));
     TRY(tri_reduce(fp32, c->nwin, c->d_order_w, c->d_counter, c->d_n, c->d_offC, c->d_offA, c->d_offN,
                    fp32 ? (const void*)tri_hhat32(c) : (const void*)c->d_Hhat, c->d_triA, c->d_trid, c->d_trie,
-                   c->d_tritau, c->d_tstatus, c->tri_nb, c->tri_nt, c->tri_ldv, c->smem_budget, s));
+                   c->d_tritau, c->d_tstatus, c->tri, c->nmax, c->smem_budget, s));
     TRY(mark(c, 6, 1, s));
     TRY(mark(c, 7, 0, s));
     TRY(tri_rows(c, false, s));
@@ -597,7 +622,7 @@ int tri_run_pass(lres_ctx* c, bool trace, cudaStream_t s) {
     TRY(tri_pass(fp32, ri.npass, ri.pass, c->d_counter, c->d_n, trace ? c->d_mT : c->d_m, c->d_offN,
                  trace ? c->d_offFT : c->d_offF, trace ? c->d_offQT : c->d_offQ, trace ? nullptr : c->d_Oflat,
                  trace ? c->d_Ytr : c->d_Yown, c->d_trid, c->d_trie, c->npoles, c->d_shifts, c->d_wq, c->d_wzq,
-                 trace ? nullptr : c->d_dens, ri.part, c->d_status, c->tri_ldv, c->smem_budget, s));
+                 trace ? nullptr : c->d_dens, ri.part, c->d_status, c->tri.ldv, c->smem_budget, s));
     TRY(mark(c, 0, 1, s));
     TRY(mark(c, 1, 0, s));
     TRY(tri_window_sums(c->nwin, ri.first, ri.count, ri.part, c->dV, c->d_nw, c->d_ew, s));
@@ -883,6 +908,12 @@ extern "C" int lres_ctx_create(lres_ctx** out, const lres_system_desc* d, int pr
     TRY(upload(&c->sp.soff, soff, s));
     TRY(upload(&c->sp.sgrid, sgrid, s));
     TRY(upload(&c->sp.sval, sval, s));
+    if (c->precision == LRES_MIXED && assemble_h32_supported(c->bp)) {
+        // the mixed H(v) assembly reads FP32 basis values and an FP32 potential per slot
+        std::vector<float> sval32(sval.begin(), sval.end());
+        TRY(upload(&c->sp.sval32, sval32, s));
+        TRY(dalloc(&c->sp.vslot, std::max<long long>(nslot, 1)));
+    }
     TRY(upload(&c->d_Sblk, Sblk, s));
     TRY(upload(&c->d_Tblk, Tblk, s));
     TRY(dalloc(&c->d_Hblk, nval));
@@ -921,6 +952,40 @@ extern "C" int lres_ctx_create(lres_ctx** out, const lres_system_desc* d, int pr
     TRY(upload(&c->d_wgrp_lo, wgrp_lo, s));
     TRY(upload(&c->d_gloc, gloc, s));
     {
+        // gather tables
+        std::vector<int> gfn, gbtab, gnlg(c->nwin);
+        std::vector<long long> gfnoff(c->nwin + 1, 0), gbtoff(c->nwin + 1, 0);
+        for (int w = 0; w < c->nwin; ++w) {
+            const int i0 = wgrp_off[w], L = wgrp_off[w + 1] - i0;
+            gnlg[w] = L;
+            for (int a = 0; a < L; ++a) {
+                const int g = wgrp[i0 + a], nf = c->gptr_h[g + 1] - c->gptr_h[g];
+                if (nf > 63 || a >= (1 << 19)) {
+                    lres_set_error("window gather: atoms of at most 63 functions (got %d)", nf);
+                    return LRES_EINVAL;
+                }
+                for (int f = 0; f < nf; ++f) gfn.push_back((a << 12) | (f << 6) | nf);
+            }
+            gfnoff[w + 1] = (long long)gfn.size();
+            for (int a = 0; a < L; ++a)
+                for (int b = 0; b < L; ++b) {
+                    const int blkid = find_block(c->bptr_h, c->bcol_h, wgrp[i0 + b], wgrp[i0 + a]);
+                    if (blkid >= 0 && c->boff_h[blkid] > INT_MAX - 4096) {
+                        lres_set_error("window gather: block storage beyond 2^31 values");
+                        return LRES_EINVAL;
+                    }
+                    gbtab.push_back(blkid < 0 ? -1 : (int)c->boff_h[blkid]);
+                }
+            gbtoff[w + 1] = (long long)gbtab.size();
+        }
+        TRY(upload(&c->d_gfn, gfn, s));
+        TRY(upload(&c->d_gfnoff, gfnoff, s));
+        TRY(upload(&c->d_gbtab, gbtab, s));
+        TRY(upload(&c->d_gbtoff, gbtoff, s));
+        TRY(upload(&c->d_gnlg, gnlg, s));
+        LRES_CUDA_TRY(cudaStreamSynchronize(s));
+    }
+    {
         std::vector<long long> Oflat(d->Oflat, d->Oflat + c->npts);
         TRY(upload(&c->d_Oflat, Oflat, s));
     }
@@ -936,9 +1001,8 @@ extern "C" int lres_ctx_create(lres_ctx** out, const lres_system_desc* d, int pr
     // ---- dense window overlaps and owned-point blocks
     TRY(dalloc(&c->d_SW, c->sizeC));
     TRY(dalloc(&c->d_HW, c->sizeC));
-    LRES_CUDA_TRY(cudaMemsetAsync(c->d_SW, 0, sizeof(double) * c->sizeC, s));
-    TRY(gather_windows(c->bp, c->nwin, c->d_wgrp_off, c->d_wgrp, c->d_wgrp_lo, c->d_gloc, c->d_offC, c->d_n, c->nmax,
-                       c->d_Sblk, c->d_SW, s));
+    TRY(gather_windows(c->nwin, c->nmax, c->d_gfn, c->d_gfnoff, c->d_gbtab, c->d_gbtoff, c->d_gnlg, c->d_offC,
+                       c->d_n, c->d_Sblk, c->d_SW, s));
     TRY(dalloc(&c->d_F, c->sizeF));
     LRES_CUDA_TRY(cudaMemsetAsync(c->d_F, 0, sizeof(double) * c->sizeF, s));
     {
@@ -1009,9 +1073,8 @@ extern "C" int lres_ctx_create(lres_ctx** out, const lres_system_desc* d, int pr
     }
     TRY(upload(&c->d_order_w, c->order, s));
     {
-        int nb = 0, nt = 0, nba = 0, rpt = 0, ldv = 0;
-        const bool fits =
-            tri_pick_nb(precision == LRES_MIXED, c->nmax, c->smem_budget, 0, &nb, &nt, &nba, &rpt, &ldv) == LRES_OK;
+        TriPick pk;
+        const bool fits = tri_pick(precision == LRES_MIXED, c->nmax, c->smem_budget, 0, &pk) == LRES_OK;
         lres_set_error("");
         c->route = (fits && c->nwin >= 4) ? LRES_ROUTE_TRIDIAG : LRES_ROUTE_LDL;
     }
@@ -1062,7 +1125,10 @@ extern "C" int lres_set_potential(lres_ctx* c, const double* v, int v_on_device,
         dv = c->d_v;
     }
     TRY(mark(c, 2, 0, s));
-    TRY(assemble_h(c->bp, c->sp, c->d_Tblk, dv, c->dV, c->d_Hblk, s));
+    if (c->sp.sval32)
+        TRY(assemble_h32(c->bp, c->sp, c->d_Tblk, dv, c->dV, c->d_Hblk, s));
+    else
+        TRY(assemble_h(c->bp, c->sp, c->d_Tblk, dv, c->dV, c->d_Hblk, s));
     TRY(mark(c, 2, 1, s));
     return after_h_blocks(c, s);
 }
@@ -1169,9 +1235,19 @@ extern "C" int lres_autotune(lres_ctx* c, double mu, double e_lo, int32_t force_
         // panel widths of the reduction and the row application, timed on the current
         // Hamiltonian (reduction + rows per configuration)
         auto apply_cfg = [&](int cfg) -> int {
+            TriPick pk;
+            TRY(tri_pick(c->precision == LRES_MIXED, c->nmax, c->smem_budget, cfg, &pk));
             c->tri_cfg = cfg;
-            TRY(tri_pick_nb(c->precision == LRES_MIXED, c->nmax, c->smem_budget, cfg, &c->tri_nb, &c->tri_nt,
-                            &c->tri_nb_apply, &c->tri_rpt, &c->tri_ldv));
+            c->tri = pk;
+            if (c->tri_alloc) {
+                TRY(ensure_tfactors(c));
+                if (c->ri_own.arows != pk.arows) TRY(build_row_items(c, c->m_w, c->ri_own, s));
+                if (c->have_trace && c->ri_tr.arows != pk.arows) {
+                    std::vector<int> mT(c->nwin);
+                    LRES_CUDA_TRY(cudaMemcpy(mT.data(), c->d_mT, sizeof(int) * c->nwin, cudaMemcpyDeviceToHost));
+                    TRY(build_row_items(c, mT, c->ri_tr, s));
+                }
+            }
             if (c->have_h) TRY(tri_refresh(c, s));
             return LRES_OK;
         };
@@ -1247,8 +1323,8 @@ extern "C" int lres_set_route(lres_ctx* c, int32_t route, void* stream) {
         c->tri_ready = false;               // T no longer follows the Hamiltonian
         return LRES_OK;
     }
-    int nb = 0, nt = 0, nba = 0, rpt = 0, ldv = 0;
-    TRY(tri_pick_nb(c->precision == LRES_MIXED, c->nmax, c->smem_budget, c->tri_cfg, &nb, &nt, &nba, &rpt, &ldv));
+    TriPick pk;
+    TRY(tri_pick(c->precision == LRES_MIXED, c->nmax, c->smem_budget, c->tri_cfg, &pk));
     const int old = c->route;
     c->route = route;
     int rc = LRES_OK;

@@ -181,41 +181,192 @@ int assemble_h(const BlockPattern& bp, const Supports& sp, const double* Tblk, c
 }
 
 // ---------------------------------------------------------------------------
+// H(v) assembly for the mixed precision: FP32 products summed in FP32 over blocks of 32
+// common points per lane, the block sums accumulated as unevaluated FP32 pairs (hi + lo,
+// Knuth's TwoSum), the lanes' pairs reduced the same way and converted to FP64 once per
+// element.  The unblocked FP32 sum drifts (~1e-6 Ha per window in the band energy, one
+// sign); the blocked one is as accurate as the FP64 assembly ahead of the FP32 window
+// reduction.  No FP64 arithmetic per point (GB300's FP64 rate is 1/64 of FP32).
+// ---------------------------------------------------------------------------
+
+// v at every support slot, FP32 (the FP32 kernel reads it next to the basis values)
+__global__ void slot_potential_kernel(long long nslot, const int* sgrid, const double* v, float* vslot) {
+    const long long a = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a < nslot) vslot[a] = (float)v[sgrid[a]];
+}
+
+template <int NF>
+__device__ __forceinline__ void load_slot(const float* p, float (&x)[NF]) {
+    const float4 a = *reinterpret_cast<const float4*>(p);
+    x[0] = a.x; x[1] = a.y; x[2] = a.z; x[3] = a.w;
+    if constexpr (NF > 4) {
+        const float4 b = *reinterpret_cast<const float4*>(p + 4);
+        const float t[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+        for (int f = 4; f < NF; ++f) x[f] = t[f - 4];
+    }
+}
+
+constexpr int kAsmBlock = 32;                   // common points per lane and FP32 block
+
+constexpr int kAsmThreads = 128;
+
+// (hi, lo) <- (hi, lo) + x with the rounding error of hi + x kept in lo (Knuth's TwoSum).
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
+    const float s = hi + x;
+    const float bp = s - hi;
+    const float err = (hi - (s - bp)) + (x - bp);
+    hi = s;
+    lo += err;
+}
+
+// One warp per pair; the pair sums of each lane live in shared memory ([element][thread],
+// conflict-free), which keeps the kernel below 100 registers.
+template <int NF>
+__global__ void __launch_bounds__(kAsmThreads, 5) assemble_h32_kernel(int npair, const int* pair_blk, const int* brow,
+                                                                      const int* bcol, const long long* boff,
+                                                                      const int* btrans, const int* gptr,
+                                                                      const long long* soff, const float* sval32,
+                                                                      const float* vslot, const long long* coff,
+                                                                      const int2* cslot, const double* Tblk,
+                                                                      double dV, double* Hblk) {
+    __shared__ float2 acc_s[NF * NF][kAsmThreads];
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31, t = threadIdx.x;
+    if (warp >= npair) return;
+    const int b = pair_blk[warp];
+    const int g = brow[b], h = bcol[b];
+    const int nfg = gptr[g + 1] - gptr[g], nfh = gptr[h + 1] - gptr[h];
+    const long long sg0 = soff[g], sh0 = soff[h];
+#pragma unroll
+    for (int k = 0; k < NF * NF; ++k) acc_s[k][t] = make_float2(0.0f, 0.0f);
+    const long long c0 = coff[warp], c1 = coff[warp + 1];
+    for (long long base = c0; base < c1; base += 32 * kAsmBlock) {
+        const long long cend = min(c1, base + 32 * kAsmBlock);
+        float blk[NF][NF];
+#pragma unroll
+        for (int f = 0; f < NF; ++f)
+#pragma unroll
+            for (int e = 0; e < NF; ++e) blk[f][e] = 0.0f;
+#pragma unroll 2
+        for (long long c = base + lane; c < cend; c += 32) {
+            const int2 ss = cslot[c];
+            const long long a = sg0 + ss.x, bb = sh0 + ss.y;
+            const float vv = vslot[a];
+            float xg[NF], xh[NF];
+            load_slot<NF>(sval32 + a * 8, xg);
+            load_slot<NF>(sval32 + bb * 8, xh);
+#pragma unroll
+            for (int e = 0; e < NF; ++e) xh[e] *= vv;
+#pragma unroll
+            for (int f = 0; f < NF; ++f)
+#pragma unroll
+                for (int e = 0; e < NF; ++e) blk[f][e] = fmaf(xg[f], xh[e], blk[f][e]);
+        }
+        // one row at a time (the compiler would otherwise hoist all 36 loads)
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+#pragma unroll
+            for (int e = 0; e < NF; ++e) {
+                float2 a = acc_s[f * NF + e][t];
+                two_sum_acc(a.x, a.y, blk[f][e]);
+                acc_s[f * NF + e][t] = a;
+            }
+            asm volatile("" ::: "memory");
+        }
+    }
+    const long long o = boff[b];
+    const long long ot = boff[btrans[b]];
+#pragma unroll 1
+    for (int f = 0; f < NF; ++f)
+#pragma unroll 1
+        for (int e = 0; e < NF; ++e) {
+            float2 a = acc_s[f * NF + e][t];
+            for (int s = 16; s; s >>= 1) {
+                const float ohi = __shfl_xor_sync(0xffffffffu, a.x, s);
+                const float olo = __shfl_xor_sync(0xffffffffu, a.y, s);
+                // the same pair of operands in the same order on both lanes of a butterfly
+                float hi = lane & s ? ohi : a.x, lo = lane & s ? olo : a.y;
+                const float x = lane & s ? a.x : ohi, xlo = lane & s ? a.y : olo;
+                two_sum_acc(hi, lo, x);
+                a = make_float2(hi, lo + xlo);
+            }
+            if ((f * NF + e) % 32 != lane || f >= nfg || e >= nfh) continue;
+            const double x = (double)a.x + (double)a.y;
+            Hblk[o + f * nfh + e] = Tblk[o + f * nfh + e] + x * dV;
+            if (h != g) Hblk[ot + e * nfg + f] = Tblk[ot + e * nfg + f] + x * dV;
+        }
+}
+
+bool assemble_h32_supported(const BlockPattern& bp) { return bp.nfmax <= 6; }
+
+int assemble_h32(const BlockPattern& bp, const Supports& sp, const double* Tblk, const double* v, double dV,
+                 double* Hblk, cudaStream_t s) {
+    if (!sp.sval32 || !sp.vslot || bp.nfmax > 6) {
+        lres_set_error("FP32 H(v) assembly needs the FP32 basis values and at most 6 functions per atom");
+        return LRES_ESTATE;
+    }
+    if (!bp.npair) return LRES_OK;
+    if (sp.nslot)
+        slot_potential_kernel<<<(unsigned)((sp.nslot + 255) / 256), 256, 0, s>>>(sp.nslot, sp.sgrid, v, sp.vslot);
+    LRES_CUDA_TRY(cudaGetLastError());
+    const int threads = kAsmThreads;
+    const int blocks = (int)(((long long)bp.npair * 32 + threads - 1) / threads);
+    assemble_h32_kernel<6><<<blocks, threads, 0, s>>>(bp.npair, bp.pair_blk, bp.brow, bp.bcol, bp.boff, bp.btrans,
+                                                      bp.gptr, sp.soff, sp.sval32, sp.vslot, sp.coff, sp.cslot, Tblk,
+                                                      dV, Hblk);
+    LRES_CUDA_TRY(cudaGetLastError());
+    return LRES_OK;
+}
+
+// ---------------------------------------------------------------------------
 // dense window blocks from the block-sparse storage
 // ---------------------------------------------------------------------------
 
-__global__ void gather_windows_kernel(const int* bptr, const int* bcol, const long long* boff, const int* gptr,
-                                      const int* wgrp_off, const int* wgrp, const int* wgrp_lo, const int* gloc,
-                                      int ngroups, const long long* offC, const int* n_w, const double* blk,
-                                      double* dense) {
-    const int w = blockIdx.x;
+// Every element of every dense window block, column-major, from the atom-pair blocks:
+// thread = row, a warp = 32 consecutive rows of one column (coalesced stores).  H is
+// symmetric, so element (i, j) with i in atom g, j in atom h is read from the stored block
+// (h, g) at [e][f] (e, f the functions of j in h and of i in g): consecutive rows of one atom
+// read consecutive values.  fn[i] = (local atom << 12) | (f << 6) | nf_g; btab[lg_i * nlg +
+// lg_j] = value offset of block (h, g), -1 where the atoms do not overlap.
+constexpr int kGatherCols = 32;
+
+__global__ void __launch_bounds__(256) gather_windows_kernel(const int* fn, const long long* fnoff, const int* btab,
+                                                             const long long* btoff, const int* nlg,
+                                                             const long long* offC, const int* n_w, const double* blk,
+                                                             double* dense) {
+    const int w = blockIdx.y;
     const int n = n_w[w];
+    const int j0 = blockIdx.x * kGatherCols;
+    if (j0 >= n) return;
+    const int* fw = fn + fnoff[w];
+    const int* bt = btab + btoff[w];
+    const int L = nlg[w];
     double* D = dense + offC[w];
-    const int* gl = gloc + (long long)w * ngroups;
-    const int i0 = wgrp_off[w], i1 = wgrp_off[w + 1];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
-    for (int i = i0 + warp; i < i1; i += nwarp) {
-        const int g = wgrp[i], lo = wgrp_lo[i];
-        const int nfg = gptr[g + 1] - gptr[g];
-        for (int b = bptr[g] + lane; b < bptr[g + 1]; b += 32) {
-            const int h = bcol[b];
-            const int lj = gl[h];
-            if (lj < 0) continue;
-            const int nfh = gptr[h + 1] - gptr[h];
-            const double* src = blk + boff[b];
-            for (int e = 0; e < nfh; ++e)
-                for (int f = 0; f < nfg; ++f) D[(lo + f) + (long long)(lj + e) * n] = src[f * nfh + e];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int j1 = min(n, j0 + kGatherCols);
+    for (int j = j0 + warp; j < j1; j += 8) {
+        const int mj = fw[j];
+        const int lgj = mj >> 12, e = (mj >> 6) & 63;
+        for (int i = lane; i < n; i += 32) {
+            const int mi = fw[i];
+            const int lgi = mi >> 12, f = (mi >> 6) & 63, nfg = mi & 63;
+            const int off = bt[lgi * L + lgj];
+            D[i + (long long)j * n] = off >= 0 ? blk[off + e * nfg + f] : 0.0;
         }
     }
 }
 
-int gather_windows(const BlockPattern& bp, int nwin, const int* wgrp_off, const int* wgrp, const int* wgrp_lo,
-                   const int* gloc, const long long* offC, const int* n_w, int nmax, const double* blk,
-                   double* dense, cudaStream_t s) {
-    (void)nmax;
+int gather_windows(int nwin, int nmax, const int* fn, const long long* fnoff, const int* btab, const long long* btoff,
+                   const int* nlg, const long long* offC, const int* n_w, const double* blk, double* dense,
+                   cudaStream_t s) {
     if (!nwin) return LRES_OK;
-    gather_windows_kernel<<<nwin, 256, 0, s>>>(bp.bptr, bp.bcol, bp.boff, bp.gptr, wgrp_off, wgrp, wgrp_lo, gloc,
-                                               bp.ngroups, offC, n_w, blk, dense);
+    if (nwin > 65535) {
+        lres_set_error("window gather supports at most 65535 windows (got %d)", nwin);
+        return LRES_EINVAL;
+    }
+    const dim3 grid((unsigned)((nmax + kGatherCols - 1) / kGatherCols), (unsigned)nwin);
+    gather_windows_kernel<<<grid, 256, 0, s>>>(fn, fnoff, btab, btoff, nlg, offC, n_w, blk, dense);
     LRES_CUDA_TRY(cudaGetLastError());
     return LRES_OK;
 }

@@ -73,6 +73,8 @@ struct Supports {
     long long* soff = nullptr;        // [ngroups+1] slot range of each group
     int* sgrid = nullptr;             // [nslot] grid index of each slot
     double* sval = nullptr;           // [nslot * 8] basis values, 8 per slot (zero padded)
+    float* sval32 = nullptr;          // the same in FP32 (mixed precision only)
+    float* vslot = nullptr;           // [nslot] FP32 potential at each slot (mixed H(v) scratch)
     long long ncommon = 0;
     long long* coff = nullptr;        // [npair+1] common-point range of each pair
     int2* cslot = nullptr;            // [ncommon] (slot in g, slot in h)
@@ -83,9 +85,13 @@ int pair_common_points(const BlockPattern& bp, Supports& sp, int ngroups, const 
                        const std::vector<int>& pair_h, cudaStream_t s);
 int assemble_h(const BlockPattern& bp, const Supports& sp, const double* Tblk, const double* v, double dV,
                double* Hblk, cudaStream_t s);
-int gather_windows(const BlockPattern& bp, int nwin, const int* wgrp_off, const int* wgrp, const int* wgrp_lo,
-                   const int* gloc, const long long* offC, const int* n_w, int nmax, const double* blk,
-                   double* dense, cudaStream_t s);
+bool assemble_h32_supported(const BlockPattern& bp);
+int assemble_h32(const BlockPattern& bp, const Supports& sp, const double* Tblk, const double* v, double dV,
+                 double* Hblk, cudaStream_t s);
+// Dense window blocks (column-major, every element written) from the atom-pair blocks.
+int gather_windows(int nwin, int nmax, const int* fn, const long long* fnoff, const int* btab, const long long* btoff,
+                   const int* nlg, const long long* offC, const int* n_w, const double* blk, double* dense,
+                   cudaStream_t s);
 int build_F(int nwin, const long long* Xp, const int* Xi, const double* Xv, const int* group_of_fn,
             const int* gptr, const int* gloc, int ngroups, const long long* Ooff, const long long* Oflat,
             const long long* offF, const int* m_w, int mmax, double* F, cudaStream_t s);
@@ -108,14 +114,24 @@ int pole_sums(int nwin, const long long* offQ, const int* m_w, const long long* 
               double* dens, double* n_w, double* e_w, cudaStream_t s);
 
 // Multi-shift tridiagonal route (tridiag.cu): R = float (fp32) or double.
-int tri_pick_nb(bool fp32, int nmax, size_t smem_budget, int cfg, int* nb, int* nt, int* nb_apply, int* rpt,
-                int* ldv);
+// Tile configuration of the tridiagonal route for windows of at most nmax functions.
+struct TriPick {
+    int nb = 0, nt = 0;        // reduction panel width and threads
+    int rres = 0;              // 1: the reduction holds each window in shared memory (FP32)
+    int nb_apply = 0;          // row application panel width
+    int rpt = 1;               // rows per thread of the row-per-thread application; 0: resident rows
+    int arows = 0;             // rows per application item
+    int ldv = 0;               // shared vector length (multiple of 32, >= nmax)
+    long long tstride = 0;     // T-factor elements per window (resident application)
+};
+int tri_pick(bool fp32, int nmax, size_t smem_budget, int cfg, TriPick* out);
 int tri_reduce(bool fp32, int nwin, const int* order, int* counter, const int* n_w, const long long* offC,
                const long long* offA, const long long* offN, const void* H, void* A, void* d, void* e, void* tau,
-               int* status, int nb, int nt, int ldv, size_t smem_budget, cudaStream_t s);
+               int* status, const TriPick& pk, int nmax, size_t smem_budget, cudaStream_t s);
+// tfactors: form the T factors of every (window, panel) first (once per Hamiltonian)
 int tri_apply(bool fp32, int nitems, const int4* items, const int* n_w, const int* m_w, const long long* offA,
               const long long* offN, const long long* offF, const void* A, const void* tau, const void* F, void* Y,
-              int nb, int rpt, int ldv, cudaStream_t s);
+              const TriPick& pk, int nwin, bool tfactors, void* T, size_t smem_budget, cudaStream_t s);
 int tri_rows_per_item(bool fp32, int P);
 int tri_pass(bool fp32, int nitems, const int4* items, int* counter, const int* n_w, const int* m_w,
              const long long* offN, const long long* offF, const long long* offQ, const long long* Oflat,

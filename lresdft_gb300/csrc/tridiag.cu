@@ -26,9 +26,15 @@
 //                      L2-resident working copy; the rank-2 updates of each panel of nb
 //                      columns are delayed (the panel's v and w vectors in shared memory)
 //                      and applied once per panel.  Algorithmic work (4/3) n^3 flops.
-//   tri_apply_kernel   one CTA per (window, block of up to 256 rows), one thread per row:
-//                      Y = F^ Q by panels in compact WY form, y <- y - ((y V) T_p) V^T.
-//                      Algorithmic work 2 m n^2 flops per window.
+//   tri_apply_res_kernel  (FP32) one CTA per (window, block of up to 128 rows) with the
+//                      rows resident in shared memory through all panels: Y = F^ Q by
+//                      panels in compact WY form, Y <- Y - ((Y V) T_p) V^T, 4 x 4 register
+//                      tiles.  Algorithmic work 2 m n^2 flops per window.
+//   tri_tfactor_kernel one CTA per (window, panel): the T_p of the compact WY form, once
+//                      per Hamiltonian for all row sets.
+//   tri_apply_kernel   one CTA per (window, block of up to 256 rows), one thread per row,
+//                      the rows re-read from global memory per panel (FP64 path, and the
+//                      configurations without resident rows).
 //   tri_pass_kernel    one CTA per (window, batch of rows) from a work queue: thread =
 //                      (pole, rows); the pivot recurrence of its pole is shared by its rows,
 //                      the row values staged in shared memory by asynchronous copies; the
@@ -72,6 +78,16 @@ __device__ __forceinline__ R block_sum(R x, R* red) {
     for (int w = 1; w < NT / 32; ++w) s += red[w];
     return s;
 }
+
+template <class R>
+__device__ __forceinline__ void cp_async4(R* dst, const R* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    if constexpr (sizeof(R) == 8) asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src));
+    else asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src));
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 constexpr int kAppRows = 256;                 // rows of one item of the apply kernel
 
@@ -370,6 +386,233 @@ __global__ void __launch_bounds__(NT) tri_reduce_kernel(TriReduceParams<R> p) {
 }
 
 // ---------------------------------------------------------------------------
+// Householder tridiagonalisation with the window resident in shared memory (FP32)
+// ---------------------------------------------------------------------------
+//
+// The lower triangle of the window (packed by columns: column c holds rows c..n-1 from
+// colstart(c) = c n - c (c - 1) / 2) stays in shared memory for the whole reduction, so
+// p = A v and the panel updates never leave the SM.  p_i = sum_k A_ik v_k reads row i of
+// the lower triangle up to the diagonal and column i below it: along one merged loop the
+// address steps by n - k - 1 while k < i and by 1 after, so every row costs the same
+// n - j - 1 loads and no lane diverges; two threads share a row (halves of k), their
+// partial sums added in a fixed order.  Each sum runs in blocks of 32 terms from zero.
+// One CTA per window (work queue, largest first), windows up to kResReduceMaxN functions.
+
+constexpr int kResReduceNT = 640;
+constexpr int kResReduceMaxN = kResReduceNT / 2 + 1;    // two threads per row of p = A v
+
+__host__ __device__ inline long long res_colstart(int c, int n) {
+    return (long long)c * n - (long long)c * (c - 1) / 2;
+}
+
+inline size_t res_reduce_smem_elems(int nb, int ldv, int nmax) {
+    return (size_t)nmax * (nmax + 1) / 2 + 2 * (size_t)nb * ldv + 3 * (size_t)ldv + 64 + kResReduceNT / 32;
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT, 1) tri_reduce_res_kernel(TriReduceParams<float> p, int nmax) {
+    constexpr int NW = NT / 32;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int ldv = p.ldv, nb = p.nb;
+    float* const Vs = reinterpret_cast<float*>(smem_raw);            // [nb][ldv]
+    float* const Ws = Vs + (size_t)nb * ldv;                         // [nb][ldv]
+    float* const cv = Ws + (size_t)nb * ldv;                         // [ldv] current column
+    float* const pv = cv + ldv;                                      // [ldv] p = tau (A v)
+    float* const ph = pv + ldv;                                      // [ldv] second half of A v
+    float* const dots = ph + ldv;                                    // [64]
+    float* const red = dots + 64;                                    // [NW]
+    float* const Ls = red + NW;                                      // packed lower triangle
+    __shared__ int item_sh;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+    for (;;) {
+        if (tid == 0) item_sh = atomicAdd(p.counter, 1);
+        __syncthreads();
+        const int it = item_sh;
+        if (it >= p.nwin) return;
+        const int w = p.order[it];
+        const int n = p.n_w[w];
+        if (n > ldv || n > nmax || n < 1) {
+            if (tid == 0) atomicOr(p.status, ST_BAD_SHAPE);
+            __syncthreads();
+            continue;
+        }
+        const long long ld = (n + 3) & ~3;
+        const float* H = p.H + p.offC[w];
+        float* A = p.A + p.offA[w];
+        float* dw = p.d + p.offN[w];
+        float* ew = p.e + p.offN[w];
+        float* tw = p.tau + p.offN[w];
+
+        // ---- the lower triangle of H into Ls (warp per column, rows along the lanes)
+        for (int c = warp; c < n; c += NW) {
+            const long long cs = res_colstart(c, n);
+            for (int r = c + lane; r < n; r += 32) cp_async4(Ls + cs + (r - c), H + r + (long long)c * n);
+        }
+        cp_commit();
+        cp_wait<0>();
+        __syncthreads();
+
+        for (int j0 = 0; j0 < n - 2; j0 += nb) {
+            const int nbp = min(nb, n - 2 - j0);
+            for (int jj = 0; jj < nbp; ++jj) {
+                const int j = j0 + jj;
+                // (a) column j of the current matrix, rows >= j: panel-start values minus
+                //     the pending rank-2 updates; squares of rows >= j+2
+                float part = 0.0f;
+                {
+                    const int i = j + tid;
+                    if (i < n) {
+                        float c = Ls[res_colstart(j, n) + (i - j)];
+                        for (int l = 0; l < jj; ++l)
+                            c -= Vs[l * ldv + i] * Ws[l * ldv + j] + Ws[l * ldv + i] * Vs[l * ldv + j];
+                        cv[i] = c;
+                        if (i >= j + 2) part = c * c;
+                    }
+                }
+                // (b) reflector H_j = I - tau v v^T, v_{j+1} = 1, mapping rows j+1.. of the
+                //     column onto beta e_{j+1}
+                const float s2 = block_sum<NT>(part, red);    // its barriers also publish cv
+                const float alpha = cv[j + 1];
+                float beta = alpha, tau = 0.0f, scal = 0.0f;
+                if (s2 > 0.0f) {
+                    const float nrm = sqrtf(alpha * alpha + s2);
+                    beta = alpha >= 0.0f ? -nrm : nrm;
+                    tau = (beta - alpha) / beta;
+                    scal = 1.0f / (alpha - beta);
+                }
+                if (tid == 0) {
+                    dw[j] = cv[j];
+                    ew[j] = beta;
+                    tw[j] = tau;
+                    if (!isfinite(beta) || !isfinite(cv[j])) atomicOr(p.status, ST_ZERO_PIVOT);
+                }
+                for (int i = tid; i < ldv; i += NT) {
+                    float vi = 0.0f;
+                    if (i == j + 1) vi = 1.0f;
+                    else if (i > j + 1 && i < n) vi = cv[i] * scal;
+                    Vs[jj * ldv + i] = vi;
+                    if (i > j + 1 && i < n) A[i + (long long)j * ld] = vi;   // kept for Y = F^ Q
+                }
+                __syncthreads();
+                // (c) W^T v, V^T v (warp per product) and A v on rows j+1..n-1 from the
+                //     panel-start matrix (two threads per row, halves of k)
+                for (int q = warp; q < 2 * jj; q += NW) {
+                    const float* X = q < jj ? Ws + (size_t)q * ldv : Vs + (size_t)(q - jj) * ldv;
+                    float acc = 0.0f;
+                    for (int i = j + 1 + lane; i < n; i += 32) acc += X[i] * Vs[jj * ldv + i];
+                    acc = warp_sum(acc);
+                    if (lane == 0) dots[q] = acc;
+                }
+                {
+                    const int nk = n - j - 1;                 // columns (and rows) j+1..n-1
+                    const int row = tid >> 1, half = tid & 1;
+                    if (row < nk) {
+                        const int i = j + 1 + row;
+                        const int kmid = j + 1 + (nk + 1) / 2;
+                        const int ka = half ? kmid : j + 1, kz = half ? n : kmid;
+                        const float* vv = Vs + (size_t)jj * ldv;
+                        long long addr = ka <= i ? res_colstart(ka, n) + (i - ka) : res_colstart(i, n) + (ka - i);
+                        float acc = 0.0f;
+                        for (int kb = ka; kb < kz; kb += 32) {
+                            const int ke = min(kz, kb + 32);
+                            float c = 0.0f;
+#pragma unroll 8
+                            for (int k = kb; k < ke; ++k) {
+                                c = fmaf(Ls[addr], vv[k], c);
+                                addr += k < i ? (n - k - 1) : 1;
+                            }
+                            acc += c;
+                        }
+                        if (half) ph[i] = acc;
+                        else pv[i] = acc;
+                    }
+                }
+                __syncthreads();
+                // (d) p *= tau (with the pending updates), K = tau/2 p.v, w = p - K v
+                float partK = 0.0f;
+                {
+                    const int i = j + 1 + tid;
+                    if (i < n) {
+                        float pi = pv[i] + ph[i];
+                        for (int l = 0; l < jj; ++l) pi -= Vs[l * ldv + i] * dots[l] + Ws[l * ldv + i] * dots[jj + l];
+                        pi *= tau;
+                        pv[i] = pi;
+                        partK = pi * Vs[jj * ldv + i];
+                    }
+                }
+                const float K = 0.5f * tau * block_sum<NT>(partK, red);
+                for (int i = tid; i < ldv; i += NT)
+                    Ws[jj * ldv + i] = (i > j && i < n) ? pv[i] - K * Vs[jj * ldv + i] : 0.0f;
+                __syncthreads();
+            }
+            // ---- trailing update of the lower triangle: L -= V W^T + W V^T on columns >= t0,
+            //      one quad of rows x one quad of columns per thread (the quads of the lower
+            //      block triangle); v, w of both quads from shared memory as 16-byte vectors
+            const int t0 = j0 + nbp;
+            if (t0 < n) {
+                const int q0 = t0 & ~3;
+                const int nq = (ld - q0) >> 2;
+                const int ntile = nq * (nq + 1) / 2;
+                for (int tile = tid; tile < ntile; tile += NT) {
+                    int qi = 0, qc = tile;                     // tile-th quad pair (qc <= qi)
+                    {
+                        // qi = floor((sqrt(8 tile + 1) - 1) / 2), corrected for rounding
+                        qi = (int)((sqrtf(8.0f * tile + 1.0f) - 1.0f) * 0.5f);
+                        while ((qi + 1) * (qi + 2) / 2 <= tile) ++qi;
+                        while (qi * (qi + 1) / 2 > tile) --qi;
+                        qc = tile - qi * (qi + 1) / 2;
+                    }
+                    const int i = q0 + 4 * qi, c0 = q0 + 4 * qc;
+                    float acc[4][4];
+#pragma unroll
+                    for (int c = 0; c < 4; ++c)
+#pragma unroll
+                        for (int r = 0; r < 4; ++r) acc[c][r] = 0.0f;
+                    for (int l = 0; l < nbp; ++l) {
+                        float vi[4], wi[4], vk[4], wk[4];
+                        ld4(Vs + (size_t)l * ldv + i, vi);
+                        ld4(Ws + (size_t)l * ldv + i, wi);
+                        ld4(Vs + (size_t)l * ldv + c0, vk);
+                        ld4(Ws + (size_t)l * ldv + c0, wk);
+#pragma unroll
+                        for (int c = 0; c < 4; ++c)
+#pragma unroll
+                            for (int r = 0; r < 4; ++r) acc[c][r] = fmaf(vi[r], wk[c], fmaf(wi[r], vk[c], acc[c][r]));
+                    }
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        const int col = c0 + c;
+                        if (col < t0 || col >= n) continue;
+                        const long long cs = res_colstart(col, n) - col;
+#pragma unroll
+                        for (int r = 0; r < 4; ++r)
+                            if (i + r >= col && i + r < n) Ls[cs + i + r] -= acc[c][r];
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        // ---- the last (at most 2 x 2) block, fully updated
+        if (tid == 0) {
+            if (n >= 2) {
+                dw[n - 2] = Ls[res_colstart(n - 2, n)];
+                ew[n - 2] = Ls[res_colstart(n - 2, n) + 1];
+                dw[n - 1] = Ls[res_colstart(n - 1, n)];
+                tw[n - 2] = 0.0f;
+                tw[n - 1] = 0.0f;
+                ew[n - 1] = 0.0f;
+            } else {
+                dw[0] = Ls[0];
+                tw[0] = 0.0f;
+                ew[0] = 0.0f;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Y = F^ Q: the rows through the reflectors, compact WY per panel
 // ---------------------------------------------------------------------------
 
@@ -564,6 +807,255 @@ __global__ void __launch_bounds__(NT, RPT == 1 && NB <= 16 ? 3 : 1) tri_apply_ke
 }
 
 // ---------------------------------------------------------------------------
+// Y = F^ Q with the item's rows resident in shared memory (FP32)
+// ---------------------------------------------------------------------------
+//
+// The rows of one item (at most kResRows) stay in shared memory through all panels, so Y
+// crosses to global memory once per launch instead of once per panel.  Per panel of NB
+// reflectors: S = Y V (a thread = 4 rows x 4 reflectors; a warp = 8 row quads x 4 reflector
+// quads, so that every 16-byte shared load serves a broadcast or one conflict-free
+// wavefront), S <- S T (same tiles), Y <- Y - S V^T (a thread = 4 rows x 4 columns; a warp =
+// 8 row quads x 4 column quads).  The T factor of every (window, panel) is formed once per
+// Hamiltonian by tri_tfactor_kernel.
+
+constexpr int kResRows = 128;                 // rows of an item of the resident application
+constexpr int kResNT = 256;
+
+// Staged panel: rows of NB values v_l[k]; the 16-byte groups of row kk permuted by XOR with
+// kk / 4, so that rows 4 apart (one per column quad of a warp) hit different banks.
+template <int NB>
+__device__ __forceinline__ int res_index(int kk, int l) {
+    constexpr int NG = NB / 4;
+    return kk * NB + ((((l >> 2) ^ (kk >> 2)) & (NG - 1)) << 2) + (l & 3);
+}
+
+// v_l (l < nbp) on the panel rows kk = 0..nk-1 (window row j0+1+kk), v_l = 1 on row j0+l+1,
+// zero above; reads run down the reflector columns (coalesced).
+// The reflector values go by asynchronous copies (all of a thread's copies in flight at
+// once), the zeros and ones by plain stores; the caller waits (cp_wait) before the barrier.
+template <int NT, int NB>
+__device__ __forceinline__ void res_stage(float* Vs, const float* Aw, long long ld, int j0, int nbp, int nk) {
+    for (int idx = threadIdx.x; idx < nk * NB; idx += NT) {
+        const int l = idx / nk, kk = idx % nk, k = j0 + 1 + kk;
+        const int j = j0 + l;
+        float* dst = Vs + res_index<NB>(kk, l);
+        if (l < nbp && k > j + 1) cp_async4(dst, Aw + k + (long long)j * ld);
+        else *dst = (l < nbp && k == j + 1) ? 1.0f : 0.0f;
+    }
+    cp_commit();
+}
+
+struct TriTParams {
+    int nwin;
+    int maxp;                // panels per window at most
+    const int* n_w;
+    const long long* offA;
+    const long long* offN;
+    const float* A;
+    const float* tau;
+    float* T;                // [window][panel][NB][NB], upper triangular
+    long long tstride;       // per window
+    int ldv;
+};
+
+// T of the compact WY form of one panel, Q_p = I - V T V^T: T_ll = tau_l,
+// T[0:l, l] = -tau_l T[0:l, 0:l] (V^T V)[0:l, l].  One CTA per (window, panel).
+template <int NB>
+__global__ void __launch_bounds__(128) tri_tfactor_kernel(TriTParams p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float* const Vs = reinterpret_cast<float*>(smem_raw);      // [ldv][NB]
+    float* const Gm = Vs + (size_t)p.ldv * NB;                  // [NB][NB]
+    float* const Tm = Gm + NB * NB;                              // [NB][NB]
+    const int w = blockIdx.x / p.maxp, panel = blockIdx.x % p.maxp;
+    const int n = p.n_w[w];
+    const int j0 = panel * NB;
+    if (n > p.ldv || j0 >= n - 2) return;
+    const int tid = threadIdx.x;
+    const int nbp = min(NB, n - 2 - j0), nk = n - j0 - 1;
+    const long long ld = (n + 3) & ~3;
+    res_stage<128, NB>(Vs, p.A + p.offA[w], ld, j0, nbp, nk);
+    cp_wait<0>();
+    __syncthreads();
+    for (int q = tid; q < NB * NB / 4; q += 128) {
+        const int a0 = 2 * (q / (NB / 2)), b0 = 2 * (q % (NB / 2));
+        float g00 = 0.0f, g01 = 0.0f, g10 = 0.0f, g11 = 0.0f;
+        if (b0 + 1 > a0) {
+            for (int kk = 0; kk < nk; ++kk) {
+                const float va0 = Vs[res_index<NB>(kk, a0)], va1 = Vs[res_index<NB>(kk, a0 + 1)];
+                const float vb0 = Vs[res_index<NB>(kk, b0)], vb1 = Vs[res_index<NB>(kk, b0 + 1)];
+                g00 = fmaf(va0, vb0, g00);
+                g01 = fmaf(va0, vb1, g01);
+                g10 = fmaf(va1, vb0, g10);
+                g11 = fmaf(va1, vb1, g11);
+            }
+        }
+        Gm[a0 * NB + b0] = g00;
+        Gm[a0 * NB + b0 + 1] = g01;
+        Gm[(a0 + 1) * NB + b0] = g10;
+        Gm[(a0 + 1) * NB + b0 + 1] = g11;
+    }
+    __syncthreads();
+    const float* tw = p.tau + p.offN[w];
+    if (tid < 32) {
+        for (int l = 0; l < NB; ++l) {
+            const float tl = l < nbp ? tw[j0 + l] : 0.0f;
+            for (int a = tid; a < NB; a += 32) {
+                float val = 0.0f;
+                if (a < l) {
+                    float sacc = 0.0f;
+                    for (int b = a; b < l; ++b) sacc = fmaf(Tm[a * NB + b], Gm[b * NB + l], sacc);
+                    val = -tl * sacc;
+                } else if (a == l) {
+                    val = tl;
+                }
+                Tm[a * NB + l] = val;
+            }
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+    float* Tw = p.T + (long long)w * p.tstride + (long long)panel * NB * NB;
+    for (int i = tid; i < NB * NB; i += 128) Tw[i] = Tm[i];
+}
+
+inline size_t res_smem_bytes(int nb, int ldv, int rows) {
+    return sizeof(float) * ((size_t)ldv * rows + (size_t)ldv * nb + (size_t)nb * rows + (size_t)nb * nb);
+}
+
+template <int NB>
+__global__ void __launch_bounds__(kResNT, 1) tri_apply_res_kernel(TriApplyParams<float> p, const float* Tg,
+                                                                  long long tstride, int rows) {
+    constexpr int NG = NB / 4;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int ldv = p.ldv;
+    float* const Ys = reinterpret_cast<float*>(smem_raw);       // [ldv][rows]: Y[r][k] at Ys[k * rows + r]
+    float* const Vs = Ys + (size_t)ldv * rows;                   // [ldv][NB], res_index layout
+    float* const Ss = Vs + (size_t)ldv * NB;                     // [NB][rows]: S[r][l] at Ss[l * rows + r]
+    float* const Tm = Ss + (size_t)NB * rows;                    // [NB][NB]
+    const int4 item = p.items[blockIdx.x];
+    const int w = item.x, r0 = item.y, nr = item.z;
+    const int n = p.n_w[w], m = p.m_w[w];
+    if (n > ldv || nr > rows) return;                           // flagged by the reduction / never built
+    const long long ld = (n + 3) & ~3;
+    const float* Aw = p.A + p.offA[w];
+    const float* Fw = p.F + p.offF[w] + r0;
+    float* Yw = p.Y + p.offF[w] + r0;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int rq = (nr + 31) / 32;                               // groups of 8 row quads
+    for (int idx = tid; idx < n * rq * 32; idx += kResNT) {
+        const int k = idx / (rq * 32), r = idx % (rq * 32);
+        if (r < nr) cp_async4(Ys + (size_t)k * rows + r, Fw + r + (long long)k * m);
+        else Ys[(size_t)k * rows + r] = 0.0f;
+    }
+    cp_commit();
+    const int rt_l = lane & 7, ct_l = lane >> 3;                 // lane: row quad, reflector / column quad
+    for (int j0 = 0; j0 < n - 2; j0 += NB) {
+        const int nbp = min(NB, n - 2 - j0);
+        const int nk = n - j0 - 1;
+        const float* Tp = Tg + (long long)w * tstride + (long long)(j0 / NB) * NB * NB;
+        __syncthreads();                                         // the previous panel is consumed
+        res_stage<kResNT, NB>(Vs, Aw, ld, j0, nbp, nk);
+        for (int i = tid; i < NB * NB; i += kResNT) cp_async4(Tm + i, Tp + i);
+        cp_commit();
+        cp_wait<0>();                                            // Y (first panel), V, T
+        __syncthreads();
+        const int nw1 = rq * (NB / 16);                          // warp tiles of S
+        // S = Y V over the panel rows
+        for (int wt = warp; wt < nw1; wt += kResNT / 32) {
+            const int rt = (wt % rq) * 8 + rt_l, lt = (wt / rq) * 4 + ct_l;
+            float acc[4][4] = {};
+            const float* yp = Ys + (size_t)(j0 + 1) * rows + 4 * rt;
+#pragma unroll 4
+            for (int kk = 0; kk < nk; ++kk) {
+                const float4 y = *reinterpret_cast<const float4*>(yp + (size_t)kk * rows);
+                const float4 v = *reinterpret_cast<const float4*>(Vs + kk * NB + ((lt ^ (kk >> 2)) & (NG - 1)) * 4);
+                const float yy[4] = {y.x, y.y, y.z, y.w}, vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(yy[i], vv[j], acc[i][j]);
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                *reinterpret_cast<float4*>(Ss + (size_t)(4 * lt + j) * rows + 4 * rt) =
+                    make_float4(acc[0][j], acc[1][j], acc[2][j], acc[3][j]);
+        }
+        __syncthreads();
+        // S <- S T (T upper triangular)
+        float st[4][4] = {};
+        int st_rt = -1, st_bt = 0;
+        if (warp < nw1) {                                        // nw1 <= 8: one tile per warp
+            st_rt = (warp % rq) * 8 + rt_l;
+            st_bt = (warp / rq) * 4 + ct_l;
+            const int amax = min(NB, 4 * st_bt + 4);
+            for (int a = 0; a < amax; ++a) {
+                const float4 s = *reinterpret_cast<const float4*>(Ss + (size_t)a * rows + 4 * st_rt);
+                const float4 tt = *reinterpret_cast<const float4*>(Tm + a * NB + 4 * st_bt);
+                const float ss[4] = {s.x, s.y, s.z, s.w}, t4[4] = {tt.x, tt.y, tt.z, tt.w};
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) st[i][j] = fmaf(ss[i], t4[j], st[i][j]);
+            }
+        }
+        __syncthreads();
+        if (st_rt >= 0) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                *reinterpret_cast<float4*>(Ss + (size_t)(4 * st_bt + j) * rows + 4 * st_rt) =
+                    make_float4(st[0][j], st[1][j], st[2][j], st[3][j]);
+        }
+        __syncthreads();
+        // Y <- Y - S V^T on the panel rows
+        const int nw3 = rq * ((nk + 15) / 16);
+        for (int wt = warp; wt < nw3; wt += kResNT / 32) {
+            const int rt = (wt % rq) * 8 + rt_l, kt = (wt / rq) * 4 + ct_l;
+            float acc[4][4] = {};                                // [row][column]
+#pragma unroll
+            for (int lc = 0; lc < NG; ++lc) {
+                float s[4][4], v[4][4];                          // s[l][row], v[column][l]
+#pragma unroll
+                for (int jj = 0; jj < 4; ++jj) {
+                    const float4 x = *reinterpret_cast<const float4*>(Ss + (size_t)(4 * lc + jj) * rows + 4 * rt);
+                    s[jj][0] = x.x; s[jj][1] = x.y; s[jj][2] = x.z; s[jj][3] = x.w;
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int kk = 4 * kt + q;
+                    const float4 x = *reinterpret_cast<const float4*>(Vs + kk * NB + ((lc ^ kt) & (NG - 1)) * 4);
+                    v[q][0] = x.x; v[q][1] = x.y; v[q][2] = x.z; v[q][3] = x.w;
+                }
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+#pragma unroll
+                        for (int jj = 0; jj < 4; ++jj) acc[i][q] = fmaf(s[jj][i], v[q][jj], acc[i][q]);
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int kk = 4 * kt + q;
+                if (kk < nk) {
+                    float4* yp = reinterpret_cast<float4*>(Ys + (size_t)(j0 + 1 + kk) * rows + 4 * rt);
+                    float4 y = *yp;
+                    y.x -= acc[0][q];
+                    y.y -= acc[1][q];
+                    y.z -= acc[2][q];
+                    y.w -= acc[3][q];
+                    *yp = y;
+                }
+            }
+        }
+    }
+    cp_wait<0>();                                                // (no panel: the rows as loaded)
+    __syncthreads();
+    for (int idx = tid; idx < n * rq * 32; idx += kResNT) {
+        const int k = idx / (rq * 32), r = idx % (rq * 32);
+        if (r < nr) Yw[r + (long long)k * m] = Ys[(size_t)k * rows + r];
+    }
+}
+
+// ---------------------------------------------------------------------------
 // shifted tridiagonal solves at all poles, fused with the pole sums
 // ---------------------------------------------------------------------------
 
@@ -591,16 +1083,6 @@ struct TriPassParams {
     int ldv;
 };
 
-template <class R>
-__device__ __forceinline__ void cp_async4(R* dst, const R* src) {
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-    if constexpr (sizeof(R) == 8) asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src));
-    else asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src));
-}
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-template <int N>
-__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
-
 constexpr int kPassNT = 256;
 constexpr int kPassIC = 32;                   // steps per staged chunk
 constexpr int kPassMaxRows = 256;             // rows per pass item at most
@@ -616,6 +1098,37 @@ inline size_t pass_smem_bytes(int elem, int P, int RR, int ldv) {
     return sizeof(double2) * (size_t)RB * P + (size_t)elem * (2 * (size_t)ldv + 2 * (size_t)kPassIC * RB);
 }
 
+// Unevaluated pairs of floats (hi + lo): the row sums of the FP32 pass and its pole
+// weighting, with the rounding errors kept (Knuth's TwoSum, FMA-exact products), so that no
+// FP64 arithmetic runs per item (GB300's FP64 rate is 1/64 of FP32).
+__device__ __forceinline__ void df_add(float& hi, float& lo, float x) {
+    const float s = hi + x;
+    const float bp = s - hi;
+    lo += (hi - (s - bp)) + (x - bp);
+    hi = s;
+}
+__device__ __forceinline__ void df_mul(float ah, float al, float bh, float bl, float& ph, float& pl) {
+    ph = ah * bh;
+    pl = fmaf(ah, bh, -ph);
+    pl = fmaf(ah, bl, pl);
+    pl = fmaf(al, bh, pl);
+}
+// Re((ar + i ai)(qr + i qi)) as a pair
+__device__ __forceinline__ void df_cre(const float4& a, float qrh, float qrl, float qih, float qil, float& h,
+                                       float& l) {
+    float p1h, p1l, p2h, p2l;
+    df_mul(a.x, a.y, qrh, qrl, p1h, p1l);
+    df_mul(a.z, a.w, qih, qil, p2h, p2l);
+    h = p1h;
+    l = p1l;
+    df_add(h, l, -p2h);
+    l -= p2l;
+}
+__device__ __forceinline__ float4 df_split(double2 a) {
+    const float rh = (float)a.x, ih = (float)a.y;
+    return make_float4(rh, (float)(a.x - (double)rh), ih, (float)(a.y - (double)ih));
+}
+
 template <class R, int NT, int RR>
 __global__ void __launch_bounds__(NT) tri_pass_kernel(TriPassParams<R> p) {
     using C = typename Cplx<R>::T;
@@ -624,7 +1137,10 @@ __global__ void __launch_bounds__(NT) tri_pass_kernel(TriPassParams<R> p) {
     const int P = p.P;
     const int G = pass_groups(P, RR);              // row groups
     const int RB = G * RR;                         // rows per item
-    double2* const red = reinterpret_cast<double2*>(smem_raw);      // [RB][P]
+    constexpr bool kDF = sizeof(R) == 4;           // FP32 path: float pairs for the sums
+    // [RB][P] weighted quadratic forms: (n, e) as double2, or (n_hi, n_lo, e_hi, e_lo)
+    double2* const red = reinterpret_cast<double2*>(smem_raw);
+    float4* const redf = reinterpret_cast<float4*>(smem_raw);
     R* const ds = reinterpret_cast<R*>(red + (size_t)RB * P);         // [ldv]
     R* const es = ds + p.ldv;                                         // [ldv]
     R* const yb = es + p.ldv;                                         // [2][IC][RB]
@@ -633,6 +1149,11 @@ __global__ void __launch_bounds__(NT) tri_pass_kernel(TriPassParams<R> p) {
     const int tid = threadIdx.x;
     const int k = tid % P, g = tid / P;
     const bool on = g < G;
+    float4 wsp = make_float4(0.f, 0.f, 0.f, 0.f), wzsp = wsp;      // w_k, w_k z_k split (FP32 path)
+    if (kDF && on) {
+        wsp = df_split(p.wq[k]);
+        wzsp = df_split(p.wzq[k]);
+    }
 
     for (;;) {
         if (tid == 0) item_sh = atomicAdd(p.counter, 1);
@@ -668,14 +1189,15 @@ __global__ void __launch_bounds__(NT) tri_pass_kernel(TriPassParams<R> p) {
 
         const C z = p.shifts[k < P ? k : 0];
         C gp = C{R(0), R(0)};                       // 1 / D_{i-1}
-        C uc[RR], pr[RR], pc[RR];
-        double2 acc[RR];
+        C uc[RR], pr[RR];
+        double2 acc[RR];                            // FP64 path: row sums
+        float4 accf[RR];                            // FP32 path: (re_hi, re_lo, im_hi, im_lo)
 #pragma unroll
         for (int u = 0; u < RR; ++u) {
             uc[u] = C{R(0), R(0)};
             pr[u] = C{R(0), R(0)};
-            pc[u] = C{R(0), R(0)};
             acc[u] = make_double2(0.0, 0.0);
+            accf[u] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
         for (int c = 0; c < nch; ++c) {
             if (c + 1 < nch) {
@@ -714,42 +1236,61 @@ __global__ void __launch_bounds__(NT) tri_pass_kernel(TriPassParams<R> p) {
                         pr[u].y = fma(sr, gp.y, fma(si, gp.x, pr[u].y));
                     }
                 }
-                // each chunk's sum is formed from zero; chunk sums are added in the working
-                // precision over 8 chunks, those sums in FP64 (GB300's FP64 rate is 1/64 of FP32)
+                // each chunk's sum is formed from zero and added to the row sums
 #pragma unroll
                 for (int u = 0; u < RR; ++u) {
-                    pc[u].x += pr[u].x;
-                    pc[u].y += pr[u].y;
-                    pr[u] = C{R(0), R(0)};
-                }
-                if ((c & 7) == 7 || c + 1 == nch) {
-#pragma unroll
-                    for (int u = 0; u < RR; ++u) {
-                        acc[u].x += (double)pc[u].x;
-                        acc[u].y += (double)pc[u].y;
-                        pc[u] = C{R(0), R(0)};
+                    if constexpr (kDF) {
+                        df_add(accf[u].x, accf[u].y, (float)pr[u].x);
+                        df_add(accf[u].z, accf[u].w, (float)pr[u].y);
+                    } else {
+                        acc[u].x += (double)pr[u].x;
+                        acc[u].y += (double)pr[u].y;
                     }
+                    pr[u] = C{R(0), R(0)};
                 }
             }
             __syncthreads();                          // buffer c & 1 is free for chunk c + 2
         }
         // pole sums: n(r) = 4 Re sum_k w_k d_k(r), e(r) = 4 Re sum_k w_k z_k d_k(r)
         if (on) {
-            const double2 a = p.wq[k], b = p.wzq[k];
+            if constexpr (kDF) {
 #pragma unroll
-            for (int u = 0; u < RR; ++u) {
-                const double qx = acc[u].x, qy = acc[u].y;
-                red[(size_t)(g * RR + u) * P + k] = make_double2(a.x * qx - a.y * qy, b.x * qx - b.y * qy);
+                for (int u = 0; u < RR; ++u) {
+                    float nh, nl, eh, el;
+                    df_cre(wsp, accf[u].x, accf[u].y, accf[u].z, accf[u].w, nh, nl);
+                    df_cre(wzsp, accf[u].x, accf[u].y, accf[u].z, accf[u].w, eh, el);
+                    redf[(size_t)(g * RR + u) * P + k] = make_float4(nh, nl, eh, el);
+                }
+            } else {
+                const double2 a = p.wq[k], b = p.wzq[k];
+#pragma unroll
+                for (int u = 0; u < RR; ++u) {
+                    const double qx = acc[u].x, qy = acc[u].y;
+                    red[(size_t)(g * RR + u) * P + k] = make_double2(a.x * qx - a.y * qy, b.x * qx - b.y * qy);
+                }
             }
         }
         __syncthreads();
         double tn = 0.0, te = 0.0;
         for (int row = tid; row < nr; row += NT) {
             double sn = 0.0, se = 0.0;
-            for (int kk = 0; kk < P; ++kk) {
-                const double2 v = red[(size_t)row * P + kk];
-                sn += v.x;
-                se += v.y;
+            if constexpr (kDF) {
+                float nh = 0.f, nl = 0.f, eh = 0.f, el = 0.f;
+                for (int kk = 0; kk < P; ++kk) {
+                    const float4 v = redf[(size_t)row * P + kk];
+                    df_add(nh, nl, v.x);
+                    nl += v.y;
+                    df_add(eh, el, v.z);
+                    el += v.w;
+                }
+                sn = (double)nh + (double)nl;
+                se = (double)eh + (double)el;
+            } else {
+                for (int kk = 0; kk < P; ++kk) {
+                    const double2 v = red[(size_t)row * P + kk];
+                    sn += v.x;
+                    se += v.y;
+                }
             }
             const double nrow = 4.0 * sn, erow = 4.0 * se;
             if (!isfinite(nrow) || !isfinite(erow)) atomicOr(p.status, ST_ZERO_PIVOT);
@@ -843,33 +1384,55 @@ __global__ void tri_mineig_kernel(int nwin, const int* n_w, const long long* off
 // ---------------------------------------------------------------------------
 
 // Tile configurations of the tridiagonal route: reduction panel width and threads, row
-// application panel width and rows per thread.  Panel widths are capped by what fits the
-// shared memory at windows of nmax.
+// application panel width, rows per thread of the row-per-thread application and whether
+// the rows stay resident in shared memory (res; FP32 only).  Panel widths are capped by
+// what fits the shared memory at windows of nmax.
 struct TriCfg {
-    int nb, nt, nba, rpt;
+    int nb, nt, nba, rpt, res, rres;     // rres: the reduction with the window in shared memory
 };
-// Measured at 1024 electrons (reduction + rows, mixed): (16, 512, 32, 1) 12.5 ms, (32, 512, 32, 1)
-// 13.0-13.9 ms, the 256-thread reductions and the two-rows-per-thread applications 14-18 ms.
-static const TriCfg kTriCfg[6] = {{16, 512, 32, 1}, {32, 512, 32, 1}, {16, 512, 16, 1},
-                                  {16, 512, 16, 4}, {16, 256, 32, 1}, {16, 512, 32, 2}};
+// Measured at 1024 electrons (reduction + rows, mixed), row-per-thread application:
+// (16, 512, 32, 1) 12.5 ms, (32, 512, 32, 1) 13.0-13.9 ms, the 256-thread reductions and the
+// two-rows-per-thread applications 14-18 ms.
+static const TriCfg kTriCfg[6] = {{16, 512, 32, 1, 1, 1}, {16, 512, 32, 1, 1, 0}, {16, 512, 32, 1, 0, 0},
+                                  {8, 512, 32, 1, 1, 1},  {16, 512, 16, 1, 1, 1}, {16, 256, 32, 1, 1, 0}};
 
-int tri_pick_nb(bool fp32, int nmax, size_t smem_budget, int cfg, int* nb, int* nt, int* nb_apply, int* rpt,
-                int* ldv) {
+int tri_pick(bool fp32, int nmax, size_t smem_budget, int cfg, TriPick* out) {
     const int el = fp32 ? 4 : 8;
-    *ldv = (std::max(nmax, 1) + 31) / 32 * 32;
+    TriPick r;
+    r.ldv = (std::max(nmax, 1) + 31) / 32 * 32;
     if (cfg < 0 || cfg >= 6) cfg = 0;
     const TriCfg& t = kTriCfg[cfg];
-    *nt = t.nt;
-    *nb = *nb_apply = 0;
+    r.nt = t.nt;
+    if (t.rres && fp32 && nmax <= kResReduceMaxN)
+        for (int b : {16, 8, 4})
+            if (b <= t.nb && !r.nb && res_reduce_smem_elems(b, r.ldv, nmax) * el <= smem_budget) {
+                r.nb = b;
+                r.nt = kResReduceNT;
+                r.rres = 1;
+            }
     for (int b : {32, 16, 8, 4})
-        if (b <= t.nb && !*nb && reduce_smem_elems(b, *ldv, t.nt) * el <= smem_budget) *nb = b;
-    for (int b : {32, 16, 8, 4})
-        if (b <= t.nba && !*nb_apply && (size_t)el * ((size_t)*ldv * b + 2 * b * b) <= smem_budget) *nb_apply = b;
-    *rpt = *nb_apply >= 16 ? t.rpt : 1;
-    if (!*nb || !*nb_apply) {
+        if (b <= t.nb && !r.nb && reduce_smem_elems(b, r.ldv, t.nt) * el <= smem_budget) r.nb = b;
+    if (t.res && fp32)
+        for (int b : {32, 16})
+            for (int rows = kResRows; rows >= 32 && !r.nb_apply; rows -= 32)
+                if (b <= t.nba && res_smem_bytes(b, r.ldv, rows) <= smem_budget) {
+                    r.nb_apply = b;
+                    r.arows = rows;
+                    r.rpt = 0;
+                }
+    if (!r.nb_apply) {
+        for (int b : {32, 16, 8, 4})
+            if (b <= t.nba && !r.nb_apply && (size_t)el * ((size_t)r.ldv * b + 2 * b * b) <= smem_budget) r.nb_apply = b;
+        r.rpt = r.nb_apply >= 16 ? t.rpt : 1;
+        r.arows = kAppRows;
+    }
+    if (!r.nb || !r.nb_apply) {
         lres_set_error("windows of %d functions exceed the shared memory of the tridiagonal reduction", nmax);
         return LRES_EINVAL;
     }
+    // T factors of the resident application: panels of nb_apply, per window
+    r.tstride = r.rpt == 0 ? (long long)(r.ldv / r.nb_apply + 1) * r.nb_apply * r.nb_apply : 0;
+    *out = r;
     return LRES_OK;
 }
 
@@ -890,12 +1453,26 @@ static int launch_reduce(const TriReduceParams<R>& p, size_t smem_budget, cudaSt
 
 int tri_reduce(bool fp32, int nwin, const int* order, int* counter, const int* n_w, const long long* offC,
                const long long* offA, const long long* offN, const void* H, void* A, void* d, void* e, void* tau,
-               int* status, int nb, int nt, int ldv, size_t smem_budget, cudaStream_t s) {
+               int* status, const TriPick& pk, int nmax, size_t smem_budget, cudaStream_t s) {
     if (!nwin) return LRES_OK;
+    const int nb = pk.nb, nt = pk.nt, ldv = pk.ldv;
     LRES_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), s));
     if (fp32) {
         TriReduceParams<float> p{nwin, order, counter, n_w, offC, offA, offN, (const float*)H, (float*)A,
                                  (float*)d, (float*)e, (float*)tau, status, nb, ldv};
+        if (pk.rres) {
+            const size_t smem = res_reduce_smem_elems(nb, ldv, nmax) * sizeof(float);
+            if (smem > smem_budget || nmax > kResReduceMaxN) {
+                lres_set_error("resident tridiagonal reduction needs %zu B of shared memory", smem);
+                return LRES_EINVAL;
+            }
+            int per_sm = 0;
+            if (int rc = prepare_kernel<tri_reduce_res_kernel<kResReduceNT>>(kResReduceNT, smem, &per_sm)) return rc;
+            const int grid = std::min(nwin, std::max(1, per_sm) * device_sms());
+            tri_reduce_res_kernel<kResReduceNT><<<grid, kResReduceNT, smem, s>>>(p, nmax);
+            LRES_CUDA_TRY(cudaGetLastError());
+            return LRES_OK;
+        }
         return nt == 512 ? launch_reduce<float, 512>(p, smem_budget, s) : launch_reduce<float, 256>(p, smem_budget, s);
     }
     TriReduceParams<double> p{nwin, order, counter, n_w, offC, offA, offN, (const double*)H, (double*)A,
@@ -930,18 +1507,52 @@ static int dispatch_apply(const TriApplyParams<R>& p, int nb, int rpt, cudaStrea
     }
 }
 
+template <int NB>
+static int launch_apply_res(const TriApplyParams<float>& p, const TriTParams& tp, int rows, size_t smem_budget,
+                            cudaStream_t s) {
+    const size_t smem_t = sizeof(float) * ((size_t)p.ldv * NB + 2 * NB * NB);
+    const size_t smem = res_smem_bytes(NB, p.ldv, rows);
+    if (smem > smem_budget || rows > kResRows || rows % 32) {
+        lres_set_error("resident row application needs %zu B of shared memory", smem);
+        return LRES_EINVAL;
+    }
+    int per_sm = 0;
+    if (tp.maxp > 0 && tp.nwin > 0) {
+        if (int rc = prepare_kernel<tri_tfactor_kernel<NB>>(128, smem_t, &per_sm)) return rc;
+        tri_tfactor_kernel<NB><<<(unsigned)tp.nwin * tp.maxp, 128, smem_t, s>>>(tp);
+        LRES_CUDA_TRY(cudaGetLastError());
+    }
+    if (int rc = prepare_kernel<tri_apply_res_kernel<NB>>(kResNT, smem, &per_sm)) return rc;
+    tri_apply_res_kernel<NB><<<p.nitems, kResNT, smem, s>>>(p, tp.T, tp.tstride, rows);
+    LRES_CUDA_TRY(cudaGetLastError());
+    return LRES_OK;
+}
+
 int tri_apply(bool fp32, int nitems, const int4* items, const int* n_w, const int* m_w, const long long* offA,
               const long long* offN, const long long* offF, const void* A, const void* tau, const void* F, void* Y,
-              int nb, int rpt, int ldv, cudaStream_t s) {
+              const TriPick& pk, int nwin, bool tfactors, void* T, size_t smem_budget, cudaStream_t s) {
     if (!nitems) return LRES_OK;
     if (fp32) {
         TriApplyParams<float> p{nitems, items, n_w, m_w, offA, offN, offF, (const float*)A, (const float*)tau,
-                                (const float*)F, (float*)Y, ldv};
-        return dispatch_apply(p, nb, rpt, s);
+                                (const float*)F, (float*)Y, pk.ldv};
+        if (pk.rpt == 0) {
+            if (!T) {
+                lres_set_error("resident row application without a T-factor buffer");
+                return LRES_ESTATE;
+            }
+            const int maxp = tfactors ? (pk.ldv + pk.nb_apply - 1) / pk.nb_apply : 0;
+            TriTParams tp{nwin, maxp, n_w, offA, offN, (const float*)A, (const float*)tau, (float*)T, pk.tstride,
+                          pk.ldv};
+            if (pk.nb_apply == 32) return launch_apply_res<32>(p, tp, pk.arows, smem_budget, s);
+            if (pk.nb_apply == 16) return launch_apply_res<16>(p, tp, pk.arows, smem_budget, s);
+            lres_set_error("resident row application: panel width %d not compiled", pk.nb_apply);
+            return LRES_EINVAL;
+        }
+        return dispatch_apply(p, pk.nb_apply, pk.rpt, s);
     }
     TriApplyParams<double> p{nitems, items, n_w, m_w, offA, offN, offF, (const double*)A, (const double*)tau,
-                             (const double*)F, (double*)Y, ldv};
-    return dispatch_apply(p, nb, rpt, s);
+                             (const double*)F, (double*)Y, pk.ldv};
+    return dispatch_apply(p, pk.nb_apply, pk.rpt, s);
 }
 
 int tri_rows_per_item(bool fp32, int P) {

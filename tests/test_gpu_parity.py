@@ -189,6 +189,35 @@ def test_mixed_precision_density_within_gate(systems, name):
     s.close()
 
 
+@pytest.mark.parametrize("name", CASES)
+def test_mixed_h_assembly_blocked_sums(systems, name):
+    """The mixed context assembles H(v) from FP32 products with FP32 sums over blocks of 32
+    common points per lane and FP64 sums of the blocks; the FP64 context in FP64.  Both
+    against the host H(v) = T + X^T diag(v) X dV (lrft/lcao3d.py:98-100) window by window:
+    FP64 to 1e-12 Ha, mixed to 1e-6 Ha (FP32 rounding of the basis values and the
+    potential), with a mean error (the drift of long FP32 sums) below 1e-8 Ha."""
+    from lresdft_gb300.autograd import window_matrices
+    g, cr, b = systems[name]
+    v = g["v"].reshape(cr.shape)
+    Hhost = b.H(v).tocsr()
+    errs = {}
+    for precision in ("fp64", "mixed"):
+        s = _solver(b, cr, g, precision=precision)
+        s.set_potential(v)
+        HW = window_matrices(s)[0].cpu().numpy()
+        off = s.window_offsets
+        d = []
+        for w, W in enumerate(s.ctx_windows):
+            n = len(W)
+            blk = HW[off[w]:off[w + 1]].reshape(n, n, order="F")
+            d.append((blk - Hhost[W][:, W].toarray()).ravel())
+        errs[precision] = np.concatenate(d)
+        s.close()
+    assert np.max(np.abs(errs["fp64"])) < 1e-12
+    assert np.max(np.abs(errs["mixed"])) < 1e-6
+    assert abs(np.mean(errs["mixed"])) < 1e-8
+
+
 def test_grid_kernels_match_oracle(systems):
     from lresdft_gb300.scf import GridOps
     from oracle import lrft_oracle as orc
@@ -258,6 +287,31 @@ def test_every_tile_configuration_matches_reference(systems, name, config):
             assert np.max(np.abs(dens - g["cold_dens"])) < 1e-10 and abs(eb - g["cold_eband"]) < 1e-9
         else:
             assert abs(eb - g["cold_eband"]) / cr.n_elec < 2e-7
+        s.close()
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("config", [0, 1, 2, 3, 4, 5])
+def test_every_tridiagonal_configuration_matches_reference(systems, name, config):
+    """Each configuration of the tridiagonal route, forced (reduction with the window in
+    shared memory or in the L2-resident working copy; row application with resident rows
+    or one row per thread; panel widths): FP64 to 1e-10 in density, mixed within the 2e-7
+    Ha/electron gate and 1e-6 in the density norm, after the potential was set and again
+    after a second potential (the T factors and row items follow the configuration)."""
+    g, cr, b = systems[name]
+    v = g["v"].reshape(cr.shape)
+    ne = cr.n_elec
+    for precision in ("fp64", "mixed"):
+        s = _solver(b, cr, g, precision, route="tridiag")
+        s.set_potential(0.5 * v)
+        s.autotune(0.0, -1.0, config=config)
+        s.set_potential(v)
+        dens, N, eb = s.pole_pass(float(g["cold_mu"]), float(g["cold_elo"]))
+        if precision == "fp64":
+            assert np.max(np.abs(dens - g["cold_dens"])) < 1e-10 and abs(eb - g["cold_eband"]) < 1e-9
+        else:
+            assert abs(eb - g["cold_eband"]) / ne < 2e-7
+            assert np.sqrt(np.sum((dens - g["cold_dens"]) ** 2) * cr.dV) / ne < 1e-6
         s.close()
 
 
