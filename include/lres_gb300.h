@@ -136,9 +136,11 @@ int lres_density_ptr(lres_ctx* ctx, const double** d_dens);
  * On the LDL^T route it is the tile configuration of the fused pole kernel, timed with full
  * passes at (mu, e_lo) (LRES_MIXED configuration 4 runs the chunk products on the tensor cores,
  * tcgen05 with a 3xTF32 split; it is timed but kept only when forced, its error being ~5x that
- * of the FP32 configurations).  On the tridiagonal route it is the pair of panel widths of the
- * reduction and of the row application with their thread layouts (six measured variants,
- * each capped by the shared memory), timed as reduction + rows (mu, e_lo unused).
+ * of the FP32 configurations).  On the tridiagonal route it selects the reduction (working
+ * copy in L2, or with LRES_MIXED the window's lower triangle in shared memory), the row
+ * application (rows resident in shared memory with LRES_MIXED, or one row per thread), their
+ * panel widths and rows per item (six measured variants, each capped by the shared memory),
+ * timed as reduction + rows (mu, e_lo unused).
  * *chosen (may be NULL) receives the choice, ms_per_config[6] (may be NULL) the measured times. */
 int lres_autotune(lres_ctx* ctx, double mu, double e_lo, int32_t force_config, int32_t* chosen,
                   double* ms_per_config, void* stream);

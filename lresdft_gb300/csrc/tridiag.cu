@@ -1389,12 +1389,15 @@ __global__ void tri_mineig_kernel(int nwin, const int* n_w, const long long* off
 // what fits the shared memory at windows of nmax.
 struct TriCfg {
     int nb, nt, nba, rpt, res, rres;     // rres: the reduction with the window in shared memory
+    int rows;                            // resident application: rows per item at most
 };
-// Measured at 1024 electrons (reduction + rows, mixed), row-per-thread application:
-// (16, 512, 32, 1) 12.5 ms, (32, 512, 32, 1) 13.0-13.9 ms, the 256-thread reductions and the
-// two-rows-per-thread applications 14-18 ms.
-static const TriCfg kTriCfg[6] = {{16, 512, 32, 1, 1, 1}, {16, 512, 32, 1, 1, 0}, {16, 512, 32, 1, 0, 0},
-                                  {8, 512, 32, 1, 1, 1},  {16, 512, 16, 1, 1, 1}, {16, 256, 32, 1, 1, 0}};
+// Measured at 1024 electrons (mixed): reduction 7.0 ms with the L2-resident working copy
+// (nb 16, 512 threads), 8.1 ms with the window in shared memory (nb 8); row application
+// 3.1 ms with resident rows (NB 32), 6.3 ms one row per thread; 256-thread reductions and
+// two or four rows per thread slower.
+static const TriCfg kTriCfg[6] = {{16, 512, 32, 1, 1, 0, 128}, {16, 512, 32, 1, 1, 1, 128},
+                                  {16, 512, 32, 1, 0, 0, 0},    {16, 512, 16, 1, 1, 0, 64},
+                                  {16, 512, 32, 1, 1, 0, 32},   {8, 512, 32, 1, 1, 1, 128}};
 
 int tri_pick(bool fp32, int nmax, size_t smem_budget, int cfg, TriPick* out) {
     const int el = fp32 ? 4 : 8;
@@ -1414,7 +1417,7 @@ int tri_pick(bool fp32, int nmax, size_t smem_budget, int cfg, TriPick* out) {
         if (b <= t.nb && !r.nb && reduce_smem_elems(b, r.ldv, t.nt) * el <= smem_budget) r.nb = b;
     if (t.res && fp32)
         for (int b : {32, 16})
-            for (int rows = kResRows; rows >= 32 && !r.nb_apply; rows -= 32)
+            for (int rows = std::min(kResRows, t.rows); rows >= 32 && !r.nb_apply; rows -= 32)
                 if (b <= t.nba && res_smem_bytes(b, r.ldv, rows) <= smem_budget) {
                     r.nb_apply = b;
                     r.arows = rows;
