@@ -42,10 +42,10 @@ WORKLOAD = dict(workload="8x8x8 H2 crystal, 1024 electrons, a=4.5, jitter U(+-0.
 SCF_ITERS = 4           # the fixed SCF window of the GPU and CPU s/iter figures
 
 
-def build_system(cells=8, assembly="native"):
+def build_system(cells=8, assembly="native", tabulation="numpy"):
     from lresdft_gb300 import system
     cr = system.jittered_h2((cells,) * 3, a=4.5, bond=1.4, pts_per_cell=8, jitter=0.1, seed=0)
-    return cr, system.LCAOBasis(cr, assembly=assembly)
+    return cr, system.LCAOBasis(cr, assembly=assembly, tabulation=tabulation)
 
 
 def read_peaks():
@@ -214,7 +214,7 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     t_setup = time.perf_counter()
-    cr, b = build_system(args.cells)
+    cr, b = build_system(args.cells, tabulation="gpu")     # GPU tabulation, native sparse assembly
     basis_s = time.perf_counter() - t_setup
     if args.cells != 8:
         WORKLOAD.update(workload=f"{args.cells}^3 H2 crystal (profiling size), {cr.n_elec} electrons",
@@ -347,11 +347,17 @@ def run_ours(args):
     nnz_h = float(b.S.nnz)
     cand = {k: breakdown[k] for k in ("pole_kernel", "transform", "tri_reduce", "tri_rows", "assemble_h", "gather")
             if k in breakdown}
+    # kernels of the chosen tridiagonal configuration (TriCfg in csrc/tridiag.cu): mixed
+    # configurations 1 and 5 reduce in shared memory, all but 2 apply with resident rows
+    mixed = args.precision == "mixed"
+    cfg = s.tile_config if isinstance(s.tile_config, int) else 0
     kernel_names = {"pole_kernel": "tri_pass_kernel" if route == "tridiag" else "ldl_left_kernel",
-                    "transform": "gemm_f32blk_kernel" if (route == "tridiag" and args.precision == "mixed")
+                    "transform": "gemm_f32blk_kernel" if (route == "tridiag" and mixed)
                     else ("gemm_f64_kernel" if args.precision == "fp64" else "gemm_df64_kernel"),
-                    "tri_reduce": "tri_reduce_kernel", "tri_rows": "tri_apply_kernel",
-                    "assemble_h": "assemble_h_kernel", "gather": "gather_windows_kernel"}
+                    "tri_reduce": "tri_reduce_res_kernel" if (mixed and cfg in (1, 5)) else "tri_reduce_kernel",
+                    "tri_rows": "tri_apply_res_kernel" if (mixed and cfg != 2) else "tri_apply_kernel",
+                    "assemble_h": "assemble_h32_kernel" if mixed else "assemble_h_kernel",
+                    "gather": "gather_windows_kernel"}
 
     def work_name(k):
         return {"pole_kernel": "pole_kernel_tri" if route == "tridiag" else "pole_kernel_ldl"}.get(k, k)
@@ -389,9 +395,10 @@ def run_ours(args):
                             "tflops_per_s": round(flops_step / (ms_step / 1e3) / 1e12, 2)},
         "clocks": clk,
         "breakdown_ms": breakdown,
+        "tile_config": {"chosen": s.tile_config, "ms_per_config": getattr(s, "tune_ms", None)},
         "extra_pass_ms": round(pass_ms, 3),
         "cuda_graph": graph_leg,
-        "setup_s": round(setup_s, 2), "basis_s": round(basis_s, 2), "accuracy": err,
+        "setup_s": round(setup_s, 2), "basis_s": round(basis_s, 2), "basis_tabulation": "gpu", "accuracy": err,
     }
 
     # FP64 path on the same potential (the target ratio is mixed vs FP64)

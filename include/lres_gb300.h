@@ -31,6 +31,7 @@
  *   lres_hartree                lrft/three_d.py:122-129
  *   lres_ion_potential          lrft/three_d.py:102-112,119 (erf part; no GTH short-range term)
  *   lres_basis_build / _fetch   the sparse assembly of LCAOBasis (lrft/lcao3d.py:86-96), on the host
+ *   lres_basis_tabulate         the tabulation loop of LCAOBasis.__init__ (lrft/lcao3d.py:61-84), on the GPU
  */
 #ifndef LRES_GB300_H
 #define LRES_GB300_H
@@ -267,6 +268,21 @@ int lres_basis_build(lres_basis** out, int64_t ngroups, const int64_t* gptr, con
 int lres_basis_fetch(const lres_basis* b, int64_t* Xp, int64_t* Xi, double* Xv, int64_t* Xrp, int64_t* Xri,
                      double* Xrv, int64_t* Sp, int64_t* Si, double* Sv, int64_t* Tp, int64_t* Ti, double* Tv);
 int lres_basis_free(lres_basis* b);
+
+/* Tabulation of the atom-centred grid basis on the GPU (lrft/lcao3d.py:61-84), the input of
+ * lres_basis_build.  Atom a at pos[3a..3a+2] has ns[a] s exponents then np[a] p exponents in
+ * exps (atoms concatenated), 1..8 functions (s: exp(-e r^2) cut(r); p: x, y, z times
+ * exp(-e r^2) cut(r); cut(r) = (1 - (r / rcut)^2)^2).  Its points are those of the cube
+ * round(R / dx) + [-ceil(rcut / dx), ceil(rcut / dx)]^3 (lexicographic) whose minimum-image
+ * distance (cell[]) is below rcut, in cube order; each function is normalised on the grid
+ * (f / sqrt(sum f^2 dV)).  The operations are the reference's, rounded in its order: the
+ * points are the same, the values differ from numpy's by CUDA's exp (a few ulp) and by the
+ * order of the normalisation sum.  Host arrays.  Two calls: idx = val = NULL fills cnt[natoms]
+ * (points per atom); then idx[sum cnt] (grid indices) and val[sum cnt * functions] (atom by
+ * atom, function by function) are filled.  Synchronous on the current device. */
+int lres_basis_tabulate(int64_t natoms, const double* pos, const int32_t* ns, const int32_t* np,
+                        const double* exps, const int64_t shape[3], const double cell[3], double dx, double rcut,
+                        double dV, int64_t* cnt, int64_t* idx, double* val);
 
 /* Grid kernels on device arrays of ng doubles (context supplies shape and cell). */
 int lres_lda_xc(lres_ctx* ctx, const double* dens, double* exc, double* vxc, void* stream);

@@ -22,7 +22,7 @@ EXPORTS = ("lres_version", "lres_last_error", "lres_ctx_create", "lres_ctx_destr
            "lres_set_route", "lres_get_route", "lres_timings", "lres_window_sums", "lres_inertia", "lres_min_eig",
            "lres_voronoi_owner", "lres_lda_xc", "lres_hartree", "lres_ion_potential", "lres_inertia_noalloc",
            "lres_set_windows", "lres_window_ptrs", "lres_adjoint", "lres_owned_gram", "lres_set_trace_rows",
-           "lres_basis_build", "lres_basis_fetch", "lres_basis_free")
+           "lres_basis_build", "lres_basis_fetch", "lres_basis_free", "lres_basis_tabulate")
 
 
 class LResError(RuntimeError):
@@ -86,6 +86,8 @@ def _load():
         "lres_basis_build": (i32, [C.POINTER(vp), i64, P64, P64, P64, PD, P64, dbl, dbl, dbl, i32, P64]),
         "lres_basis_fetch": (i32, [vp, P64, P64, PD, P64, P64, PD, P64, P64, PD, P64, P64, PD]),
         "lres_basis_free": (i32, [vp]),
+        "lres_basis_tabulate": (i32, [i64, PD, C.POINTER(C.c_int32), C.POINTER(C.c_int32), PD, P64, PD, dbl, dbl,
+                                      dbl, P64, P64, PD]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -130,6 +132,29 @@ def voronoi_owner(shape, cell, centres):
     check(lib.lres_voronoi_owner(ptr64(shape), ptrd(cell), centres.shape[0], ptrd(centres),
                                  owner.ctypes.data_as(C.POINTER(C.c_int32))))
     return owner
+
+
+def basis_tabulate(pos, s_exps, p_exps, shape, cell, dx, rcut, dV):
+    """Grid basis of every atom tabulated on the GPU (lres_basis_tabulate): per atom the
+    points within rcut in cube order and the normalised s / p values.  s_exps, p_exps:
+    one sequence of exponents per atom.  Returns (cnt, idx, val) in the layout of
+    basis_matrices' inputs."""
+    pos = f64(pos).reshape(-1, 3)
+    nat = pos.shape[0]
+    ns = np.array([len(e) for e in s_exps], np.int32)
+    npp = np.array([len(e) for e in p_exps], np.int32)
+    exps = f64([x for a in range(nat) for x in list(s_exps[a]) + list(p_exps[a])])
+    shape, cell = i64(shape), f64(cell)
+    cnt = np.zeros(nat, np.int64)
+    i32p = C.POINTER(C.c_int32)
+    args = (nat, ptrd(pos), ns.ctypes.data_as(i32p), npp.ctypes.data_as(i32p), ptrd(exps), ptr64(shape), ptrd(cell),
+            float(dx), float(rcut), float(dV), ptr64(cnt))
+    check(lib.lres_basis_tabulate(*args, None, None))
+    nf = ns.astype(np.int64) + 3 * npp
+    idx = np.empty(int(cnt.sum()), np.int64)
+    val = np.empty(int((cnt * nf).sum()), np.float64)
+    check(lib.lres_basis_tabulate(*args, ptr64(idx), ptrd(val)))
+    return cnt, idx, val
 
 
 def basis_matrices(gptr, cnt, idx, val, shape, dV, t_diag, t_off, nthreads=0):

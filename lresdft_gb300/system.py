@@ -169,13 +169,22 @@ class LCAOBasis:
     assembly (X from the tabulated points, X^T X, X^T T_FD X) runs in the native
     library (``assembly="native"``, lres_basis_build: the reference's scipy sums in
     their order, per atom pair, on the cores this process may use, or ``nthreads``);
-    ``assembly="scipy"`` forms them with scipy.sparse as the reference does."""
+    ``assembly="scipy"`` forms them with scipy.sparse as the reference does.
+    ``tabulation="gpu"`` tabulates on the GPU instead (lres_basis_tabulate: the same points,
+    values within a few ulp of numpy's exp and normalisation sums), then assembles natively."""
 
     def __init__(self, cr: Crystal, rcut=5.5, s_exps=None, p_exps=None, atom_exps=None, assembly="native",
-                 nthreads=None):
+                 nthreads=None, tabulation="numpy"):
         self.cr, self.rcut = cr, rcut
         s_exps = S_EXPS if s_exps is None else s_exps
         p_exps = P_EXPS if p_exps is None else p_exps
+        if tabulation not in ("numpy", "gpu"):
+            raise ValueError(f"tabulation must be 'numpy' or 'gpu', not {tabulation!r}")
+        if tabulation == "gpu":
+            if assembly != "native":
+                raise ValueError("the GPU tabulation feeds the native assembly (assembly='native')")
+            self._init_gpu(s_exps, p_exps, atom_exps, nthreads)
+            return
         dx = cr.dx
         n1, n2, n3 = cr.shape
         rad = int(np.ceil(rcut / dx))
@@ -225,16 +234,34 @@ class LCAOBasis:
         else:
             raise ValueError(f"assembly must be 'native' or 'scipy', not {assembly!r}")
 
+    def _init_gpu(self, s_exps, p_exps, atom_exps, nthreads):
+        """The tabulation on the GPU (lres_basis_tabulate: same points, values within a
+        few ulp of numpy's), then the native sparse assembly."""
+        from . import _lib
+        cr = self.cr
+        nat = len(cr.pos)
+        se = [atom_exps[a][0] if atom_exps is not None else s_exps for a in range(nat)]
+        pe = [atom_exps[a][1] if atom_exps is not None else p_exps for a in range(nat)]
+        cnt, idx, val = _lib.basis_tabulate(cr.pos, se, pe, cr.shape, cr.cell, cr.dx, self.rcut, cr.dV)
+        nf = np.array([len(se[a]) + 3 * len(pe[a]) for a in range(nat)], np.int64)
+        self.nb = int(nf.sum())
+        self.atom_of_fn = np.repeat(np.arange(nat), nf)
+        self.atom_fn_ptr = np.concatenate([[0], np.cumsum(nf)]).astype(np.int64)
+        self._assemble_arrays(cnt, idx, val, nthreads)
+
     def _assemble_native(self, idxs, blocks, nthreads):
+        cnt = np.array([idx.size for idx in idxs], np.int64)
+        self._assemble_arrays(cnt, np.concatenate(idxs), np.concatenate([f for blk in blocks for f in blk]),
+                              nthreads)
+
+    def _assemble_arrays(self, cnt, idx, val, nthreads):
         from . import _lib
         cr = self.cr
         if nthreads is None:        # the cores this process may run on
             nthreads = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
         dx = cr.dx
-        cnt = np.array([idx.size for idx in idxs], np.int64)
         (Xp, Xi, Xv), (Rp, Ri, Rv), (Sp, Si, Sv), (Tp, Ti, Tv) = _lib.basis_matrices(
-            self.atom_fn_ptr, cnt, np.concatenate(idxs), np.concatenate([f for blk in blocks for f in blk]),
-            cr.shape, cr.dV, 3.0 / dx**2, -0.5 / dx**2, nthreads)
+            self.atom_fn_ptr, cnt, idx, val, cr.shape, cr.dV, 3.0 / dx**2, -0.5 / dx**2, nthreads)
         ng, nb = cr.ng, self.nb
         self.X = sparse.csc_matrix((Xv, Xi, Xp), shape=(ng, nb))
         self.Xr = sparse.csr_matrix((Rv, Ri, Rp), shape=(ng, nb))
