@@ -395,7 +395,9 @@ def run_ours(args):
                             "tflops_per_s": round(flops_step / (ms_step / 1e3) / 1e12, 2)},
         "clocks": clk,
         "breakdown_ms": breakdown,
-        "tile_config": {"chosen": s.tile_config, "ms_per_config": getattr(s, "tune_ms", None)},
+        "tile_config": {"chosen": s.tile_config,
+                        "ms_per_config": None if getattr(s, "tune_ms", None) is None
+                        else [round(float(x), 3) for x in s.tune_ms]},
         "extra_pass_ms": round(pass_ms, 3),
         "cuda_graph": graph_leg,
         "setup_s": round(setup_s, 2), "basis_s": round(basis_s, 2), "basis_tabulation": "gpu", "accuracy": err,

@@ -32,6 +32,7 @@
  *   lres_ion_potential          lrft/three_d.py:102-112,119 (erf part; no GTH short-range term)
  *   lres_basis_build / _fetch   the sparse assembly of LCAOBasis (lrft/lcao3d.py:86-96), on the host
  *   lres_basis_tabulate         the tabulation loop of LCAOBasis.__init__ (lrft/lcao3d.py:61-84), on the GPU
+ *   lres_ks_density             ks_density (src/lrft_cpp.cpp:235-284) / ks_lcao (lrft/lcao3d.py:110-117)
  */
 #ifndef LRES_GB300_H
 #define LRES_GB300_H
@@ -283,6 +284,17 @@ int lres_basis_free(lres_basis* b);
 int lres_basis_tabulate(int64_t natoms, const double* pos, const int32_t* ns, const int32_t* np,
                         const double* exps, const int64_t shape[3], const double cell[3], double dx, double rcut,
                         double dV, int64_t* cnt, int64_t* idx, double* val);
+
+/* Dense Kohn-Sham LCAO of the whole cell (ks_lcao, lrft/lcao3d.py:110-117; ks_density,
+ * src/lrft_cpp.cpp:235-284): the generalised eigenproblem H C = S C diag(w) (H, S: nb x nb
+ * CSR), w[0..nocc] = the lowest nocc + 1 eigenvalues, dens[ng] = 2 sum_{i < nocc}
+ * (X[r,:] C_i)^2 with X the ng x nb CSR basis, *e_band = 2 sum_{i < nocc} w_i.  Host arrays;
+ * synchronous on the current device.  The dense eigensolver is cuSOLVER's dsygvd, opened at
+ * run time (LRES_ESTATE if libcusolver is absent); LRES_ENUMERIC if S is not positive
+ * definite.  The oracle side of LRes(R_w >= cell) = KS, not the window solve. */
+int lres_ks_density(int64_t nb, const int64_t* Hp, const int64_t* Hi, const double* Hv, const int64_t* Sp,
+                    const int64_t* Si, const double* Sv, int64_t ng, const int64_t* Xp, const int64_t* Xi,
+                    const double* Xv, int32_t nocc, double* dens, double* w, double* e_band);
 
 /* Grid kernels on device arrays of ng doubles (context supplies shape and cell). */
 int lres_lda_xc(lres_ctx* ctx, const double* dens, double* exc, double* vxc, void* stream);

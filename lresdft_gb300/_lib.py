@@ -22,7 +22,8 @@ EXPORTS = ("lres_version", "lres_last_error", "lres_ctx_create", "lres_ctx_destr
            "lres_set_route", "lres_get_route", "lres_timings", "lres_window_sums", "lres_inertia", "lres_min_eig",
            "lres_voronoi_owner", "lres_lda_xc", "lres_hartree", "lres_ion_potential", "lres_inertia_noalloc",
            "lres_set_windows", "lres_window_ptrs", "lres_adjoint", "lres_owned_gram", "lres_set_trace_rows",
-           "lres_basis_build", "lres_basis_fetch", "lres_basis_free", "lres_basis_tabulate")
+           "lres_basis_build", "lres_basis_fetch", "lres_basis_free", "lres_basis_tabulate",
+           "lres_ks_density")
 
 
 class LResError(RuntimeError):
@@ -88,6 +89,7 @@ def _load():
         "lres_basis_free": (i32, [vp]),
         "lres_basis_tabulate": (i32, [i64, PD, C.POINTER(C.c_int32), C.POINTER(C.c_int32), PD, P64, PD, dbl, dbl,
                                       dbl, P64, P64, PD]),
+        "lres_ks_density": (i32, [i64, P64, P64, PD, P64, P64, PD, i64, P64, P64, PD, C.c_int32, PD, PD, PD]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

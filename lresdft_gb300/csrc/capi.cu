@@ -340,9 +340,11 @@ int transform_df64(lres_ctx* c, cudaStream_t s) {
 float* tri_hhat32(lres_ctx* c) { return reinterpret_cast<float*>(c->d_Y_df) + c->sizeC; }
 
 int transform_f32(lres_ctx* c, cudaStream_t s) {
+    // Y = H L^-T (B = L^-T given k-major: its transpose L^-1), written row-major (k-major for
+    // the next product); A^ = lower(L^-1 Y)
     float* Y = reinterpret_cast<float*>(c->d_Y_df);
-    TRY(batched_gemm_f32(c->nwin, c->d_n, c->d_offC, c->nmax, 1, c->d_HW, true, c->d_LinvT32, Y, s));
-    TRY(batched_gemm_f32(c->nwin, c->d_n, c->d_offC, c->nmax, 2, c->d_Linv32, false, Y, tri_hhat32(c), s));
+    TRY(batched_gemm_f32(c->nwin, c->d_n, c->d_offC, c->nmax, 1, c->d_HW, true, c->d_Linv32, Y, true, s));
+    TRY(batched_gemm_f32(c->nwin, c->d_n, c->d_offC, c->nmax, 2, c->d_Linv32, false, Y, tri_hhat32(c), false, s));
     c->hhat_df = false;                  // d_Hhat32 no longer follows H_W
     return LRES_OK;
 }

@@ -787,18 +787,22 @@ __global__ void __launch_bounds__(256) gemm_df64_kernel(const int* n_w, const lo
 }
 
 // ---------------------------------------------------------------------------
-// batched FP32 GEMM with blocked sums  C_w = A_w B_w  (n_w x n_w, column-major, offsets off)
+// batched FP32 GEMM with blocked sums  C_w = A_w B_w  (n_w x n_w, offsets off)
 // ---------------------------------------------------------------------------
 // KLIM as gemm_f64_kernel (1: B upper triangular, k <= column; 2: A lower triangular, k <= row,
-// lower triangle of C only).  A is FP64 (converted on load) or FP32, B and C FP32.  Each
+// lower triangle of C only).  A is column-major, FP64 (converted on load) or FP32; B is given
+// k-major (Bt[j + k n] = B[k][j], i.e. B stored row-major), so that both operand tiles are
+// staged with coalesced loads and conflict-free stores and read as 16-byte vectors; C is
+// written column-major or (CROW) row-major, the k-major layout of the next product.  Each
 // 32-term block of the k sum is formed from zero and added to the running value, so the
 // rounding grows with the number of blocks rather than the number of terms.  64 x 64 tiles,
-// 4 x 4 outputs per thread; A staged k-major (16-byte reads of 4 rows), B column-major with a
-// padded row so that both the staging stores and the reads are free of bank conflicts.
-template <int KLIM, bool AF64>
-__global__ void __launch_bounds__(256) gemm_f32blk_kernel(const int* n_w, const long long* off, const void* Av,
-                                                          const float* B, float* C) {
-    constexpr int BM = 64, BN = 64, BK = 32;
+// 128 threads, 8 x 4 outputs per thread (rows 4tx..4tx+3 and 32+4tx..; columns 4ty..4ty+3:
+// per k two 16-byte loads of A and one of B feed 32 FMAs); the next k tile is loaded into
+// registers while the current one is multiplied (two shared-memory buffers).
+template <int KLIM, bool AF64, bool CROW>
+__global__ void __launch_bounds__(128) gemm_f32blk_kernel(const int* n_w, const long long* off, const void* Av,
+                                                          const float* Bt, float* C) {
+    constexpr int BM = 64, BN = 64, BK = 32, NT = 128, PER = BK * BM / NT;     // 16 staged values each
     const int w = blockIdx.z;
     const int n = n_w[w];
     const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
@@ -807,69 +811,96 @@ __global__ void __launch_bounds__(256) gemm_f32blk_kernel(const int* n_w, const 
     const int kend = KLIM == 1 ? min(n, n0 + BN) : KLIM == 2 ? min(n, m0 + BM) : n;
     const double* A64 = AF64 ? static_cast<const double*>(Av) + off[w] : nullptr;
     const float* A32 = AF64 ? nullptr : static_cast<const float*>(Av) + off[w];
-    const float* Bw = B + off[w];
-    __shared__ __align__(16) float As[BK][BM];
-    __shared__ float Bs[BN][BK + 1];
+    const float* Bw = Bt + off[w];
+    __shared__ __align__(16) float As[2][BK][BM];
+    __shared__ __align__(16) float Bs[2][BK][BN];
     const int tid = threadIdx.x;
-    const int tx = tid % 16, ty = tid / 16;
-    float acc[4][4];
+    const int tx = tid & 7, ty = tid >> 3;
+    float ra[PER], rb[PER];
+    auto load = [&](int k0) {
 #pragma unroll
-    for (int u = 0; u < 4; ++u)
+        for (int q = 0; q < PER; ++q) {
+            const int idx = tid + q * NT, kk = idx / BM, x = idx % BM;
+            const int gk = k0 + kk;
+            const int gi = m0 + x, gj = n0 + x;
+            float a = 0.f, b = 0.f;
+            if (gi < n && gk < n) a = AF64 ? (float)A64[gi + (long long)gk * n] : A32[gi + (long long)gk * n];
+            if (gj < n && gk < n) b = Bw[gj + (long long)gk * n];
+            ra[q] = a;
+            rb[q] = b;
+        }
+    };
+    auto store = [&](int buf) {
+#pragma unroll
+        for (int q = 0; q < PER; ++q) {
+            const int idx = tid + q * NT, kk = idx / BM, x = idx % BM;
+            As[buf][kk][x] = ra[q];
+            Bs[buf][kk][x] = rb[q];
+        }
+    };
+    float acc[8][4];
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
 #pragma unroll
         for (int v = 0; v < 4; ++v) acc[u][v] = 0.f;
+    load(0);
+    store(0);
+    __syncthreads();
+    int buf = 0;
     for (int k0 = 0; k0 < kend; k0 += BK) {
-        for (int idx = tid; idx < BK * BM; idx += 256) {
-            const int kk = idx / BM, i = idx % BM;
-            const int gi = m0 + i, gk = k0 + kk;
-            float a = 0.f;
-            if (gi < n && gk < n) a = AF64 ? (float)A64[gi + (long long)gk * n] : A32[gi + (long long)gk * n];
-            As[kk][i] = a;
-        }
-        for (int idx = tid; idx < BK * BN; idx += 256) {
-            const int j = idx / BK, kk = idx % BK;
-            const int gj = n0 + j, gk = k0 + kk;
-            Bs[j][kk] = (gj < n && gk < n) ? Bw[gk + (long long)gj * n] : 0.f;
-        }
-        __syncthreads();
-        float blk[4][4];
+        const bool more = k0 + BK < kend;
+        if (more) load(k0 + BK);
+        float blk[8][4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
+        for (int u = 0; u < 8; ++u)
 #pragma unroll
             for (int v = 0; v < 4; ++v) blk[u][v] = 0.f;
 #pragma unroll 8
         for (int kk = 0; kk < BK; ++kk) {
-            const float4 a = *reinterpret_cast<const float4*>(&As[kk][4 * tx]);
-            const float av[4] = {a.x, a.y, a.z, a.w};
-            float bv[4];
+            const float4 a0 = *reinterpret_cast<const float4*>(&As[buf][kk][4 * tx]);
+            const float4 a1 = *reinterpret_cast<const float4*>(&As[buf][kk][32 + 4 * tx]);
+            const float4 b = *reinterpret_cast<const float4*>(&Bs[buf][kk][4 * ty]);
+            const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+            const float bv[4] = {b.x, b.y, b.z, b.w};
 #pragma unroll
-            for (int v = 0; v < 4; ++v) bv[v] = Bs[4 * ty + v][kk];
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
+            for (int u = 0; u < 8; ++u)
 #pragma unroll
                 for (int v = 0; v < 4; ++v) blk[u][v] = fmaf(av[u], bv[v], blk[u][v]);
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
+        for (int u = 0; u < 8; ++u)
 #pragma unroll
             for (int v = 0; v < 4; ++v) acc[u][v] += blk[u][v];
-        __syncthreads();
+        if (more) {
+            store(buf ^ 1);
+            __syncthreads();
+            buf ^= 1;
+        }
     }
     float* Cw = C + off[w];
 #pragma unroll
-    for (int u = 0; u < 4; ++u)
+    for (int u = 0; u < 8; ++u)
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
-            const int gi = m0 + 4 * tx + u, gj = n0 + 4 * ty + v;
-            if (gi < n && gj < n) Cw[gi + (long long)gj * n] = acc[u][v];
+            const int gi = m0 + (u < 4 ? 4 * tx + u : 32 + 4 * tx + u - 4), gj = n0 + 4 * ty + v;
+            if (gi < n && gj < n) {
+                if (CROW) Cw[(long long)gi * n + gj] = acc[u][v];
+                else Cw[gi + (long long)gj * n] = acc[u][v];
+            }
         }
 }
 
 int batched_gemm_f32(int nwin, const int* n_w, const long long* off, int nmax, int klim, const void* A, bool a_f64,
-                     const float* B, float* C, cudaStream_t s) {
+                     const float* Bt, float* C, bool c_rowmajor, cudaStream_t s) {
     if (!nwin) return LRES_OK;
+    if (nwin > 65535) {
+        lres_set_error("FP32 GEMM supports at most 65535 windows (got %d)", nwin);
+        return LRES_EINVAL;
+    }
     dim3 grid((nmax + 63) / 64, (nmax + 63) / 64, nwin);
-    if (klim == 1 && a_f64) gemm_f32blk_kernel<1, true><<<grid, 256, 0, s>>>(n_w, off, A, B, C);
-    else if (klim == 2 && !a_f64) gemm_f32blk_kernel<2, false><<<grid, 256, 0, s>>>(n_w, off, A, B, C);
+    if (klim == 1 && a_f64 && c_rowmajor) gemm_f32blk_kernel<1, true, true><<<grid, 128, 0, s>>>(n_w, off, A, Bt, C);
+    else if (klim == 2 && !a_f64 && !c_rowmajor)
+        gemm_f32blk_kernel<2, false, false><<<grid, 128, 0, s>>>(n_w, off, A, Bt, C);
     else {
         lres_set_error("unsupported FP32 GEMM variant");
         return LRES_EINVAL;

@@ -105,8 +105,10 @@ int convert_f64_f32(const double* a, float* b, long long n, cudaStream_t s);
 int split_f64(const double* a, float2* b, long long n, cudaStream_t s);
 int batched_gemm_df64(int nwin, const int* n_w, const long long* off, int nmax, bool transA, int klim,
                       const float2* A, const float2* B, float2* C, float* C32, cudaStream_t s);
+// C = A B for every window block: A column-major (FP64 or FP32), B k-major (Bt[j + k n] =
+// B[k][j]), C column-major or row-major (c_rowmajor); klim as batched_gemm.
 int batched_gemm_f32(int nwin, const int* n_w, const long long* off, int nmax, int klim, const void* A, bool a_f64,
-                     const float* B, float* C, cudaStream_t s);
+                     const float* Bt, float* C, bool c_rowmajor, cudaStream_t s);
 int batched_transpose_f32(int nwin, const int* n_w, const long long* off, int nmax, const float* A, float* B,
                           cudaStream_t s);
 int pole_sums(int nwin, const long long* offQ, const int* m_w, const long long* Oflat, bool fp32,

@@ -389,24 +389,30 @@ __global__ void __launch_bounds__(NT) tri_reduce_kernel(TriReduceParams<R> p) {
 // Householder tridiagonalisation with the window resident in shared memory (FP32)
 // ---------------------------------------------------------------------------
 //
-// The lower triangle of the window (packed by columns: column c holds rows c..n-1 from
-// colstart(c) = c n - c (c - 1) / 2) stays in shared memory for the whole reduction, so
-// p = A v and the panel updates never leave the SM.  p_i = sum_k A_ik v_k reads row i of
-// the lower triangle up to the diagonal and column i below it: along one merged loop the
-// address steps by n - k - 1 while k < i and by 1 after, so every row costs the same
-// n - j - 1 loads and no lane diverges; two threads share a row (halves of k), their
-// partial sums added in a fixed order.  Each sum runs in blocks of 32 terms from zero.
-// One CTA per window (work queue, largest first), windows up to kResReduceMaxN functions.
+// The lower triangle of the window stays in shared memory for the whole reduction, in 4 x 4
+// blocks: column c holds rows 4 (c / 4) .. ld-1, i.e. the lower part plus the upper part of
+// its diagonal block (kept equal to the lower one), from
+//     colstart(c) = c ld - 8 a (a - 1) - 4 a b,   a = c / 4, b = c % 4,
+// so that every block's four column segments start on 16-byte boundaries.  p = A v uses
+// each stored block twice: for the row quad I, block (I, K) (K <= I) directly and block (K, I)
+// (K > I) transposed; a warp takes one row quad at a time, its lanes the column quads K
+// (16-byte loads, four per block), and the lanes' partial sums are added by a butterfly in a
+// fixed order.  The trailing update touches the stored blocks only (half the FMAs of a full
+// update).  One CTA per window (work queue, largest first), windows up to ld <= 320.
 
 constexpr int kResReduceNT = 640;
-constexpr int kResReduceMaxN = kResReduceNT / 2 + 1;    // two threads per row of p = A v
+constexpr int kResReduceMaxN = 320;
 
-__host__ __device__ inline long long res_colstart(int c, int n) {
-    return (long long)c * n - (long long)c * (c - 1) / 2;
+__host__ __device__ inline int res_cs(int c, int ld) {
+    const int a = c >> 2, b = c & 3;
+    return c * ld - 8 * a * (a - 1) - 4 * a * b;
 }
+// element (r, c) of the stored part (r >= 4 (c / 4))
+__host__ __device__ inline int res_at(int r, int c, int ld) { return res_cs(c, ld) + r - 4 * (c >> 2); }
 
 inline size_t res_reduce_smem_elems(int nb, int ldv, int nmax) {
-    return (size_t)nmax * (nmax + 1) / 2 + 2 * (size_t)nb * ldv + 3 * (size_t)ldv + 64 + kResReduceNT / 32;
+    const int ld = (nmax + 3) & ~3;
+    return (size_t)res_cs(ld, ld) + 2 * (size_t)nb * ldv + 2 * (size_t)ldv + 64 + kResReduceNT / 32;
 }
 
 template <int NT>
@@ -416,12 +422,11 @@ __global__ void __launch_bounds__(NT, 1) tri_reduce_res_kernel(TriReduceParams<f
     const int ldv = p.ldv, nb = p.nb;
     float* const Vs = reinterpret_cast<float*>(smem_raw);            // [nb][ldv]
     float* const Ws = Vs + (size_t)nb * ldv;                         // [nb][ldv]
-    float* const cv = Ws + (size_t)nb * ldv;                         // [ldv] current column
+    float* const Ls = Ws + (size_t)nb * ldv;                         // blocked lower triangle
+    float* const cv = Ls + res_cs((nmax + 3) & ~3, (nmax + 3) & ~3); // [ldv] current column
     float* const pv = cv + ldv;                                      // [ldv] p = tau (A v)
-    float* const ph = pv + ldv;                                      // [ldv] second half of A v
-    float* const dots = ph + ldv;                                    // [64]
+    float* const dots = pv + ldv;                                    // [64]
     float* const red = dots + 64;                                    // [NW]
-    float* const Ls = red + NW;                                      // packed lower triangle
     __shared__ int item_sh;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
@@ -432,25 +437,29 @@ __global__ void __launch_bounds__(NT, 1) tri_reduce_res_kernel(TriReduceParams<f
         if (it >= p.nwin) return;
         const int w = p.order[it];
         const int n = p.n_w[w];
+        const int ld = (n + 3) & ~3;
         if (n > ldv || n > nmax || n < 1) {
             if (tid == 0) atomicOr(p.status, ST_BAD_SHAPE);
             __syncthreads();
             continue;
         }
-        const long long ld = (n + 3) & ~3;
+        const int nq = ld >> 2;
         const float* H = p.H + p.offC[w];
         float* A = p.A + p.offA[w];
         float* dw = p.d + p.offN[w];
         float* ew = p.e + p.offN[w];
         float* tw = p.tau + p.offN[w];
 
-        // ---- the lower triangle of H into Ls (warp per column, rows along the lanes)
-        for (int c = warp; c < n; c += NW) {
-            const long long cs = res_colstart(c, n);
-            for (int r = c + lane; r < n; r += 32) cp_async4(Ls + cs + (r - c), H + r + (long long)c * n);
+        // ---- the stored part of H (lower triangle, mirrored into the diagonal blocks; zero
+        //      beyond n), warp per column, rows along the lanes
+        for (int c = warp; c < ld; c += NW) {
+            const int r0 = 4 * (c >> 2);
+            for (int r = r0 + lane; r < ld; r += 32) {
+                float x = 0.0f;
+                if (r < n && c < n) x = r >= c ? H[r + (long long)c * n] : H[c + (long long)r * n];
+                Ls[res_at(r, c, ld)] = x;
+            }
         }
-        cp_commit();
-        cp_wait<0>();
         __syncthreads();
 
         for (int j0 = 0; j0 < n - 2; j0 += nb) {
@@ -463,15 +472,14 @@ __global__ void __launch_bounds__(NT, 1) tri_reduce_res_kernel(TriReduceParams<f
                 {
                     const int i = j + tid;
                     if (i < n) {
-                        float c = Ls[res_colstart(j, n) + (i - j)];
+                        float c = Ls[res_at(i, j, ld)];
                         for (int l = 0; l < jj; ++l)
                             c -= Vs[l * ldv + i] * Ws[l * ldv + j] + Ws[l * ldv + i] * Vs[l * ldv + j];
                         cv[i] = c;
                         if (i >= j + 2) part = c * c;
                     }
                 }
-                // (b) reflector H_j = I - tau v v^T, v_{j+1} = 1, mapping rows j+1.. of the
-                //     column onto beta e_{j+1}
+                // (b) reflector H_j = I - tau v v^T, v_{j+1} = 1
                 const float s2 = block_sum<NT>(part, red);    // its barriers also publish cv
                 const float alpha = cv[j + 1];
                 float beta = alpha, tau = 0.0f, scal = 0.0f;
@@ -495,8 +503,8 @@ __global__ void __launch_bounds__(NT, 1) tri_reduce_res_kernel(TriReduceParams<f
                     if (i > j + 1 && i < n) A[i + (long long)j * ld] = vi;   // kept for Y = F^ Q
                 }
                 __syncthreads();
-                // (c) W^T v, V^T v (warp per product) and A v on rows j+1..n-1 from the
-                //     panel-start matrix (two threads per row, halves of k)
+                // (c) W^T v, V^T v (warp per product) and A v on the row quads from (j+1)/4,
+                //     from the panel-start matrix (v is zero on the rows <= j)
                 for (int q = warp; q < 2 * jj; q += NW) {
                     const float* X = q < jj ? Ws + (size_t)q * ldv : Vs + (size_t)(q - jj) * ldv;
                     float acc = 0.0f;
@@ -505,27 +513,38 @@ __global__ void __launch_bounds__(NT, 1) tri_reduce_res_kernel(TriReduceParams<f
                     if (lane == 0) dots[q] = acc;
                 }
                 {
-                    const int nk = n - j - 1;                 // columns (and rows) j+1..n-1
-                    const int row = tid >> 1, half = tid & 1;
-                    if (row < nk) {
-                        const int i = j + 1 + row;
-                        const int kmid = j + 1 + (nk + 1) / 2;
-                        const int ka = half ? kmid : j + 1, kz = half ? n : kmid;
-                        const float* vv = Vs + (size_t)jj * ldv;
-                        long long addr = ka <= i ? res_colstart(ka, n) + (i - ka) : res_colstart(i, n) + (ka - i);
-                        float acc = 0.0f;
-                        for (int kb = ka; kb < kz; kb += 32) {
-                            const int ke = min(kz, kb + 32);
-                            float c = 0.0f;
-#pragma unroll 8
-                            for (int k = kb; k < ke; ++k) {
-                                c = fmaf(Ls[addr], vv[k], c);
-                                addr += k < i ? (n - k - 1) : 1;
+                    const float* vv = Vs + (size_t)jj * ldv;
+                    const int q0 = (j + 1) >> 2;
+                    for (int I = q0 + warp; I < nq; I += NW) {
+                        float pr[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+                        const float4 vI = *reinterpret_cast<const float4*>(vv + 4 * I);
+                        const float vi[4] = {vI.x, vI.y, vI.z, vI.w};
+                        for (int K = q0 + lane; K < nq; K += 32) {
+                            const float4 vK4 = *reinterpret_cast<const float4*>(vv + 4 * K);
+                            const float vk[4] = {vK4.x, vK4.y, vK4.z, vK4.w};
+                            if (K > I) {
+                                // block (K, I): column 4I+c, rows 4K..4K+3; p_I[c] += sum_r b[r] v_K[r]
+#pragma unroll
+                                for (int c = 0; c < 4; ++c) {
+                                    const float4 b = *reinterpret_cast<const float4*>(Ls + res_at(4 * K, 4 * I + c, ld));
+                                    pr[c] = fmaf(b.x, vk[0], fmaf(b.y, vk[1], fmaf(b.z, vk[2], fmaf(b.w, vk[3], pr[c]))));
+                                }
+                            } else {
+                                // block (I, K): column 4K+c, rows 4I..4I+3; p_I[r] += b[r] v_K[c]
+#pragma unroll
+                                for (int c = 0; c < 4; ++c) {
+                                    const float4 b = *reinterpret_cast<const float4*>(Ls + res_at(4 * I, 4 * K + c, ld));
+                                    pr[0] = fmaf(b.x, vk[c], pr[0]);
+                                    pr[1] = fmaf(b.y, vk[c], pr[1]);
+                                    pr[2] = fmaf(b.z, vk[c], pr[2]);
+                                    pr[3] = fmaf(b.w, vk[c], pr[3]);
+                                }
                             }
-                            acc += c;
                         }
-                        if (half) ph[i] = acc;
-                        else pv[i] = acc;
+                        (void)vi;
+#pragma unroll
+                        for (int r = 0; r < 4; ++r) pr[r] = warp_sum(pr[r]);
+                        if (lane < 4) pv[4 * I + lane] = pr[lane];
                     }
                 }
                 __syncthreads();
@@ -534,7 +553,7 @@ __global__ void __launch_bounds__(NT, 1) tri_reduce_res_kernel(TriReduceParams<f
                 {
                     const int i = j + 1 + tid;
                     if (i < n) {
-                        float pi = pv[i] + ph[i];
+                        float pi = pv[i];
                         for (int l = 0; l < jj; ++l) pi -= Vs[l * ldv + i] * dots[l] + Ws[l * ldv + i] * dots[jj + l];
                         pi *= tau;
                         pv[i] = pi;
@@ -546,24 +565,19 @@ __global__ void __launch_bounds__(NT, 1) tri_reduce_res_kernel(TriReduceParams<f
                     Ws[jj * ldv + i] = (i > j && i < n) ? pv[i] - K * Vs[jj * ldv + i] : 0.0f;
                 __syncthreads();
             }
-            // ---- trailing update of the lower triangle: L -= V W^T + W V^T on columns >= t0,
-            //      one quad of rows x one quad of columns per thread (the quads of the lower
-            //      block triangle); v, w of both quads from shared memory as 16-byte vectors
+            // ---- trailing update of the stored blocks (I >= K >= t0 / 4): B -= V W^T + W V^T,
+            //      one 4 x 4 block per thread, v, w of both quads as 16-byte vectors
             const int t0 = j0 + nbp;
             if (t0 < n) {
-                const int q0 = t0 & ~3;
-                const int nq = (ld - q0) >> 2;
-                const int ntile = nq * (nq + 1) / 2;
+                const int qa = t0 >> 2;
+                const int m = nq - qa;
+                const int ntile = m * (m + 1) / 2;
                 for (int tile = tid; tile < ntile; tile += NT) {
-                    int qi = 0, qc = tile;                     // tile-th quad pair (qc <= qi)
-                    {
-                        // qi = floor((sqrt(8 tile + 1) - 1) / 2), corrected for rounding
-                        qi = (int)((sqrtf(8.0f * tile + 1.0f) - 1.0f) * 0.5f);
-                        while ((qi + 1) * (qi + 2) / 2 <= tile) ++qi;
-                        while (qi * (qi + 1) / 2 > tile) --qi;
-                        qc = tile - qi * (qi + 1) / 2;
-                    }
-                    const int i = q0 + 4 * qi, c0 = q0 + 4 * qc;
+                    int qi = (int)((sqrtf(8.0f * tile + 1.0f) - 1.0f) * 0.5f);
+                    while ((qi + 1) * (qi + 2) / 2 <= tile) ++qi;
+                    while (qi * (qi + 1) / 2 > tile) --qi;
+                    const int qc = tile - qi * (qi + 1) / 2;
+                    const int i = 4 * (qa + qi), c0 = 4 * (qa + qc);
                     float acc[4][4];
 #pragma unroll
                     for (int c = 0; c < 4; ++c)
@@ -582,12 +596,12 @@ __global__ void __launch_bounds__(NT, 1) tri_reduce_res_kernel(TriReduceParams<f
                     }
 #pragma unroll
                     for (int c = 0; c < 4; ++c) {
-                        const int col = c0 + c;
-                        if (col < t0 || col >= n) continue;
-                        const long long cs = res_colstart(col, n) - col;
+                        float* dst = Ls + res_at(i, c0 + c, ld);
+                        float x[4];
+                        ld4(dst, x);
 #pragma unroll
-                        for (int r = 0; r < 4; ++r)
-                            if (i + r >= col && i + r < n) Ls[cs + i + r] -= acc[c][r];
+                        for (int r = 0; r < 4; ++r) x[r] -= acc[c][r];
+                        st4(dst, x);
                     }
                 }
             }
@@ -596,9 +610,9 @@ __global__ void __launch_bounds__(NT, 1) tri_reduce_res_kernel(TriReduceParams<f
         // ---- the last (at most 2 x 2) block, fully updated
         if (tid == 0) {
             if (n >= 2) {
-                dw[n - 2] = Ls[res_colstart(n - 2, n)];
-                ew[n - 2] = Ls[res_colstart(n - 2, n) + 1];
-                dw[n - 1] = Ls[res_colstart(n - 1, n)];
+                dw[n - 2] = Ls[res_at(n - 2, n - 2, ld)];
+                ew[n - 2] = Ls[res_at(n - 1, n - 2, ld)];
+                dw[n - 1] = Ls[res_at(n - 1, n - 1, ld)];
                 tw[n - 2] = 0.0f;
                 tw[n - 1] = 0.0f;
                 ew[n - 1] = 0.0f;
