@@ -13,6 +13,7 @@
 
 #include <algorithm>
 #include <numeric>
+#include <type_traits>
 
 namespace lres {
 
@@ -800,7 +801,7 @@ __global__ void __launch_bounds__(256) gemm_df64_kernel(const int* n_w, const lo
 // per k two 16-byte loads of A and one of B feed 32 FMAs); the next k tile is loaded into
 // registers while the current one is multiplied (two shared-memory buffers).
 template <int KLIM, bool AF64, bool CROW>
-__global__ void __launch_bounds__(128) gemm_f32blk_kernel(const int* n_w, const long long* off, const void* Av,
+__global__ void __launch_bounds__(128, 3) gemm_f32blk_kernel(const int* n_w, const long long* off, const void* Av,
                                                           const float* Bt, float* C) {
     constexpr int BM = 64, BN = 64, BK = 32, NT = 128, PER = BK * BM / NT;     // 16 staged values each
     const int w = blockIdx.z;
@@ -816,15 +817,23 @@ __global__ void __launch_bounds__(128) gemm_f32blk_kernel(const int* n_w, const 
     __shared__ __align__(16) float Bs[2][BK][BN];
     const int tid = threadIdx.x;
     const int tx = tid & 7, ty = tid >> 3;
-    float ra[PER], rb[PER];
+    // the next tile is held in registers as loaded (FP64 values converted only when stored,
+    // so that the loads stay in flight during the multiplication)
+    using AT = typename std::conditional<AF64, double, float>::type;
+    AT ra[PER];
+    float rb[PER];
     auto load = [&](int k0) {
 #pragma unroll
         for (int q = 0; q < PER; ++q) {
             const int idx = tid + q * NT, kk = idx / BM, x = idx % BM;
             const int gk = k0 + kk;
             const int gi = m0 + x, gj = n0 + x;
-            float a = 0.f, b = 0.f;
-            if (gi < n && gk < n) a = AF64 ? (float)A64[gi + (long long)gk * n] : A32[gi + (long long)gk * n];
+            AT a = AT(0);
+            float b = 0.f;
+            if (gi < n && gk < n) {
+                if constexpr (AF64) a = A64[gi + (long long)gk * n];
+                else a = A32[gi + (long long)gk * n];
+            }
             if (gj < n && gk < n) b = Bw[gj + (long long)gk * n];
             ra[q] = a;
             rb[q] = b;
@@ -834,7 +843,7 @@ __global__ void __launch_bounds__(128) gemm_f32blk_kernel(const int* n_w, const 
 #pragma unroll
         for (int q = 0; q < PER; ++q) {
             const int idx = tid + q * NT, kk = idx / BM, x = idx % BM;
-            As[buf][kk][x] = ra[q];
+            As[buf][kk][x] = (float)ra[q];
             Bs[buf][kk][x] = rb[q];
         }
     };

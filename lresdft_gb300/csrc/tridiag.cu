@@ -410,13 +410,15 @@ __host__ __device__ inline int res_cs(int c, int ld) {
 // element (r, c) of the stored part (r >= 4 (c / 4))
 __host__ __device__ inline int res_at(int r, int c, int ld) { return res_cs(c, ld) + r - 4 * (c >> 2); }
 
+// shared memory without the partial sums of p = A v (nseg x ldv more)
 inline size_t res_reduce_smem_elems(int nb, int ldv, int nmax) {
     const int ld = (nmax + 3) & ~3;
-    return (size_t)res_cs(ld, ld) + 2 * (size_t)nb * ldv + 2 * (size_t)ldv + 64 + kResReduceNT / 32;
+    const size_t head = (size_t)res_cs(ld, ld) + 2 * (size_t)nb * ldv + 2 * (size_t)ldv + 64 + kResReduceNT / 32;
+    return ((head + 3) & ~(size_t)3) + (size_t)ldv;      // + the column-start table (16-byte aligned)
 }
 
 template <int NT>
-__global__ void __launch_bounds__(NT, 1) tri_reduce_res_kernel(TriReduceParams<float> p, int nmax) {
+__global__ void __launch_bounds__(NT, 1) tri_reduce_res_kernel(TriReduceParams<float> p, int nmax, int nseg) {
     constexpr int NW = NT / 32;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int ldv = p.ldv, nb = p.nb;
@@ -427,7 +429,10 @@ __global__ void __launch_bounds__(NT, 1) tri_reduce_res_kernel(TriReduceParams<f
     float* const pv = cv + ldv;                                      // [ldv] p = tau (A v)
     float* const dots = pv + ldv;                                    // [64]
     float* const red = dots + 64;                                    // [NW]
-    __shared__ int item_sh;
+    const size_t head = (size_t)(red + NW - reinterpret_cast<float*>(smem_raw));
+    int* const cst = reinterpret_cast<int*>(smem_raw) + ((head + 3) & ~(size_t)3);   // [ldv] column starts
+    float* const psum = reinterpret_cast<float*>(cst + ldv);         // [nseg][ldv] partial A v
+    __shared__ int item_sh, nseg_used;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
     for (;;) {
@@ -450,6 +455,7 @@ __global__ void __launch_bounds__(NT, 1) tri_reduce_res_kernel(TriReduceParams<f
         float* ew = p.e + p.offN[w];
         float* tw = p.tau + p.offN[w];
 
+        for (int c = tid; c < ld; c += NT) cst[c] = res_cs(c, ld);
         // ---- the stored part of H (lower triangle, mirrored into the diagonal blocks; zero
         //      beyond n), warp per column, rows along the lanes
         for (int c = warp; c < ld; c += NW) {
@@ -513,39 +519,51 @@ __global__ void __launch_bounds__(NT, 1) tri_reduce_res_kernel(TriReduceParams<f
                     if (lane == 0) dots[q] = acc;
                 }
                 {
+                    // lanes over 32 row quads I, warps over (row-quad group, segment of the
+                    // column quads K); each warp's partial sums go to psum[segment] and are
+                    // added in segment order in (d)
                     const float* vv = Vs + (size_t)jj * ldv;
-                    const int q0 = (j + 1) >> 2;
-                    for (int I = q0 + warp; I < nq; I += NW) {
+                    const int q0 = (j + 1) >> 2, mq = nq - q0;
+                    const int G = (mq + 31) >> 5;
+                    const int S = min(NW / G, nseg);
+                    const int g = warp / S, s = warp % S;
+                    if (g < G) {
+                        const int I = q0 + 32 * g + lane;
+                        const int k0 = q0 + (int)((long long)mq * s / S), k1 = q0 + (int)((long long)mq * (s + 1) / S);
                         float pr[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-                        const float4 vI = *reinterpret_cast<const float4*>(vv + 4 * I);
-                        const float vi[4] = {vI.x, vI.y, vI.z, vI.w};
-                        for (int K = q0 + lane; K < nq; K += 32) {
-                            const float4 vK4 = *reinterpret_cast<const float4*>(vv + 4 * K);
-                            const float vk[4] = {vK4.x, vK4.y, vK4.z, vK4.w};
-                            if (K > I) {
-                                // block (K, I): column 4I+c, rows 4K..4K+3; p_I[c] += sum_r b[r] v_K[r]
+                        if (I < nq) {
+                            const int4 cI = *reinterpret_cast<const int4*>(cst + 4 * I);
+                            const int csI[4] = {cI.x, cI.y, cI.z, cI.w};
+                            for (int K = k0; K < k1; ++K) {
+                                const float4 vK4 = *reinterpret_cast<const float4*>(vv + 4 * K);
+                                const float vk[4] = {vK4.x, vK4.y, vK4.z, vK4.w};
+                                if (K > I) {
+                                    // block (K, I): column 4I+c, rows 4K..4K+3: p_I[c] += b . v_K
+                                    const int base = 4 * K - 4 * I;
 #pragma unroll
-                                for (int c = 0; c < 4; ++c) {
-                                    const float4 b = *reinterpret_cast<const float4*>(Ls + res_at(4 * K, 4 * I + c, ld));
-                                    pr[c] = fmaf(b.x, vk[0], fmaf(b.y, vk[1], fmaf(b.z, vk[2], fmaf(b.w, vk[3], pr[c]))));
-                                }
-                            } else {
-                                // block (I, K): column 4K+c, rows 4I..4I+3; p_I[r] += b[r] v_K[c]
+                                    for (int c = 0; c < 4; ++c) {
+                                        const float4 b = *reinterpret_cast<const float4*>(Ls + csI[c] + base);
+                                        pr[c] = fmaf(b.x, vk[0], fmaf(b.y, vk[1], fmaf(b.z, vk[2], fmaf(b.w, vk[3], pr[c]))));
+                                    }
+                                } else {
+                                    // block (I, K): column 4K+c, rows 4I..4I+3: p_I[r] += b[r] v_K[c]
+                                    const int4 cK = *reinterpret_cast<const int4*>(cst + 4 * K);
+                                    const int off = 4 * I - 4 * K;
+                                    const int cc[4] = {cK.x, cK.y, cK.z, cK.w};
 #pragma unroll
-                                for (int c = 0; c < 4; ++c) {
-                                    const float4 b = *reinterpret_cast<const float4*>(Ls + res_at(4 * I, 4 * K + c, ld));
-                                    pr[0] = fmaf(b.x, vk[c], pr[0]);
-                                    pr[1] = fmaf(b.y, vk[c], pr[1]);
-                                    pr[2] = fmaf(b.z, vk[c], pr[2]);
-                                    pr[3] = fmaf(b.w, vk[c], pr[3]);
+                                    for (int c = 0; c < 4; ++c) {
+                                        const float4 b = *reinterpret_cast<const float4*>(Ls + cc[c] + off);
+                                        pr[0] = fmaf(b.x, vk[c], pr[0]);
+                                        pr[1] = fmaf(b.y, vk[c], pr[1]);
+                                        pr[2] = fmaf(b.z, vk[c], pr[2]);
+                                        pr[3] = fmaf(b.w, vk[c], pr[3]);
+                                    }
                                 }
                             }
+                            *reinterpret_cast<float4*>(psum + (size_t)s * ldv + 4 * I) = make_float4(pr[0], pr[1], pr[2], pr[3]);
                         }
-                        (void)vi;
-#pragma unroll
-                        for (int r = 0; r < 4; ++r) pr[r] = warp_sum(pr[r]);
-                        if (lane < 4) pv[4 * I + lane] = pr[lane];
                     }
+                    if (tid == 0) nseg_used = S;
                 }
                 __syncthreads();
                 // (d) p *= tau (with the pending updates), K = tau/2 p.v, w = p - K v
@@ -553,7 +571,8 @@ __global__ void __launch_bounds__(NT, 1) tri_reduce_res_kernel(TriReduceParams<f
                 {
                     const int i = j + 1 + tid;
                     if (i < n) {
-                        float pi = pv[i];
+                        float pi = psum[i];
+                        for (int s2 = 1; s2 < nseg_used; ++s2) pi += psum[(size_t)s2 * ldv + i];
                         for (int l = 0; l < jj; ++l) pi -= Vs[l * ldv + i] * dots[l] + Ws[l * ldv + i] * dots[jj + l];
                         pi *= tau;
                         pv[i] = pi;
@@ -565,19 +584,20 @@ __global__ void __launch_bounds__(NT, 1) tri_reduce_res_kernel(TriReduceParams<f
                     Ws[jj * ldv + i] = (i > j && i < n) ? pv[i] - K * Vs[jj * ldv + i] : 0.0f;
                 __syncthreads();
             }
-            // ---- trailing update of the stored blocks (I >= K >= t0 / 4): B -= V W^T + W V^T,
-            //      one 4 x 4 block per thread, v, w of both quads as 16-byte vectors
+            // ---- trailing update of the stored blocks (I >= K >= t0 / 4): B -= V W^T + W V^T;
+            //      a warp takes one column quad K and 32 consecutive row quads I (lanes), so
+            //      the v, w of the rows and the blocks themselves are contiguous across the
+            //      lanes and the v, w of the columns are broadcast
             const int t0 = j0 + nbp;
             if (t0 < n) {
                 const int qa = t0 >> 2;
-                const int m = nq - qa;
-                const int ntile = m * (m + 1) / 2;
-                for (int tile = tid; tile < ntile; tile += NT) {
-                    int qi = (int)((sqrtf(8.0f * tile + 1.0f) - 1.0f) * 0.5f);
-                    while ((qi + 1) * (qi + 2) / 2 <= tile) ++qi;
-                    while (qi * (qi + 1) / 2 > tile) --qi;
-                    const int qc = tile - qi * (qi + 1) / 2;
-                    const int i = 4 * (qa + qi), c0 = 4 * (qa + qc);
+                const int nitems = (nq - qa) * ((nq - qa + 31) >> 5);
+                const int gpk = (nq - qa + 31) >> 5;             // row groups per column quad
+                for (int item = warp; item < nitems; item += NW) {
+                    const int K = qa + item / gpk, gr = item % gpk;
+                    const int I = K + 32 * gr + lane;
+                    if (I >= nq) continue;
+                    const int i = 4 * I, c0 = 4 * K;
                     float acc[4][4];
 #pragma unroll
                     for (int c = 0; c < 4; ++c)
@@ -594,9 +614,11 @@ __global__ void __launch_bounds__(NT, 1) tri_reduce_res_kernel(TriReduceParams<f
 #pragma unroll
                             for (int r = 0; r < 4; ++r) acc[c][r] = fmaf(vi[r], wk[c], fmaf(wi[r], vk[c], acc[c][r]));
                     }
+                    const int4 cK = *reinterpret_cast<const int4*>(cst + c0);
+                    const int cc[4] = {cK.x, cK.y, cK.z, cK.w};
 #pragma unroll
                     for (int c = 0; c < 4; ++c) {
-                        float* dst = Ls + res_at(i, c0 + c, ld);
+                        float* dst = Ls + cc[c] + i - c0;
                         float x[4];
                         ld4(dst, x);
 #pragma unroll
@@ -859,6 +881,11 @@ __device__ __forceinline__ void res_stage(float* Vs, const float* Aw, long long 
     cp_commit();
 }
 
+constexpr int kTfSplit = 4;                   // row ranges of V^T V in the T-factor kernel
+
+// scratch of the partial blocks of V^T V, in floats (aliases T and what follows it)
+__host__ __device__ inline int tf_part_elems(int nb) { return kTfSplit * (nb / 4) * (nb / 4 + 1) / 2 * 16; }
+
 struct TriTParams {
     int nwin;
     int maxp;                // panels per window at most
@@ -879,7 +906,7 @@ __global__ void __launch_bounds__(128) tri_tfactor_kernel(TriTParams p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float* const Vs = reinterpret_cast<float*>(smem_raw);      // [ldv][NB]
     float* const Gm = Vs + (size_t)p.ldv * NB;                  // [NB][NB]
-    float* const Tm = Gm + NB * NB;                              // [NB][NB]
+    float* const Tm = Gm + NB * NB;                              // [NB][NB]; the partial blocks of G first
     const int w = blockIdx.x / p.maxp, panel = blockIdx.x % p.maxp;
     const int n = p.n_w[w];
     const int j0 = panel * NB;
@@ -890,25 +917,51 @@ __global__ void __launch_bounds__(128) tri_tfactor_kernel(TriTParams p) {
     res_stage<128, NB>(Vs, p.A + p.offA[w], ld, j0, nbp, nk);
     cp_wait<0>();
     __syncthreads();
-    for (int q = tid; q < NB * NB / 4; q += 128) {
-        const int a0 = 2 * (q / (NB / 2)), b0 = 2 * (q % (NB / 2));
-        float g00 = 0.0f, g01 = 0.0f, g10 = 0.0f, g11 = 0.0f;
-        if (b0 + 1 > a0) {
-            for (int kk = 0; kk < nk; ++kk) {
-                const float va0 = Vs[res_index<NB>(kk, a0)], va1 = Vs[res_index<NB>(kk, a0 + 1)];
-                const float vb0 = Vs[res_index<NB>(kk, b0)], vb1 = Vs[res_index<NB>(kk, b0 + 1)];
-                g00 = fmaf(va0, vb0, g00);
-                g01 = fmaf(va0, vb1, g01);
-                g10 = fmaf(va1, vb0, g10);
-                g11 = fmaf(va1, vb1, g11);
+    // G = V^T V by 4 x 4 blocks on or above the diagonal (16-byte reads of the staged rows),
+    // the rows split into kTfSplit ranges whose partial blocks are added in range order
+    {
+        constexpr int NQ = NB / 4, NTILE = NQ * (NQ + 1) / 2;
+        float* const part = Tm;                                  // [kTfSplit][NTILE][16] scratch
+        for (int item = tid; item < NTILE * kTfSplit; item += 128) {
+            const int tile = item % NTILE, sp = item / NTILE;
+            int qa = 0, rem = tile;                              // tile-th (qa <= qb) pair
+            while (rem >= NQ - qa) {
+                rem -= NQ - qa;
+                ++qa;
             }
+            const int qb = qa + rem;
+            const int k0 = nk * sp / kTfSplit, k1 = nk * (sp + 1) / kTfSplit;
+            float g[4][4] = {};
+            for (int kk = k0; kk < k1; ++kk) {
+                const float4 x = *reinterpret_cast<const float4*>(Vs + kk * NB + (((qa ^ (kk >> 2)) & (NQ - 1)) << 2));
+                const float4 y = *reinterpret_cast<const float4*>(Vs + kk * NB + (((qb ^ (kk >> 2)) & (NQ - 1)) << 2));
+                const float xa[4] = {x.x, x.y, x.z, x.w}, yb[4] = {y.x, y.y, y.z, y.w};
+#pragma unroll
+                for (int r = 0; r < 4; ++r)
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) g[r][c] = fmaf(xa[r], yb[c], g[r][c]);
+            }
+            float* dst = part + ((size_t)sp * NTILE + tile) * 16;
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+#pragma unroll
+                for (int c = 0; c < 4; ++c) dst[r * 4 + c] = g[r][c];
         }
-        Gm[a0 * NB + b0] = g00;
-        Gm[a0 * NB + b0 + 1] = g01;
-        Gm[(a0 + 1) * NB + b0] = g10;
-        Gm[(a0 + 1) * NB + b0 + 1] = g11;
+        __syncthreads();
+        for (int item = tid; item < NTILE * 16; item += 128) {
+            const int tile = item / 16, e = item % 16;
+            int qa = 0, rem = tile;
+            while (rem >= NQ - qa) {
+                rem -= NQ - qa;
+                ++qa;
+            }
+            const int qb = qa + rem;
+            float s = 0.0f;
+            for (int sp = 0; sp < kTfSplit; ++sp) s += part[((size_t)sp * NTILE + tile) * 16 + e];
+            Gm[(4 * qa + e / 4) * NB + 4 * qb + e % 4] = s;
+        }
+        __syncthreads();
     }
-    __syncthreads();
     const float* tw = p.tau + p.offN[w];
     if (tid < 32) {
         for (int l = 0; l < NB; ++l) {
@@ -1422,7 +1475,7 @@ int tri_pick(bool fp32, int nmax, size_t smem_budget, int cfg, TriPick* out) {
     r.nt = t.nt;
     if (t.rres && fp32 && nmax <= kResReduceMaxN)
         for (int b : {16, 8, 4})
-            if (b <= t.nb && !r.nb && res_reduce_smem_elems(b, r.ldv, nmax) * el <= smem_budget) {
+            if (b <= t.nb && !r.nb && (res_reduce_smem_elems(b, r.ldv, nmax) + r.ldv) * el <= smem_budget) {
                 r.nb = b;
                 r.nt = kResReduceNT;
                 r.rres = 1;
@@ -1478,15 +1531,20 @@ int tri_reduce(bool fp32, int nwin, const int* order, int* counter, const int* n
         TriReduceParams<float> p{nwin, order, counter, n_w, offC, offA, offN, (const float*)H, (float*)A,
                                  (float*)d, (float*)e, (float*)tau, status, nb, ldv};
         if (pk.rres) {
-            const size_t smem = res_reduce_smem_elems(nb, ldv, nmax) * sizeof(float);
-            if (smem > smem_budget || nmax > kResReduceMaxN) {
-                lres_set_error("resident tridiagonal reduction needs %zu B of shared memory", smem);
+            // as many partial-sum rows of p = A v (one per column segment) as fit, at most a warp each
+            const size_t fixed = res_reduce_smem_elems(nb, ldv, nmax) * sizeof(float);
+            const int nseg = fixed + sizeof(float) * ldv > smem_budget
+                                 ? 0
+                                 : (int)std::min<size_t>(kResReduceNT / 32, (smem_budget - fixed) / (sizeof(float) * ldv));
+            if (nseg < 1 || nmax > kResReduceMaxN) {
+                lres_set_error("resident tridiagonal reduction needs %zu B of shared memory", fixed + sizeof(float) * ldv);
                 return LRES_EINVAL;
             }
+            const size_t smem = fixed + sizeof(float) * (size_t)nseg * ldv;
             int per_sm = 0;
             if (int rc = prepare_kernel<tri_reduce_res_kernel<kResReduceNT>>(kResReduceNT, smem, &per_sm)) return rc;
             const int grid = std::min(nwin, std::max(1, per_sm) * device_sms());
-            tri_reduce_res_kernel<kResReduceNT><<<grid, kResReduceNT, smem, s>>>(p, nmax);
+            tri_reduce_res_kernel<kResReduceNT><<<grid, kResReduceNT, smem, s>>>(p, nmax, nseg);
             LRES_CUDA_TRY(cudaGetLastError());
             return LRES_OK;
         }
@@ -1527,7 +1585,7 @@ static int dispatch_apply(const TriApplyParams<R>& p, int nb, int rpt, cudaStrea
 template <int NB>
 static int launch_apply_res(const TriApplyParams<float>& p, const TriTParams& tp, int rows, size_t smem_budget,
                             cudaStream_t s) {
-    const size_t smem_t = sizeof(float) * ((size_t)p.ldv * NB + 2 * NB * NB);
+    const size_t smem_t = sizeof(float) * ((size_t)p.ldv * NB + NB * NB + std::max(NB * NB, tf_part_elems(NB)));
     const size_t smem = res_smem_bytes(NB, p.ldv, rows);
     if (smem > smem_budget || rows > kResRows || rows % 32) {
         lres_set_error("resident row application needs %zu B of shared memory", smem);
