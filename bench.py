@@ -115,6 +115,9 @@ def kernel_work(name, nW, mW, P, nnz_h):
     return None, None
 
 
+FP32_SIMT_TFLOPS = round(152 * 128 * 2 * 2.07e9 / 1e12, 1)     # 80.5
+
+
 def roofline_of(name, ms, nW, mW, P, nnz_h, peaks):
     kind, work = kernel_work(name, nW, mW, P, nnz_h)
     if kind is None:
@@ -122,10 +125,14 @@ def roofline_of(name, ms, nW, mW, P, nnz_h, peaks):
     if kind == "flop":
         achieved = work / (ms / 1e3) / 1e12
         peak = peaks.get("bf16_tflops_sustained") if peaks else 1700.0
+        # these kernels run on the FP32 SIMT pipes; their own ceiling beside the tensor peak
+        simt = FP32_SIMT_TFLOPS
         return {"bound": "tensor", "achieved": round(achieved, 3), "peak": peak, "unit": "TFLOP/s",
                 "frac": round(achieved / peak, 5), "traffic": None, "kernel_ms": round(ms, 3),
                 "algorithmic_flop_per_launch": work,
-                "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (of measured)" if peaks else "fallback"}
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (of measured)" if peaks else "fallback",
+                "fp32_simt": {"peak": simt, "frac": round(achieved / simt, 4),
+                              "peak_source": "nominal: 152 SMs x 128 FP32 FMA/clk x 2 x 2.07 GHz"}}
     achieved = work / (ms / 1e3) / 1e9
     peak = peaks.get("hbm_gbs") if peaks else 6800.0
     return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
@@ -134,10 +141,14 @@ def roofline_of(name, ms, nW, mW, P, nnz_h, peaks):
             "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback"}
 
 
-def launches_per_step(route, precision):
+def launches_per_step(route, precision, tile_config=0):
     """Our kernels in one step (H(v) + window blocks + standard form + pass)."""
     if route == "tridiag":
-        # assemble_h, gather, 2 standard-form GEMMs, reduction, rows, pole nodes, pass, window sums
+        # assemble_h, gather, 2 standard-form GEMMs, reduction, rows, pole nodes, pass, window
+        # sums; mixed: + the FP32 potential per slot, + V^T V and the T factors of the
+        # resident-row application (every configuration but 2)
+        if precision == "mixed":
+            return 10 + 2 * (tile_config != 2)
         return 9
     # assemble_h, gather, [split + 2 double-float GEMMs], pole nodes, LDL^T kernel, pole sums
     return 8 if precision == "mixed" else 5
@@ -248,7 +259,7 @@ def run_ours(args):
     mW = np.array([len(o) for o in s.ctx_own])
     P = s.M // 2
     units = len(s.nW) * P
-    lps = launches_per_step(route, args.precision)
+    lps = launches_per_step(route, args.precision, s.tile_config if isinstance(s.tile_config, int) else 0)
 
     def step():
         s.set_potential_device(v_dev.data_ptr())

@@ -30,8 +30,9 @@
 //                      rows resident in shared memory through all panels: Y = F^ Q by
 //                      panels in compact WY form, Y <- Y - ((Y V) T_p) V^T, 4 x 4 register
 //                      tiles.  Algorithmic work 2 m n^2 flops per window.
-//   tri_tfactor_kernel one CTA per (window, panel): the T_p of the compact WY form, once
-//                      per Hamiltonian for all row sets.
+//   tri_gram_kernel / tri_tfactor_kernel   per (window, panel): V^T V (one CTA), then the
+//                      T_p of the compact WY form (one warp), once per Hamiltonian for all
+//                      row sets.
 //   tri_apply_kernel   one CTA per (window, block of up to 256 rows), one thread per row,
 //                      the rows re-read from global memory per panel (FP64 path, and the
 //                      configurations without resident rows).
@@ -585,18 +586,19 @@ __global__ void __launch_bounds__(NT, 1) tri_reduce_res_kernel(TriReduceParams<f
                 __syncthreads();
             }
             // ---- trailing update of the stored blocks (I >= K >= t0 / 4): B -= V W^T + W V^T;
-            //      a warp takes one column quad K and 32 consecutive row quads I (lanes), so
-            //      the v, w of the rows and the blocks themselves are contiguous across the
-            //      lanes and the v, w of the columns are broadcast
+            //      the blocks in column order from the last column quad, consecutive threads
+            //      on consecutive row quads of one column quad, so that the v, w of the rows
+            //      and the blocks are contiguous across a warp and those of the columns broadcast
             const int t0 = j0 + nbp;
             if (t0 < n) {
                 const int qa = t0 >> 2;
-                const int nitems = (nq - qa) * ((nq - qa + 31) >> 5);
-                const int gpk = (nq - qa + 31) >> 5;             // row groups per column quad
-                for (int item = warp; item < nitems; item += NW) {
-                    const int K = qa + item / gpk, gr = item % gpk;
-                    const int I = K + 32 * gr + lane;
-                    if (I >= nq) continue;
+                const int m = nq - qa;
+                const int ntile = m * (m + 1) / 2;
+                for (int tile = tid; tile < ntile; tile += NT) {
+                    int u = (int)((sqrtf(8.0f * tile + 1.0f) - 1.0f) * 0.5f);
+                    while ((u + 1) * (u + 2) / 2 <= tile) ++u;
+                    while (u * (u + 1) / 2 > tile) --u;
+                    const int K = qa + m - 1 - u, I = K + tile - u * (u + 1) / 2;
                     const int i = 4 * I, c0 = 4 * K;
                     float acc[4][4];
 #pragma unroll
@@ -852,7 +854,7 @@ __global__ void __launch_bounds__(NT, RPT == 1 && NB <= 16 ? 3 : 1) tri_apply_ke
 // quads, so that every 16-byte shared load serves a broadcast or one conflict-free
 // wavefront), S <- S T (same tiles), Y <- Y - S V^T (a thread = 4 rows x 4 columns; a warp =
 // 8 row quads x 4 column quads).  The T factor of every (window, panel) is formed once per
-// Hamiltonian by tri_tfactor_kernel.
+// Hamiltonian by tri_gram_kernel and tri_tfactor_kernel.
 
 constexpr int kResRows = 128;                 // rows of an item of the resident application
 constexpr int kResNT = 256;
@@ -902,7 +904,7 @@ struct TriTParams {
 // T of the compact WY form of one panel, Q_p = I - V T V^T: T_ll = tau_l,
 // T[0:l, l] = -tau_l T[0:l, 0:l] (V^T V)[0:l, l].  One CTA per (window, panel).
 template <int NB>
-__global__ void __launch_bounds__(128) tri_tfactor_kernel(TriTParams p) {
+__global__ void __launch_bounds__(128) tri_gram_kernel(TriTParams p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float* const Vs = reinterpret_cast<float*>(smem_raw);      // [ldv][NB]
     float* const Gm = Vs + (size_t)p.ldv * NB;                  // [NB][NB]
@@ -962,27 +964,44 @@ __global__ void __launch_bounds__(128) tri_tfactor_kernel(TriTParams p) {
         }
         __syncthreads();
     }
-    const float* tw = p.tau + p.offN[w];
-    if (tid < 32) {
-        for (int l = 0; l < NB; ++l) {
-            const float tl = l < nbp ? tw[j0 + l] : 0.0f;
-            for (int a = tid; a < NB; a += 32) {
-                float val = 0.0f;
-                if (a < l) {
-                    float sacc = 0.0f;
-                    for (int b = a; b < l; ++b) sacc = fmaf(Tm[a * NB + b], Gm[b * NB + l], sacc);
-                    val = -tl * sacc;
-                } else if (a == l) {
-                    val = tl;
-                }
-                Tm[a * NB + l] = val;
-            }
-            __syncwarp();
-        }
-    }
-    __syncthreads();
+    // G (the blocks on and above the diagonal) into the panel's T slot; tri_tfactor_kernel
+    // turns it into T in place
+    float* Gw = p.T + (long long)w * p.tstride + (long long)panel * NB * NB;
+    for (int i = tid; i < NB * NB; i += 128) Gw[i] = Gm[i];
+}
+
+// T of the compact WY form of one panel from its G = V^T V (in the T slot), one warp per
+// (window, panel): T_ll = tau_l, T[0:l, l] = -tau_l T[0:l, 0:l] G[0:l, l].  The recurrence is
+// sequential in l; a warp per panel keeps many panels in flight on each SM.
+template <int NB>
+__global__ void __launch_bounds__(32) tri_tfactor_kernel(TriTParams p) {
+    __shared__ float Gm[NB * NB], Tm[NB * NB];
+    const int w = blockIdx.x / p.maxp, panel = blockIdx.x % p.maxp;
+    const int n = p.n_w[w];
+    const int j0 = panel * NB;
+    if (n > p.ldv || j0 >= n - 2) return;
+    const int tid = threadIdx.x;
+    const int nbp = min(NB, n - 2 - j0);
     float* Tw = p.T + (long long)w * p.tstride + (long long)panel * NB * NB;
-    for (int i = tid; i < NB * NB; i += 128) Tw[i] = Tm[i];
+    for (int i = tid; i < NB * NB; i += 32) Gm[i] = Tw[i];
+    __syncwarp();
+    const float* tw = p.tau + p.offN[w];
+    for (int l = 0; l < NB; ++l) {
+        const float tl = l < nbp ? tw[j0 + l] : 0.0f;
+        for (int a = tid; a < NB; a += 32) {
+            float val = 0.0f;
+            if (a < l) {
+                float sacc = 0.0f;
+                for (int b = a; b < l; ++b) sacc = fmaf(Tm[a * NB + b], Gm[b * NB + l], sacc);
+                val = -tl * sacc;
+            } else if (a == l) {
+                val = tl;
+            }
+            Tm[a * NB + l] = val;
+        }
+        __syncwarp();
+    }
+    for (int i = tid; i < NB * NB; i += 32) Tw[i] = Tm[i];
 }
 
 inline size_t res_smem_bytes(int nb, int ldv, int rows) {
@@ -1196,6 +1215,10 @@ __device__ __forceinline__ float4 df_split(double2 a) {
     return make_float4(rh, (float)(a.x - (double)rh), ih, (float)(a.y - (double)ih));
 }
 
+// 1 / x correctly rounded (the value of R(1) / x)
+__device__ __forceinline__ float rcp_rn(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double rcp_rn(double x) { return __drcp_rn(x); }
+
 template <class R, int NT, int RR>
 __global__ void __launch_bounds__(NT) tri_pass_kernel(TriPassParams<R> p) {
     using C = typename Cplx<R>::T;
@@ -1288,7 +1311,7 @@ __global__ void __launch_bounds__(NT) tri_pass_kernel(TriPassParams<R> p) {
                         t = C{ei * gp.x, ei * gp.y};
                         D = C{z.x - di - ei * t.x, z.y - ei * t.y};
                     }
-                    const R inv = R(1) / (D.x * D.x + D.y * D.y);
+                    const R inv = rcp_rn(D.x * D.x + D.y * D.y);
                     gp = C{D.x * inv, -D.y * inv};
                     const R* yi = yc + (size_t)(i - i0) * RB;
 #pragma unroll
@@ -1593,8 +1616,10 @@ static int launch_apply_res(const TriApplyParams<float>& p, const TriTParams& tp
     }
     int per_sm = 0;
     if (tp.maxp > 0 && tp.nwin > 0) {
-        if (int rc = prepare_kernel<tri_tfactor_kernel<NB>>(128, smem_t, &per_sm)) return rc;
-        tri_tfactor_kernel<NB><<<(unsigned)tp.nwin * tp.maxp, 128, smem_t, s>>>(tp);
+        if (int rc = prepare_kernel<tri_gram_kernel<NB>>(128, smem_t, &per_sm)) return rc;
+        tri_gram_kernel<NB><<<(unsigned)tp.nwin * tp.maxp, 128, smem_t, s>>>(tp);
+        LRES_CUDA_TRY(cudaGetLastError());
+        tri_tfactor_kernel<NB><<<(unsigned)tp.nwin * tp.maxp, 32, 0, s>>>(tp);
         LRES_CUDA_TRY(cudaGetLastError());
     }
     if (int rc = prepare_kernel<tri_apply_res_kernel<NB>>(kResNT, smem, &per_sm)) return rc;
