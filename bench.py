@@ -234,6 +234,7 @@ def run_ours(args):
         WORKLOAD.update(parallelism=f"{world} replicas")
     s = LResGPU(b, cr.pos, R_w=8.0, M=64, precision=args.precision, route=args.route,
                 tile_config="auto" if args.tile_config is None else args.tile_config)
+    s.set_standard_form(args.standard_form)
     route = s.route
     go = GridOps(s)
     vion = go.ion_potential()
@@ -363,7 +364,8 @@ def run_ours(args):
     mixed = args.precision == "mixed"
     cfg = s.tile_config if isinstance(s.tile_config, int) else 0
     kernel_names = {"pole_kernel": "tri_pass_kernel" if route == "tridiag" else "ldl_left_kernel",
-                    "transform": "gemm_f32blk_kernel" if (route == "tridiag" and mixed)
+                    "transform": ("gemm_tc_kernel" if args.standard_form == "tensor" else "gemm_f32blk_kernel")
+                    if (route == "tridiag" and mixed)
                     else ("gemm_f64_kernel" if args.precision == "fp64" else "gemm_df64_kernel"),
                     "tri_reduce": "tri_reduce_res_kernel" if (mixed and cfg in (1, 5)) else "tri_reduce_kernel",
                     "tri_rows": "tri_apply_res_kernel" if (mixed and cfg != 2) else "tri_apply_kernel",
@@ -406,6 +408,7 @@ def run_ours(args):
                             "tflops_per_s": round(flops_step / (ms_step / 1e3) / 1e12, 2)},
         "clocks": clk,
         "breakdown_ms": breakdown,
+        "standard_form": s.standard_form,
         "tile_config": {"chosen": s.tile_config,
                         "ms_per_config": None if getattr(s, "tune_ms", None) is None
                         else [round(float(x), 3) for x in s.tune_ms]},
@@ -586,6 +589,8 @@ def main():
                     help="skip the band-energy adjoint leg (mixed and FP64)")
     ap.add_argument("--cells", type=int, default=8, help="crystal of cells^3 H2 (8 = the benchmark workload)")
     ap.add_argument("--tile-config", type=int, default=None, help="force a pole-kernel tile configuration")
+    ap.add_argument("--standard-form", choices=["simt", "tensor"], default="simt",
+                    help="kernel of the mixed standard form (SIMT FP32 GEMMs or tcgen05 3xTF32)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

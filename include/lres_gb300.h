@@ -156,6 +156,18 @@ int lres_autotune(lres_ctx* ctx, double mu, double e_lo, int32_t force_config, i
 int lres_set_route(lres_ctx* ctx, int32_t route, void* stream);
 int lres_get_route(lres_ctx* ctx, int32_t* route);
 
+/* Kernel of the FP32 standard form A = L^-1 H_W L^-T of the LRES_MIXED tridiagonal route:
+ * LRES_SF_SIMT, batched FP32 GEMMs on the SIMT pipes; LRES_SF_TENSOR, the same products on
+ * the tensor cores (tcgen05.mma kind::tf32, operands split into TF32 pairs, hi.hi + hi.lo +
+ * lo.hi, accumulated from zero per 32-term chunk in tensor memory and across chunks in FP32,
+ * as the SIMT kernels block their sums).  Takes effect at the next Hamiltonian
+ * (lres_set_potential / lres_set_hamiltonian_csr / lres_set_windows); no other route or
+ * precision uses it.  A timed-out completion wait of the tensor cores is reported by the
+ * next pass as status bit 4 (LRES_EINVAL). */
+enum { LRES_SF_SIMT = 0, LRES_SF_TENSOR = 1 };
+int lres_set_standard_form_kernel(lres_ctx* ctx, int32_t kind);
+int lres_get_standard_form_kernel(lres_ctx* ctx, int32_t* kind);
+
 /* Device time (ms, CUDA events on the launching stream) of the most recent launch of:
  * ms[0] the pole kernel (LDL^T kernel, or the shifted tridiagonal solves), ms[1] the pole
  * sums, ms[2] the H(v) assembly, ms[3] the window gather, ms[4] the standard-form transform,

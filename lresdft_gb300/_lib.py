@@ -15,6 +15,7 @@ LIB_PATH = os.path.join(HERE, "liblres_gb300.so")
 
 LRES_FP64, LRES_MIXED = 0, 1
 LRES_ROUTE_LDL, LRES_ROUTE_TRIDIAG = 0, 1
+LRES_SF_SIMT, LRES_SF_TENSOR = 0, 1
 ERRORS = {-22: "EINVAL", -12: "ENOMEM", -5: "ECUDA", -33: "ENUMERIC", -71: "ESTATE"}
 
 EXPORTS = ("lres_version", "lres_last_error", "lres_ctx_create", "lres_ctx_destroy", "lres_set_potential",
@@ -23,7 +24,7 @@ EXPORTS = ("lres_version", "lres_last_error", "lres_ctx_create", "lres_ctx_destr
            "lres_voronoi_owner", "lres_lda_xc", "lres_hartree", "lres_ion_potential", "lres_inertia_noalloc",
            "lres_set_windows", "lres_window_ptrs", "lres_adjoint", "lres_owned_gram", "lres_set_trace_rows",
            "lres_basis_build", "lres_basis_fetch", "lres_basis_free", "lres_basis_tabulate",
-           "lres_ks_density")
+           "lres_ks_density", "lres_set_standard_form_kernel", "lres_get_standard_form_kernel")
 
 
 class LResError(RuntimeError):
@@ -90,6 +91,8 @@ def _load():
         "lres_basis_tabulate": (i32, [i64, PD, C.POINTER(C.c_int32), C.POINTER(C.c_int32), PD, P64, PD, dbl, dbl,
                                       dbl, P64, P64, PD]),
         "lres_ks_density": (i32, [i64, P64, P64, PD, P64, P64, PD, i64, P64, P64, PD, C.c_int32, PD, PD, PD]),
+        "lres_set_standard_form_kernel": (i32, [vp, C.c_int32]),
+        "lres_get_standard_form_kernel": (i32, [vp, C.POINTER(C.c_int32)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

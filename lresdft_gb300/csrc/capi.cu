@@ -100,6 +100,7 @@ struct lres_ctx {
     int route = LRES_ROUTE_LDL;
     bool tri_alloc = false, tri_ready = false;
     TriPick tri;                                 // tile configuration (tri_pick)
+    int sf_kind = LRES_SF_SIMT;                  // kernel of the FP32 standard form
     int tri_cfg = 0;
     float* d_triT = nullptr;                     // T factors of the resident row application
     long long triT_size = 0;
@@ -343,8 +344,15 @@ int transform_f32(lres_ctx* c, cudaStream_t s) {
     // Y = H L^-T (B = L^-T given k-major: its transpose L^-1), written row-major (k-major for
     // the next product); A^ = lower(L^-1 Y)
     float* Y = reinterpret_cast<float*>(c->d_Y_df);
-    TRY(batched_gemm_f32(c->nwin, c->d_n, c->d_offC, c->nmax, 1, c->d_HW, true, c->d_Linv32, Y, true, s));
-    TRY(batched_gemm_f32(c->nwin, c->d_n, c->d_offC, c->nmax, 2, c->d_Linv32, false, Y, tri_hhat32(c), false, s));
+    if (c->sf_kind == LRES_SF_TENSOR && c->d_tstatus) {
+        TRY(batched_gemm_tc(c->nwin, c->d_n, c->d_offC, c->nmax, 1, c->d_HW, true, c->d_Linv32, Y, true, c->d_tstatus,
+                            s));
+        TRY(batched_gemm_tc(c->nwin, c->d_n, c->d_offC, c->nmax, 2, c->d_Linv32, false, Y, tri_hhat32(c), false,
+                            c->d_tstatus, s));
+    } else {
+        TRY(batched_gemm_f32(c->nwin, c->d_n, c->d_offC, c->nmax, 1, c->d_HW, true, c->d_Linv32, Y, true, s));
+        TRY(batched_gemm_f32(c->nwin, c->d_n, c->d_offC, c->nmax, 2, c->d_Linv32, false, Y, tri_hhat32(c), false, s));
+    }
     c->hhat_df = false;                  // d_Hhat32 no longer follows H_W
     return LRES_OK;
 }
@@ -1342,6 +1350,24 @@ extern "C" int lres_set_route(lres_ctx* c, int32_t route, void* stream) {
         return rc;
     }
     LRES_CUDA_TRY(cudaStreamSynchronize(s));
+    return LRES_OK;
+}
+
+extern "C" int lres_set_standard_form_kernel(lres_ctx* c, int32_t kind) {
+    if (!c || (kind != LRES_SF_SIMT && kind != LRES_SF_TENSOR)) {
+        lres_set_error("standard-form kernel must be LRES_SF_SIMT or LRES_SF_TENSOR");
+        return LRES_EINVAL;
+    }
+    c->sf_kind = kind;
+    return LRES_OK;
+}
+
+extern "C" int lres_get_standard_form_kernel(lres_ctx* c, int32_t* kind) {
+    if (!c || !kind) {
+        lres_set_error("null argument");
+        return LRES_EINVAL;
+    }
+    *kind = c->sf_kind;
     return LRES_OK;
 }
 

@@ -109,6 +109,10 @@ int batched_gemm_df64(int nwin, const int* n_w, const long long* off, int nmax, 
 // B[k][j]), C column-major or row-major (c_rowmajor); klim as batched_gemm.
 int batched_gemm_f32(int nwin, const int* n_w, const long long* off, int nmax, int klim, const void* A, bool a_f64,
                      const float* Bt, float* C, bool c_rowmajor, cudaStream_t s);
+// batched_gemm_f32's products on the tensor cores (tcgen05, 3xTF32, 32-term chunks); a timed-out
+// completion wait sets ST_TIMEOUT in *status (device)
+int batched_gemm_tc(int nwin, const int* n_w, const long long* off, int nmax, int klim, const void* A, bool a_f64,
+                    const float* Bt, float* C, bool c_rowmajor, int* status, cudaStream_t s);
 int batched_transpose_f32(int nwin, const int* n_w, const long long* off, int nmax, const float* A, float* B,
                           cudaStream_t s);
 int pole_sums(int nwin, const long long* offQ, const int* m_w, const long long* Oflat, bool fp32,

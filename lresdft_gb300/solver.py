@@ -263,6 +263,19 @@ class LResGPU:
         _lib.check(_lib.lib.lres_get_route(self._ctx, C.byref(r)))
         return "tridiag" if r.value == _lib.LRES_ROUTE_TRIDIAG else "ldl"
 
+    @property
+    def standard_form(self):
+        """Kernel of the mixed tridiagonal route's FP32 standard form: "simt" or "tensor"."""
+        r = C.c_int32()
+        _lib.check(_lib.lib.lres_get_standard_form_kernel(self._ctx, C.byref(r)))
+        return "tensor" if r.value == _lib.LRES_SF_TENSOR else "simt"
+
+    def set_standard_form(self, kind):
+        """Run the FP32 standard form on the SIMT pipes ("simt") or the tensor cores
+        ("tensor"); takes effect at the next Hamiltonian."""
+        code = {"simt": _lib.LRES_SF_SIMT, "tensor": _lib.LRES_SF_TENSOR}[kind]
+        _lib.check(_lib.lib.lres_set_standard_form_kernel(self._ctx, code))
+
     def set_route(self, route):
         """Switch the route of the pole solves ("tridiag" or "ldl")."""
         code = {"tridiag": _lib.LRES_ROUTE_TRIDIAG, "ldl": _lib.LRES_ROUTE_LDL}[route]

@@ -64,6 +64,23 @@ def test_mixed_pass_within_gate_at_1024_electrons(jit8):
     s.close()
 
 
+def test_mixed_tensor_core_standard_form_at_1024_electrons(jit8):
+    """The mixed pass with the standard form on the tensor cores (tcgen05, 3xTF32): within the
+    same gates as the SIMT standard form."""
+    from lresdft_gb300 import LResGPU
+    g, cr, b, v = jit8
+    s = LResGPU(b, cr.pos, R_w=8.0, M=64, precision="mixed")
+    s.set_standard_form("tensor")
+    s.set_potential(v)
+    dens, N, eb = s.pole_pass(float(g["mu"]), float(g["e_lo"]))
+    err_e = abs(eb - float(g["eband"])) / cr.n_elec
+    err_d = float(np.max(np.abs(dens.ravel()[g["sample"]] - g["dens_sample"])))
+    print("mixed, tensor-core standard form: band energy per electron", err_e, "density", err_d)
+    assert err_e < 2e-7 and err_d < 1e-6
+    assert abs(N - cr.n_elec) / cr.n_elec < 1e-6
+    s.close()
+
+
 def test_density_call_reproduces_reference_cold_call(jit8):
     """The drop-in protocol at 1024 electrons: a cold density() call finds the reference's
     e_lo and mu and its density (FP64)."""

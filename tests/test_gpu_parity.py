@@ -291,6 +291,29 @@ def test_every_tile_configuration_matches_reference(systems, name, config):
 
 
 @pytest.mark.parametrize("name", CASES)
+def test_tensor_core_standard_form(systems, name):
+    """The mixed standard form on the tensor cores (tcgen05, 3xTF32, 32-term chunks) against the
+    SIMT kernels and the reference: the band energy within the 2e-7 Ha/electron gate, the
+    density norm within 1e-6, the two kernels within 2e-8 Ha/electron of each other, and no
+    tensor-core completion timeout (status 0)."""
+    g, cr, b = systems[name]
+    v = g["v"].reshape(cr.shape)
+    ne = cr.n_elec
+    res = {}
+    for kind in ("simt", "tensor"):
+        s = _solver(b, cr, g, "mixed", route="tridiag")
+        s.set_standard_form(kind)
+        assert s.standard_form == kind
+        s.set_potential(v)
+        dens, N, eb = s.pole_pass(float(g["cold_mu"]), float(g["cold_elo"]))
+        assert abs(eb - g["cold_eband"]) / ne < 2e-7
+        assert np.sqrt(np.sum((dens - g["cold_dens"]) ** 2) * cr.dV) / ne < 1e-6
+        res[kind] = (dens, eb)
+        s.close()
+    assert abs(res["tensor"][1] - res["simt"][1]) / ne < 2e-8
+
+
+@pytest.mark.parametrize("name", CASES)
 @pytest.mark.parametrize("config", [0, 1, 2, 3, 4, 5])
 def test_every_tridiagonal_configuration_matches_reference(systems, name, config):
     """Each configuration of the tridiagonal route, forced (reduction with the window in
