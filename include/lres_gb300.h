@@ -210,11 +210,11 @@ int lres_voronoi_owner(const int64_t shape[3], const double cell[3], int64_t nce
  * over eight CTAs: on many windows this runs several times slower than lres_inertia.
  * Returns LRES_ENUMERIC when some window meets a zero or non-finite pivot (NaN or Inf in
  * H or S, or sigma exactly on an eigenvalue); its counts are then meaningless.  The
- * first call on each device looks up the array's device address (once per device; make
- * that first call before any stream capture).  All calls on a device share the array
- * and reset its work queue and status at the start: calls that overlap on the GPU race
- * and must be serialised by the caller (one stream, or events).  Waits for the stream to
- * read the kernel status. */
+ * first call on each device looks up the array's device address (once per device).  All
+ * calls on a device share the array and reset its work queue and status at the start:
+ * calls that overlap on the GPU race and must be serialised by the caller (one stream, or
+ * events).  Every call waits for the stream to read the kernel status back, so it cannot
+ * be captured in a CUDA graph. */
 int lres_inertia_noalloc(int32_t nwin, const int32_t* n_w, const int64_t* offC, const double* H, const double* S,
                          double sigma, int32_t* below, int32_t nmax, void* stream);
 
