@@ -873,12 +873,17 @@ __device__ __forceinline__ int res_index(int kk, int l) {
 // once), the zeros and ones by plain stores; the caller waits (cp_wait) before the barrier.
 template <int NT, int NB>
 __device__ __forceinline__ void res_stage(float* Vs, const float* Aw, long long ld, int j0, int nbp, int nk) {
-    for (int idx = threadIdx.x; idx < nk * NB; idx += NT) {
-        const int l = idx / nk, kk = idx % nk, k = j0 + 1 + kk;
+    // warp per reflector column, lanes down its rows (no division by nk)
+    const int lane = threadIdx.x & 31;
+    for (int l = threadIdx.x >> 5; l < NB; l += NT / 32) {
         const int j = j0 + l;
-        float* dst = Vs + res_index<NB>(kk, l);
-        if (l < nbp && k > j + 1) cp_async4(dst, Aw + k + (long long)j * ld);
-        else *dst = (l < nbp && k == j + 1) ? 1.0f : 0.0f;
+        const float* src = Aw + (long long)j * ld;
+        for (int kk = lane; kk < nk; kk += 32) {
+            const int k = j0 + 1 + kk;
+            float* dst = Vs + res_index<NB>(kk, l);
+            if (l < nbp && k > j + 1) cp_async4(dst, src + k);
+            else *dst = (l < nbp && k == j + 1) ? 1.0f : 0.0f;
+        }
     }
     cp_commit();
 }
@@ -1028,11 +1033,11 @@ __global__ void __launch_bounds__(kResNT, 1) tri_apply_res_kernel(TriApplyParams
     float* Yw = p.Y + p.offF[w] + r0;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int rq = (nr + 31) / 32;                               // groups of 8 row quads
-    for (int idx = tid; idx < n * rq * 32; idx += kResNT) {
-        const int k = idx / (rq * 32), r = idx % (rq * 32);
-        if (r < nr) cp_async4(Ys + (size_t)k * rows + r, Fw + r + (long long)k * m);
-        else Ys[(size_t)k * rows + r] = 0.0f;
-    }
+    for (int k = warp; k < n; k += kResNT / 32)                  // warp per column, lanes down the rows
+        for (int r = lane; r < rq * 32; r += 32) {
+            if (r < nr) cp_async4(Ys + (size_t)k * rows + r, Fw + r + (long long)k * m);
+            else Ys[(size_t)k * rows + r] = 0.0f;
+        }
     cp_commit();
     const int rt_l = lane & 7, ct_l = lane >> 3;                 // lane: row quad, reflector / column quad
     for (int j0 = 0; j0 < n - 2; j0 += NB) {
@@ -1135,10 +1140,8 @@ __global__ void __launch_bounds__(kResNT, 1) tri_apply_res_kernel(TriApplyParams
     }
     cp_wait<0>();                                                // (no panel: the rows as loaded)
     __syncthreads();
-    for (int idx = tid; idx < n * rq * 32; idx += kResNT) {
-        const int k = idx / (rq * 32), r = idx % (rq * 32);
-        if (r < nr) Yw[r + (long long)k * m] = Ys[(size_t)k * rows + r];
-    }
+    for (int k = warp; k < n; k += kResNT / 32)
+        for (int r = lane; r < nr; r += 32) Yw[r + (long long)k * m] = Ys[(size_t)k * rows + r];
 }
 
 // ---------------------------------------------------------------------------
