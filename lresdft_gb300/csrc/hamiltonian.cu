@@ -249,13 +249,9 @@ __global__ void __launch_bounds__(kAsmThreads, 5) assemble_h32_kernel(int npair,
         for (int f = 0; f < NF; ++f)
 #pragma unroll
             for (int e = 0; e < NF; ++e) blk[f][e] = 0.0f;
-        // the slot pair of the next point is loaded one iteration ahead (the basis values
-        // depend on it)
-        int2 nxt = base + lane < cend ? cslot[base + lane] : make_int2(0, 0);
 #pragma unroll 2
         for (long long c = base + lane; c < cend; c += 32) {
-            const int2 ss = nxt;
-            if (c + 32 < cend) nxt = cslot[c + 32];
+            const int2 ss = cslot[c];
             const long long a = sg0 + ss.x, bb = sh0 + ss.y;
             const float vv = vslot[a];
             float xg[NF], xh[NF];
