@@ -96,3 +96,45 @@ def test_one_and_eight_function_atoms_and_many_threads():
     b64 = system.LCAOBasis(cr, atom_exps=atom_exps, nthreads=64)
     for attr in ("X", "Xr", "S", "T"):
         _same(getattr(b1, attr), getattr(b64, attr))
+
+
+def test_tabulation_and_dense_ks_argument_checks():
+    """Host-side argument checks of the GPU entry points (no device work): the tabulation
+    option of LCAOBasis, lres_basis_tabulate, lres_ks_density and the standard-form switch."""
+    import ctypes as C
+    from lresdft_gb300 import _lib, system
+    g = load("cubic3")
+    cr = crystal(g)
+    with pytest.raises(ValueError, match="tabulation"):
+        system.LCAOBasis(cr, tabulation="cpu")
+    with pytest.raises(ValueError, match="native"):
+        system.LCAOBasis(cr, tabulation="gpu", assembly="scipy")
+    cnt = np.zeros(1, np.int64)
+    shape = np.array([4, 4, 4], np.int64)
+    cell = np.array([4.0, 4.0, 4.0])
+    ns = np.array([3], np.int32)
+    npp = np.array([1], np.int32)
+    exps = np.array([1.0, 0.3, 0.12, 0.5])
+    pos = np.zeros(3)
+    i32p = C.POINTER(C.c_int32)
+    args = [1, _lib.ptrd(pos), ns.ctypes.data_as(i32p), npp.ctypes.data_as(i32p), _lib.ptrd(exps), _lib.ptr64(shape),
+            _lib.ptrd(cell), 1.0, 5.5, 1.0, _lib.ptr64(cnt)]
+    bad = list(args)
+    bad[0] = 0                                            # no atoms
+    assert _lib.lib.lres_basis_tabulate(*bad, None, None) == -22
+    bad = list(args)
+    bad[7] = -1.0                                         # dx <= 0
+    assert _lib.lib.lres_basis_tabulate(*bad, None, None) == -22
+    ns9 = np.array([9], np.int32)                         # nine functions on one atom
+    bad = list(args)
+    bad[2] = ns9.ctypes.data_as(i32p)
+    assert _lib.lib.lres_basis_tabulate(*bad, None, None) == -22
+    assert b"1..8" in _lib.lib.lres_last_error()
+    idx = np.zeros(1, np.int64)
+    assert _lib.lib.lres_basis_tabulate(*args, _lib.ptr64(idx), None) == -22     # idx without val
+    z = np.zeros(2, np.int64)
+    d = np.zeros(2)
+    assert _lib.lib.lres_ks_density(1, _lib.ptr64(z), _lib.ptr64(z), _lib.ptrd(d), _lib.ptr64(z), _lib.ptr64(z),
+                                    _lib.ptrd(d), 1, _lib.ptr64(z), _lib.ptr64(z), _lib.ptrd(d), 1, _lib.ptrd(d),
+                                    _lib.ptrd(d), _lib.ptrd(d)) == -22   # nocc >= nb
+    assert _lib.lib.lres_set_standard_form_kernel(None, 1) == -22
