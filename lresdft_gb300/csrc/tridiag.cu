@@ -857,7 +857,7 @@ __global__ void __launch_bounds__(NT, RPT == 1 && NB <= 16 ? 3 : 1) tri_apply_ke
 // Hamiltonian by tri_gram_kernel and tri_tfactor_kernel.
 
 constexpr int kResRows = 128;                 // rows of an item of the resident application
-constexpr int kResNT = 256;
+constexpr int kResNT = 512;
 
 // Staged panel: rows of NB values v_l[k]; the 16-byte groups of row kk permuted by XOR with
 // kk / 4, so that rows 4 apart (one per column quad of a warp) hit different banks.
@@ -1050,26 +1050,40 @@ __global__ void __launch_bounds__(kResNT, 1) tri_apply_res_kernel(TriApplyParams
         cp_commit();
         cp_wait<0>();                                            // Y (first panel), V, T
         __syncthreads();
-        const int nw1 = rq * (NB / 16);                          // warp tiles of S
-        // S = Y V over the panel rows
-        for (int wt = warp; wt < nw1; wt += kResNT / 32) {
-            const int rt = (wt % rq) * 8 + rt_l, lt = (wt / rq) * 4 + ct_l;
-            float acc[4][4] = {};
-            const float* yp = Ys + (size_t)(j0 + 1) * rows + 4 * rt;
+        const int nw1 = rq * (NB / 16);                          // 8 x 4 quad tiles of S (phase 2)
+        // S = Y V over the panel rows: a warp = 4 row quads x 4 reflector quads x 2 halves of
+        // the panel rows, the halves added by a shuffle
+        {
+            const int kh = lane >> 4, sub = lane & 15;
+            const int rt_h = sub & 3, lt_h = sub >> 2;
+            const int nwh = 2 * rq * (NB / 16);                  // warp tiles of S
+            const int kmid = (nk + 1) >> 1;
+            const int ka = kh ? kmid : 0, kz = kh ? nk : kmid;
+            for (int wt = warp; wt < nwh; wt += kResNT / 32) {
+                const int rt = (wt % (2 * rq)) * 4 + rt_h, lt = (wt / (2 * rq)) * 4 + lt_h;
+                float acc[4][4] = {};
+                const float* yp = Ys + (size_t)(j0 + 1) * rows + 4 * rt;
 #pragma unroll 4
-            for (int kk = 0; kk < nk; ++kk) {
-                const float4 y = *reinterpret_cast<const float4*>(yp + (size_t)kk * rows);
-                const float4 v = *reinterpret_cast<const float4*>(Vs + kk * NB + ((lt ^ (kk >> 2)) & (NG - 1)) * 4);
-                const float yy[4] = {y.x, y.y, y.z, y.w}, vv[4] = {v.x, v.y, v.z, v.w};
+                for (int kk = ka; kk < kz; ++kk) {
+                    const float4 y = *reinterpret_cast<const float4*>(yp + (size_t)kk * rows);
+                    const float4 v = *reinterpret_cast<const float4*>(Vs + kk * NB + ((lt ^ (kk >> 2)) & (NG - 1)) * 4);
+                    const float yy[4] = {y.x, y.y, y.z, y.w}, vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                    for (int i = 0; i < 4; ++i)
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(yy[i], vv[j], acc[i][j]);
+                }
 #pragma unroll
                 for (int i = 0; i < 4; ++i)
 #pragma unroll
-                    for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(yy[i], vv[j], acc[i][j]);
-            }
+                    for (int j = 0; j < 4; ++j) acc[i][j] += __shfl_xor_sync(0xffffffffu, acc[i][j], 16);
+                if (kh == 0) {
 #pragma unroll
-            for (int j = 0; j < 4; ++j)
-                *reinterpret_cast<float4*>(Ss + (size_t)(4 * lt + j) * rows + 4 * rt) =
-                    make_float4(acc[0][j], acc[1][j], acc[2][j], acc[3][j]);
+                    for (int j = 0; j < 4; ++j)
+                        *reinterpret_cast<float4*>(Ss + (size_t)(4 * lt + j) * rows + 4 * rt) =
+                            make_float4(acc[0][j], acc[1][j], acc[2][j], acc[3][j]);
+                }
+            }
         }
         __syncthreads();
         // S <- S T (T upper triangular)
