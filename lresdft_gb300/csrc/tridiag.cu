@@ -980,6 +980,7 @@ __global__ void __launch_bounds__(128) tri_gram_kernel(TriTParams p) {
 // sequential in l; a warp per panel keeps many panels in flight on each SM.
 template <int NB>
 __global__ void __launch_bounds__(32) tri_tfactor_kernel(TriTParams p) {
+    static_assert(NB <= 32, "one lane per reflector of the panel");
     __shared__ float Gm[NB * NB], Tm[NB * NB];
     const int w = blockIdx.x / p.maxp, panel = blockIdx.x % p.maxp;
     const int n = p.n_w[w];
@@ -989,16 +990,25 @@ __global__ void __launch_bounds__(32) tri_tfactor_kernel(TriTParams p) {
     const int nbp = min(NB, n - 2 - j0);
     float* Tw = p.T + (long long)w * p.tstride + (long long)panel * NB * NB;
     for (int i = tid; i < NB * NB; i += 32) Gm[i] = Tw[i];
-    __syncwarp();
+    // the panel's tau, one per lane (NB <= 32), broadcast in the recurrence (no global load on
+    // its sequential path)
     const float* tw = p.tau + p.offN[w];
+    const float my_tau = tid < nbp ? tw[j0 + tid] : 0.0f;
+    __syncwarp();
     for (int l = 0; l < NB; ++l) {
-        const float tl = l < nbp ? tw[j0 + l] : 0.0f;
+        const float tl = __shfl_sync(0xffffffffu, my_tau, l);
         for (int a = tid; a < NB; a += 32) {
             float val = 0.0f;
             if (a < l) {
-                float sacc = 0.0f;
-                for (int b = a; b < l; ++b) sacc = fmaf(Tm[a * NB + b], Gm[b * NB + l], sacc);
-                val = -tl * sacc;
+                // four independent partial sums (b mod 4), added in a fixed order
+                float s[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+                int b = a;
+                for (; b + 3 < l; b += 4) {
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) s[u] = fmaf(Tm[a * NB + b + u], Gm[(b + u) * NB + l], s[u]);
+                }
+                for (; b < l; ++b) s[0] = fmaf(Tm[a * NB + b], Gm[b * NB + l], s[0]);
+                val = -tl * ((s[0] + s[1]) + (s[2] + s[3]));
             } else if (a == l) {
                 val = tl;
             }
