@@ -135,7 +135,7 @@ struct TriReduceParams {
 // Shared memory of the reduction, in elements of R.
 inline size_t reduce_smem_elems(int nb, int ldv, int nt) {
     const size_t big = std::max((size_t)2 * nb * ldv, (size_t)(nt / 32) * 32 * 33);
-    return big + 2 * (size_t)ldv + 4 * (size_t)nt + 64 + nt / 32;
+    return big + 5 * (size_t)ldv + 4 * (size_t)nt + 64 + nt / 32;
 }
 
 template <class R, int NT>
@@ -148,7 +148,9 @@ __global__ void __launch_bounds__(NT) tri_reduce_kernel(TriReduceParams<R> p) {
     R* const Ws = big + (size_t)nb * ldv;                // [nb][ldv]
     R* const cv = big + std::max((size_t)2 * nb * ldv, (size_t)NW * 32 * 33);   // [ldv] current column
     R* const pv = cv + ldv;                              // [ldv] p = tau (A v)
-    R* const psum = pv + ldv;                            // [4 NT] split sums of A v
+    R* const qx = pv + ldv;                              // [ldv] q = A x (unsplit)
+    R* const acol = qx + ldv;                            // [2][ldv] panel-start columns j, j+1
+    R* const psum = acol + 2 * ldv;                      // [4 NT] split sums of A x
     R* const dots = psum + 4 * NT;                       // [64] W^T v, V^T v
     R* const red = dots + 64;                            // [NW]
     __shared__ int item_sh;
@@ -206,30 +208,93 @@ __global__ void __launch_bounds__(NT) tri_reduce_kernel(TriReduceParams<R> p) {
         }
         __syncthreads();
 
-        // with one row per thread, the panel-start value of column j+1 for the row this thread
-        // handles at step j+1 is loaded during step j
-        const bool pf = n <= NT;
-        R cpre = R(0);
+        // Each column takes three barriers.  Rows are owned by threads (row i by thread i mod NT)
+        // for the column, the reflector and w; the norm, the dots W^T x, V^T x and q = A x are
+        // taken over the unscaled column x (rows >= j+2) in one phase, and the reflector's scale
+        // is applied afterwards: A v = A e_{j+1} + scal A x, X^T v = X_{j+1} + scal X^T x.  The
+        // panel-start column j+1 of the owned rows is fetched by cp.async during column j: it
+        // is A e_{j+1} of column j and the start of column j+1.
+        R Kprev = R(0);
         for (int j0 = 0; j0 < n - 2; j0 += nb) {
             const int nbp = min(nb, n - 2 - j0);
             for (int jj = 0; jj < nbp; ++jj) {
                 const int j = j0 + jj;
-                R cnext = R(0);
-                if (pf && jj + 1 < nbp && j + 1 + tid < n) cnext = A[(j + 1 + tid) + (long long)(j + 1) * ld];
-                // (a) column j of the current matrix (panel-start values minus the pending
-                //     rank-2 updates of this panel), rows >= j; squares of rows >= j+2
-                R part = R(0);
-                for (int i = j + tid; i < n; i += NT) {
-                    R c = (pf && jj > 0) ? cpre : A[i + (long long)j * ld];
-                    for (int l = 0; l < jj; ++l)
-                        c -= Vs[l * ldv + i] * Ws[l * ldv + j] + Ws[l * ldv + i] * Vs[l * ldv + j];
-                    cv[i] = c;
-                    if (i >= j + 2) part += c * c;
+                R* const anext = acol + ((j + 1) & 1) * ldv;
+                const R* const acur = acol + (j & 1) * ldv;
+                for (int i = tid; i < n; i += NT)
+                    if (i > j) cp_async4(anext + i, A + i + (long long)(j + 1) * ld);
+                cp_commit();
+                // (a) column j of the current matrix (panel-start values minus the pending rank-2
+                //     updates of this panel) on the owned rows >= j.  w_{jj-1} at row j is
+                //     p_j - K (v_{jj-1} is 1 there); every thread forms it from the published p.
+                {
+                    const R wlast = jj > 0 ? pv[j] - Kprev : R(0);
+                    for (int i = tid; i < n; i += NT) {
+                        if (i < j) continue;
+                        R c = jj > 0 ? acur[i] : A[i + (long long)j * ld];
+                        for (int l = 0; l < jj; ++l) {
+                            const R wlj = l == jj - 1 ? wlast : Ws[l * ldv + j];
+                            c -= Vs[l * ldv + i] * wlj + Ws[l * ldv + i] * Vs[l * ldv + j];
+                        }
+                        cv[i] = c;
+                    }
                 }
-                cpre = cnext;
-                // (b) reflector H_j = I - tau v v^T with v_{j+1} = 1 mapping rows j+1.. of the
-                //     column onto beta e_{j+1}
-                const R s2 = block_sum<NT>(part, red);    // its barriers also publish cv
+                __syncthreads();
+                // (b) q = A x on rows >= j+1 by quads of rows (16-byte loads) from the aligned row
+                //     i0 <= j+1; when the quads are few, the columns are split across thread groups
+                //     and the partial sums added in a fixed order.  Sums are blocked: each run of
+                //     32 terms from zero.
+                const int i0 = (j + 1) & ~3;
+                const int nq = (ld - i0) >> 2;
+                const int nsplit = nq >= NT ? 1 : NT / nq;
+                {
+                    const int qstep = nq >= NT ? NT : nq;
+                    if (tid < qstep * nsplit) {
+                        const int sp = tid / qstep;
+                        for (int q = tid % qstep; q < nq; q += qstep) {
+                            const R* Aq = A + i0 + 4 * q;
+                            R a[4] = {R(0), R(0), R(0), R(0)};
+                            for (int kb = j + 2 + sp; kb < n; kb += 32 * nsplit) {
+                                const int ke = min(n, kb + 32 * nsplit);
+                                R c[4] = {R(0), R(0), R(0), R(0)};
+#pragma unroll 8
+                                for (int k = kb; k < ke; k += nsplit) {
+                                    R x[4];
+                                    ld4(Aq + (long long)k * ld, x);
+                                    const R xk = cv[k];
+#pragma unroll
+                                    for (int r = 0; r < 4; ++r) c[r] = fma(x[r], xk, c[r]);
+                                }
+#pragma unroll
+                                for (int r = 0; r < 4; ++r) a[r] += c[r];
+                            }
+                            if (nsplit > 1) {
+#pragma unroll
+                                for (int r = 0; r < 4; ++r) psum[(sp * nq + q) * 4 + r] = a[r];
+                            } else {
+#pragma unroll
+                                for (int r = 0; r < 4; ++r) {
+                                    const int i = i0 + 4 * q + r;
+                                    if (i > j && i < n) qx[i] = a[r];
+                                }
+                            }
+                        }
+                    }
+                }
+                //     dots[l] = W_l^T x, dots[jj + l] = V_l^T x, dots[2 jj] = x^T x over rows >= j+2,
+                //     a warp each (the last warps first: they have the fewest row quads)
+                for (int q = NW - 1 - warp; q <= 2 * jj; q += NW) {
+                    const R* X = q < jj ? Ws + (size_t)q * ldv : q < 2 * jj ? Vs + (size_t)(q - jj) * ldv : cv;
+                    R acc = R(0);
+                    for (int i = j + 2 + lane; i < n; i += 32) acc += X[i] * cv[i];
+                    acc = warp_sum(acc);
+                    if (lane == 0) dots[q] = acc;
+                }
+                __syncthreads();
+                // (c) reflector H_j = I - tau v v^T with v_{j+1} = 1 mapping rows j+1.. of the
+                //     column onto beta e_{j+1} (every thread, the same bits); p = tau (A v - V (W^T v)
+                //     - W (V^T v)) on the owned rows, partial sums of p^T v
+                const R s2 = dots[2 * jj];
                 const R alpha = cv[j + 1];
                 R beta = alpha, tau = R(0), scal = R(0);
                 if (s2 > R(0)) {
@@ -244,85 +309,47 @@ __global__ void __launch_bounds__(NT) tri_reduce_kernel(TriReduceParams<R> p) {
                     tw[j] = tau;
                     if (!isfinite((double)beta) || !isfinite((double)cv[j])) atomicOr(p.status, ST_ZERO_PIVOT);
                 }
+                cp_wait<0>();
+                R partK = R(0);
                 for (int i = tid; i < ldv; i += NT) {
                     R vi = R(0);
                     if (i == j + 1) vi = R(1);
                     else if (i > j + 1 && i < n) vi = cv[i] * scal;
                     Vs[jj * ldv + i] = vi;
-                    if (i > j + 1 && i < n) A[i + (long long)j * ld] = vi;   // kept for Y = F^ Q
-                }
-                __syncthreads();
-                // (c) p = A v - V (W^T v) - W (V^T v) on rows j+1..n-1
-                for (int q = warp; q < 2 * jj; q += NW) {
-                    const R* X = q < jj ? Ws + (size_t)q * ldv : Vs + (size_t)(q - jj) * ldv;
-                    R acc = R(0);
-                    for (int i = j + 1 + lane; i < n; i += 32) acc += X[i] * Vs[jj * ldv + i];
-                    acc = warp_sum(acc);
-                    if (lane == 0) dots[q] = acc;
-                }
-                // A v by quads of rows (16-byte loads) from the aligned row i0 <= j+1; when the
-                // quads are few, the columns are split across thread groups and the partial
-                // sums added in a fixed order.  Sums are blocked: each run of 32 terms from zero.
-                const int i0 = (j + 1) & ~3;
-                const int nq = (ld - i0) >> 2;
-                const int nsplit = nq >= NT ? 1 : NT / nq;
-                {
-                    const R* vv = Vs + (size_t)jj * ldv;
-                    const int qstep = nq >= NT ? NT : nq;
-                    if (tid < qstep * nsplit) {
-                        const int sp = tid / qstep;
-                        for (int q = tid % qstep; q < nq; q += qstep) {
-                            const R* Aq = A + i0 + 4 * q;
-                            R a[4] = {R(0), R(0), R(0), R(0)};
-                            for (int kb = j + 1 + sp; kb < n; kb += 32 * nsplit) {
-                                const int ke = min(n, kb + 32 * nsplit);
-                                R c[4] = {R(0), R(0), R(0), R(0)};
-#pragma unroll 8
-                                for (int k = kb; k < ke; k += nsplit) {
-                                    R x[4];
-                                    ld4(Aq + (long long)k * ld, x);
-                                    const R vk = vv[k];
-#pragma unroll
-                                    for (int r = 0; r < 4; ++r) c[r] = fma(x[r], vk, c[r]);
-                                }
-#pragma unroll
-                                for (int r = 0; r < 4; ++r) a[r] += c[r];
-                            }
-                            if (nsplit > 1) {
-#pragma unroll
-                                for (int r = 0; r < 4; ++r) psum[(sp * nq + q) * 4 + r] = a[r];
-                            } else {
-#pragma unroll
-                                for (int r = 0; r < 4; ++r) {
-                                    const int i = i0 + 4 * q + r;
-                                    if (i > j && i < n) pv[i] = a[r];
-                                }
-                            }
+                    if (i > j && i < n) {
+                        if (i > j + 1) A[i + (long long)j * ld] = vi;      // kept for Y = F^ Q
+                        R qi;
+                        if (nsplit > 1) {
+                            const int q = (i - i0) >> 2, r = (i - i0) & 3;
+                            qi = R(0);
+                            for (int sp = 0; sp < nsplit; ++sp) qi += psum[(sp * nq + q) * 4 + r];
+                        } else {
+                            qi = qx[i];
                         }
+                        R pi = anext[i] + scal * qi;
+                        for (int l = 0; l < jj; ++l) {
+                            const R dW = Ws[l * ldv + j + 1] + scal * dots[l];
+                            const R dV = Vs[l * ldv + j + 1] + scal * dots[jj + l];
+                            pi -= Vs[l * ldv + i] * dW + Ws[l * ldv + i] * dV;
+                        }
+                        pi *= tau;
+                        pv[i] = pi;
+                        partK += pi * vi;
                     }
                 }
+                partK = warp_sum(partK);
+                if (lane == 0) red[warp] = partK;
                 __syncthreads();
-                // (d) p *= tau, K = tau/2 p.v, w = p - K v
-                R partK = R(0);
-                for (int i = j + 1 + tid; i < n; i += NT) {
-                    R pi;
-                    if (nsplit > 1) {
-                        const int q = (i - i0) >> 2, r = (i - i0) & 3;
-                        pi = R(0);
-                        for (int sp = 0; sp < nsplit; ++sp) pi += psum[(sp * nq + q) * 4 + r];
-                    } else {
-                        pi = pv[i];
-                    }
-                    for (int l = 0; l < jj; ++l) pi -= Vs[l * ldv + i] * dots[l] + Ws[l * ldv + i] * dots[jj + l];
-                    pi *= tau;
-                    pv[i] = pi;
-                    partK += pi * Vs[jj * ldv + i];
-                }
-                const R K = R(0.5) * tau * block_sum<NT>(partK, red);
+                // (d) K = tau/2 p^T v, w = p - K v on the owned rows
+                R sK = red[0];
+#pragma unroll
+                for (int w2 = 1; w2 < NW; ++w2) sK += red[w2];
+                const R K = R(0.5) * tau * sK;
+                Kprev = K;
                 for (int i = tid; i < ldv; i += NT)
                     Ws[jj * ldv + i] = (i > j && i < n) ? pv[i] - K * Vs[jj * ldv + i] : R(0);
-                __syncthreads();
             }
+            __syncthreads();
             // ---- trailing update of both triangles: A -= V W^T + W V^T on rows, columns >= t0.
             //      One quad of rows x one aligned quad of columns per thread: the v, w values of
             //      both quads come from shared memory as 16-byte vectors (4 loads per 32 FMAs);
