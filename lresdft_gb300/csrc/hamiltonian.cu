@@ -276,27 +276,40 @@ __global__ void __launch_bounds__(kAsmThreads, 5) assemble_h32_kernel(int npair,
             asm volatile("" ::: "memory");
         }
     }
+    // the lanes' pairs of element k reduced by a butterfly; lane k % 32 keeps the result, and
+    // every lane then converts and stores its own elements (the FP64 instructions are issued
+    // once or twice per warp, all lanes busy, rather than once per element)
+    constexpr int kPer = (NF * NF + 31) / 32;
+    float2 mine[kPer];
+#pragma unroll
+    for (int m = 0; m < kPer; ++m) mine[m] = make_float2(0.0f, 0.0f);
+#pragma unroll
+    for (int k = 0; k < NF * NF; ++k) {
+        float2 a = acc_s[k][t];
+#pragma unroll 1
+        for (int s = 16; s; s >>= 1) {
+            const float ohi = __shfl_xor_sync(0xffffffffu, a.x, s);
+            const float olo = __shfl_xor_sync(0xffffffffu, a.y, s);
+            // the same pair of operands in the same order on both lanes of a butterfly
+            float hi = lane & s ? ohi : a.x, lo = lane & s ? olo : a.y;
+            const float x = lane & s ? a.x : ohi, xlo = lane & s ? a.y : olo;
+            two_sum_acc(hi, lo, x);
+            a = make_float2(hi, lo + xlo);
+        }
+        if (k % 32 == lane) mine[k / 32] = a;
+    }
     const long long o = boff[b];
     const long long ot = boff[btrans[b]];
-#pragma unroll 1
-    for (int f = 0; f < NF; ++f)
-#pragma unroll 1
-        for (int e = 0; e < NF; ++e) {
-            float2 a = acc_s[f * NF + e][t];
-            for (int s = 16; s; s >>= 1) {
-                const float ohi = __shfl_xor_sync(0xffffffffu, a.x, s);
-                const float olo = __shfl_xor_sync(0xffffffffu, a.y, s);
-                // the same pair of operands in the same order on both lanes of a butterfly
-                float hi = lane & s ? ohi : a.x, lo = lane & s ? olo : a.y;
-                const float x = lane & s ? a.x : ohi, xlo = lane & s ? a.y : olo;
-                two_sum_acc(hi, lo, x);
-                a = make_float2(hi, lo + xlo);
-            }
-            if ((f * NF + e) % 32 != lane || f >= nfg || e >= nfh) continue;
-            const double x = (double)a.x + (double)a.y;
-            Hblk[o + f * nfh + e] = Tblk[o + f * nfh + e] + x * dV;
-            if (h != g) Hblk[ot + e * nfg + f] = Tblk[ot + e * nfg + f] + x * dV;
-        }
+#pragma unroll
+    for (int m = 0; m < kPer; ++m) {
+        const int k = lane + 32 * m;
+        if (k >= NF * NF) break;
+        const int f = k / NF, e = k % NF;
+        if (f >= nfg || e >= nfh) continue;
+        const double x = (double)mine[m].x + (double)mine[m].y;
+        Hblk[o + f * nfh + e] = Tblk[o + f * nfh + e] + x * dV;
+        if (h != g) Hblk[ot + e * nfg + f] = Tblk[ot + e * nfg + f] + x * dV;
+    }
 }
 
 bool assemble_h32_supported(const BlockPattern& bp) { return bp.nfmax <= 6; }

@@ -138,8 +138,11 @@ inline size_t reduce_smem_elems(int nb, int ldv, int nt) {
     return big + 5 * (size_t)ldv + 4 * (size_t)nt + 64 + nt / 32;
 }
 
+// CTAs per SM that the FP32 reduction is compiled for (registers: 65536 / (NT * that)).
+constexpr int reduce_min_ctas(int nt, int elem) { return elem != 4 ? 1 : 1024 / nt; }
+
 template <class R, int NT>
-__global__ void __launch_bounds__(NT) tri_reduce_kernel(TriReduceParams<R> p) {
+__global__ void __launch_bounds__(NT, reduce_min_ctas(NT, sizeof(R))) tri_reduce_kernel(TriReduceParams<R> p) {
     constexpr int NW = NT / 32;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int ldv = p.ldv, nb = p.nb;
@@ -269,8 +272,7 @@ __global__ void __launch_bounds__(NT) tri_reduce_kernel(TriReduceParams<R> p) {
                                 for (int r = 0; r < 4; ++r) a[r] += c[r];
                             }
                             if (nsplit > 1) {
-#pragma unroll
-                                for (int r = 0; r < 4; ++r) psum[(sp * nq + q) * 4 + r] = a[r];
+                                st4(psum + (sp * nq + q) * 4, a);    // 16-byte stores: no bank conflicts
                             } else {
 #pragma unroll
                                 for (int r = 0; r < 4; ++r) {
