@@ -141,14 +141,15 @@ def roofline_of(name, ms, nW, mW, P, nnz_h, peaks):
             "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback"}
 
 
-def launches_per_step(route, precision, tile_config=0):
+def launches_per_step(route, precision, tile_config=0, standard_form="simt"):
     """Our kernels in one step (H(v) + window blocks + standard form + pass)."""
     if route == "tridiag":
         # assemble_h, gather, 2 standard-form GEMMs, reduction, rows, pole nodes, pass, window
         # sums; mixed: + the FP32 potential per slot, + V^T V and the T factors of the
-        # resident-row application (every configuration but 2)
+        # resident-row application (every configuration but 2), + the FP32 copy of the H
+        # blocks that the SIMT standard form's FP32 windows are gathered from
         if precision == "mixed":
-            return 10 + 2 * (tile_config != 2)
+            return 10 + 2 * (tile_config != 2) + (standard_form == "simt")
         return 9
     # assemble_h, gather, [split + 2 double-float GEMMs], pole nodes, LDL^T kernel, pole sums
     return 8 if precision == "mixed" else 5
@@ -260,7 +261,8 @@ def run_ours(args):
     mW = np.array([len(o) for o in s.ctx_own])
     P = s.M // 2
     units = len(s.nW) * P
-    lps = launches_per_step(route, args.precision, s.tile_config if isinstance(s.tile_config, int) else 0)
+    lps = launches_per_step(route, args.precision, s.tile_config if isinstance(s.tile_config, int) else 0,
+                            args.standard_form)
 
     def step():
         s.set_potential_device(v_dev.data_ptr())

@@ -84,6 +84,8 @@ struct lres_ctx {
     BlockPattern bp;
     Supports sp;
     double *d_Sblk = nullptr, *d_Tblk = nullptr, *d_Hblk = nullptr;
+    float* d_Hblk32 = nullptr;           // FP32 copy of the H blocks (mixed precision)
+    bool h32_dense = false;              // the FP32 H_W of the current H sits in the second standard-form slot
     std::vector<int> bptr_h, bcol_h;
     std::vector<long long> boff_h;
     // dense windows
@@ -179,7 +181,7 @@ lres_ctx::~lres_ctx() {
     void* ptrs[] = {d_n, d_m, d_c0, d_offC, d_offF, d_offQ, d_Oflat, d_wgrp_off, d_wgrp, d_wgrp_lo, d_gloc,
                     d_gfn, d_gbtab, d_gnlg, d_gfnoff, d_gbtoff,
                     bp.gptr, bp.bptr, bp.bcol, bp.brow, bp.boff, bp.btrans, bp.pair_blk, sp.soff, sp.sgrid,
-                    sp.sval, sp.sval32, sp.vslot, sp.coff, sp.cslot, d_Sblk, d_Tblk, d_Hblk, d_SW, d_HW, d_F, d_LinvT, d_Y, d_Hhat,
+                    sp.sval, sp.sval32, sp.vslot, sp.coff, sp.cslot, d_Sblk, d_Tblk, d_Hblk, d_Hblk32, d_SW, d_HW, d_F, d_LinvT, d_Y, d_Hhat,
                     d_Hhat32, d_Fhat32, d_LinvT_df, d_H_df, d_Y_df, d_items, d_items_win, d_items_sub, d_counter, d_status, d_npos, d_ws, d_shifts,
                     d_wq, d_wzq, d_q, d_dens, d_nw, d_ew, d_v, d_fftwork, d_adjA[0], d_adjA[1], d_adjA[2],
                     d_dHW, d_dSW, d_gH, d_adjdv, d_adju, d_cw, d_order, d_eoff, d_poff, d_ent, d_pent, d_adjws,
@@ -344,11 +346,16 @@ int transform_f32(lres_ctx* c, cudaStream_t s) {
     // Y = H L^-T (B = L^-T given k-major: its transpose L^-1), written row-major (k-major for
     // the next product); A^ = lower(L^-1 Y)
     float* Y = reinterpret_cast<float*>(c->d_Y_df);
+    const bool h32 = c->h32_dense;       // consumed here, whatever the outcome
+    c->h32_dense = false;
     if (c->sf_kind == LRES_SF_TENSOR && c->d_tstatus) {
         TRY(batched_gemm_tc(c->nwin, c->d_n, c->d_offC, c->nmax, 1, c->d_HW, true, c->d_Linv32, Y, true, c->d_tstatus,
                             s));
         TRY(batched_gemm_tc(c->nwin, c->d_n, c->d_offC, c->nmax, 2, c->d_Linv32, false, Y, tri_hhat32(c), false,
                             c->d_tstatus, s));
+    } else if (h32) {
+        TRY(batched_gemm_f32(c->nwin, c->d_n, c->d_offC, c->nmax, 1, tri_hhat32(c), false, c->d_Linv32, Y, true, s));
+        TRY(batched_gemm_f32(c->nwin, c->d_n, c->d_offC, c->nmax, 2, c->d_Linv32, false, Y, tri_hhat32(c), false, s));
     } else {
         TRY(batched_gemm_f32(c->nwin, c->d_n, c->d_offC, c->nmax, 1, c->d_HW, true, c->d_Linv32, Y, true, s));
         TRY(batched_gemm_f32(c->nwin, c->d_n, c->d_offC, c->nmax, 2, c->d_Linv32, false, Y, tri_hhat32(c), false, s));
@@ -401,8 +408,14 @@ int tri_prepare(lres_ctx* c, cudaStream_t s);
 
 int after_h_blocks(lres_ctx* c, cudaStream_t s) {
     TRY(mark(c, 3, 0, s));
+    // the FP32 standard form on the SIMT pipes reads FP32 windows, gathered beside the FP64 ones
+    // from FP32 blocks into the slot its second product overwrites
+    const bool h32 = c->precision == LRES_MIXED && c->route == LRES_ROUTE_TRIDIAG && c->sf_kind == LRES_SF_SIMT &&
+                     c->d_Hblk32 && c->d_Y_df;
+    if (h32) TRY(convert_f64_f32(c->d_Hblk, c->d_Hblk32, c->bp.nval, s));
     TRY(gather_windows(c->nwin, c->nmax, c->d_gfn, c->d_gfnoff, c->d_gbtab, c->d_gbtoff, c->d_gnlg, c->d_offC,
-                       c->d_n, c->d_Hblk, c->d_HW, s));
+                       c->d_n, c->d_Hblk, c->d_HW, h32 ? c->d_Hblk32 : nullptr, h32 ? tri_hhat32(c) : nullptr, s));
+    c->h32_dense = h32;
     TRY(mark(c, 3, 1, s));
     if (needs_standard_form(c)) {
         TRY(mark(c, 4, 0, s));
@@ -927,6 +940,7 @@ extern "C" int lres_ctx_create(lres_ctx** out, const lres_system_desc* d, int pr
     TRY(upload(&c->d_Sblk, Sblk, s));
     TRY(upload(&c->d_Tblk, Tblk, s));
     TRY(dalloc(&c->d_Hblk, nval));
+    if (c->precision == LRES_MIXED) TRY(dalloc(&c->d_Hblk32, nval));
     TRY(upload(&c->d_n, c->n_w, s));
     TRY(upload(&c->d_m, c->m_w, s));
     {
@@ -1012,7 +1026,7 @@ extern "C" int lres_ctx_create(lres_ctx** out, const lres_system_desc* d, int pr
     TRY(dalloc(&c->d_SW, c->sizeC));
     TRY(dalloc(&c->d_HW, c->sizeC));
     TRY(gather_windows(c->nwin, c->nmax, c->d_gfn, c->d_gfnoff, c->d_gbtab, c->d_gbtoff, c->d_gnlg, c->d_offC,
-                       c->d_n, c->d_Sblk, c->d_SW, s));
+                       c->d_n, c->d_Sblk, c->d_SW, nullptr, nullptr, s));
     TRY(dalloc(&c->d_F, c->sizeF));
     LRES_CUDA_TRY(cudaMemsetAsync(c->d_F, 0, sizeof(double) * c->sizeF, s));
     {
@@ -1677,6 +1691,7 @@ extern "C" int lres_set_windows(lres_ctx* c, const double* HW, const double* SW,
     }
     cudaStream_t s = (cudaStream_t)stream;
     const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    c->h32_dense = false;                // the FP32 windows, if any, are of the previous H
     if (HW) LRES_CUDA_TRY(cudaMemcpyAsync(c->d_HW, HW, sizeof(double) * c->sizeC, kind, s));
     if (SW) {
         LRES_CUDA_TRY(cudaMemcpyAsync(c->d_SW, SW, sizeof(double) * c->sizeC, kind, s));

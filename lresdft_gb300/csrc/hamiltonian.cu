@@ -342,13 +342,17 @@ int assemble_h32(const BlockPattern& bp, const Supports& sp, const double* Tblk,
 // symmetric, so element (i, j) with i in atom g, j in atom h is read from the stored block
 // (h, g) at [e][f] (e, f the functions of j in h and of i in g): consecutive rows of one atom
 // read consecutive values.  fn[i] = (local atom << 12) | (f << 6) | nf_g; btab[lg_i * nlg +
-// lg_j] = value offset of block (h, g), -1 where the atoms do not overlap.
+// lg_j] = value offset of block (h, g), -1 where the atoms do not overlap.  With F32, the same
+// element of the FP32 copy of the blocks (blk32) is written to dense32 as well: the FP32
+// standard form then reads FP32 windows (the blocks are converted once, not every window
+// element once per GEMM tile).
 constexpr int kGatherCols = 32;
 
+template <bool F32>
 __global__ void __launch_bounds__(256) gather_windows_kernel(const int* fn, const long long* fnoff, const int* btab,
                                                              const long long* btoff, const int* nlg,
                                                              const long long* offC, const int* n_w, const double* blk,
-                                                             double* dense) {
+                                                             double* dense, const float* blk32, float* dense32) {
     const int w = blockIdx.y;
     const int n = n_w[w];
     const int j0 = blockIdx.x * kGatherCols;
@@ -367,20 +371,26 @@ __global__ void __launch_bounds__(256) gather_windows_kernel(const int* fn, cons
             const int lgi = mi >> 12, f = (mi >> 6) & 63, nfg = mi & 63;
             const int off = bt[lgi * L + lgj];
             D[i + (long long)j * n] = off >= 0 ? blk[off + e * nfg + f] : 0.0;
+            if constexpr (F32) dense32[offC[w] + i + (long long)j * n] = off >= 0 ? blk32[off + e * nfg + f] : 0.0f;
         }
     }
 }
 
 int gather_windows(int nwin, int nmax, const int* fn, const long long* fnoff, const int* btab, const long long* btoff,
                    const int* nlg, const long long* offC, const int* n_w, const double* blk, double* dense,
-                   cudaStream_t s) {
+                   const float* blk32, float* dense32, cudaStream_t s) {
     if (!nwin) return LRES_OK;
     if (nwin > 65535) {
         lres_set_error("window gather supports at most 65535 windows (got %d)", nwin);
         return LRES_EINVAL;
     }
     const dim3 grid((unsigned)((nmax + kGatherCols - 1) / kGatherCols), (unsigned)nwin);
-    gather_windows_kernel<<<grid, 256, 0, s>>>(fn, fnoff, btab, btoff, nlg, offC, n_w, blk, dense);
+    if (blk32 && dense32)
+        gather_windows_kernel<true><<<grid, 256, 0, s>>>(fn, fnoff, btab, btoff, nlg, offC, n_w, blk, dense, blk32,
+                                                         dense32);
+    else
+        gather_windows_kernel<false><<<grid, 256, 0, s>>>(fn, fnoff, btab, btoff, nlg, offC, n_w, blk, dense, nullptr,
+                                                          nullptr);
     LRES_CUDA_TRY(cudaGetLastError());
     return LRES_OK;
 }
@@ -921,6 +931,8 @@ int batched_gemm_f32(int nwin, const int* n_w, const long long* off, int nmax, i
     }
     dim3 grid((nmax + 63) / 64, (nmax + 63) / 64, nwin);
     if (klim == 1 && a_f64 && c_rowmajor) gemm_f32blk_kernel<1, true, true><<<grid, 128, 0, s>>>(n_w, off, A, Bt, C);
+    else if (klim == 1 && !a_f64 && c_rowmajor)
+        gemm_f32blk_kernel<1, false, true><<<grid, 128, 0, s>>>(n_w, off, A, Bt, C);
     else if (klim == 2 && !a_f64 && !c_rowmajor)
         gemm_f32blk_kernel<2, false, false><<<grid, 128, 0, s>>>(n_w, off, A, Bt, C);
     else {

@@ -88,10 +88,11 @@ int assemble_h(const BlockPattern& bp, const Supports& sp, const double* Tblk, c
 bool assemble_h32_supported(const BlockPattern& bp);
 int assemble_h32(const BlockPattern& bp, const Supports& sp, const double* Tblk, const double* v, double dV,
                  double* Hblk, cudaStream_t s);
-// Dense window blocks (column-major, every element written) from the atom-pair blocks.
+// Dense window blocks (column-major, every element written) from the atom-pair blocks; with
+// blk32 and dense32, also the FP32 windows from the FP32 copy of the blocks.
 int gather_windows(int nwin, int nmax, const int* fn, const long long* fnoff, const int* btab, const long long* btoff,
                    const int* nlg, const long long* offC, const int* n_w, const double* blk, double* dense,
-                   cudaStream_t s);
+                   const float* blk32, float* dense32, cudaStream_t s);
 int build_F(int nwin, const long long* Xp, const int* Xi, const double* Xv, const int* group_of_fn,
             const int* gptr, const int* gloc, int ngroups, const long long* Ooff, const long long* Oflat,
             const long long* offF, const int* m_w, int mmax, double* F, cudaStream_t s);
