@@ -361,6 +361,7 @@ __global__ void __launch_bounds__(256) gather_windows_kernel(const int* fn, cons
     const int* bt = btab + btoff[w];
     const int L = nlg[w];
     double* D = dense + offC[w];
+    float* D32 = F32 ? dense32 + offC[w] : nullptr;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int j1 = min(n, j0 + kGatherCols);
     for (int j = j0 + warp; j < j1; j += 8) {
@@ -371,7 +372,7 @@ __global__ void __launch_bounds__(256) gather_windows_kernel(const int* fn, cons
             const int lgi = mi >> 12, f = (mi >> 6) & 63, nfg = mi & 63;
             const int off = bt[lgi * L + lgj];
             D[i + (long long)j * n] = off >= 0 ? blk[off + e * nfg + f] : 0.0;
-            if constexpr (F32) dense32[offC[w] + i + (long long)j * n] = off >= 0 ? blk32[off + e * nfg + f] : 0.0f;
+            if constexpr (F32) D32[i + (long long)j * n] = off >= 0 ? blk32[off + e * nfg + f] : 0.0f;
         }
     }
 }

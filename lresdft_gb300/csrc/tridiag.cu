@@ -1537,10 +1537,10 @@ struct TriCfg {
     int nb, nt, nba, rpt, res, rres;     // rres: the reduction with the window in shared memory
     int rows;                            // resident application: rows per item at most
 };
-// Measured at 1024 electrons (mixed): reduction 7.0 ms with the L2-resident working copy
-// (nb 16, 512 threads), 8.1 ms with the window in shared memory (nb 8); row application
-// 3.1 ms with resident rows (NB 32), 6.3 ms one row per thread; 256-thread reductions and
-// two or four rows per thread slower.
+// Measured at 1024 electrons (mixed): reduction 6.7 ms with the L2-resident working copy
+// (nb 16, 512 threads, two CTAs per SM; nb 8 6.75 ms, nb 32 7.35 ms; 256 threads at four CTAs
+// per SM and 384 at three 7.8 ms), 8.1 ms with the window in shared memory (nb 8); row
+// application 2.0 ms with resident rows (NB 32), 6.3 ms one row per thread.
 static const TriCfg kTriCfg[6] = {{16, 512, 32, 1, 1, 0, 128}, {16, 512, 32, 1, 1, 1, 128},
                                   {16, 512, 32, 1, 0, 0, 0},    {16, 512, 16, 1, 1, 0, 64},
                                   {16, 512, 32, 1, 1, 0, 32},   {8, 512, 32, 1, 1, 1, 128}};
