@@ -1369,17 +1369,43 @@ __global__ void __launch_bounds__(NT) tri_pass_kernel(TriPassParams<R> p) {
                     }
                     const R inv = rcp_rn(D.x * D.x + D.y * D.y);
                     gp = C{D.x * inv, -D.y * inv};
+                    // u^2 / D = (ur^2 - ui^2 + 2i ur ui) gp: the factor 2 (exact in binary) is
+                    // carried by the pole's g2 = 2 gp, so each row takes one product ur ui
+                    const C g2 = C{R(2) * gp.x, R(2) * gp.y};
                     const R* yi = yc + (size_t)(i - i0) * RB;
+                    // the group's RR staged values of step i as 16-byte vectors (the chunk, the
+                    // group offset g RR and the step stride RB are multiples of 16 bytes)
+                    R yv[RR];
+                    if constexpr (sizeof(R) == 4 && RR % 4 == 0) {
+#pragma unroll
+                        for (int q4 = 0; q4 < RR / 4; ++q4) {
+                            const float4 v = reinterpret_cast<const float4*>(yi)[q4];
+                            yv[4 * q4] = v.x;
+                            yv[4 * q4 + 1] = v.y;
+                            yv[4 * q4 + 2] = v.z;
+                            yv[4 * q4 + 3] = v.w;
+                        }
+                    } else if constexpr (sizeof(R) == 8 && RR % 2 == 0) {
+#pragma unroll
+                        for (int q2 = 0; q2 < RR / 2; ++q2) {
+                            const double2 v = reinterpret_cast<const double2*>(yi)[q2];
+                            yv[2 * q2] = v.x;
+                            yv[2 * q2 + 1] = v.y;
+                        }
+                    } else {
+#pragma unroll
+                        for (int u = 0; u < RR; ++u) yv[u] = yi[u];
+                    }
 #pragma unroll
                     for (int u = 0; u < RR; ++u) {
-                        const R y = yi[u];
+                        const R y = yv[u];
                         const R ur = fma(t.x, uc[u].x, fma(-t.y, uc[u].y, y));
                         const R ui = fma(t.x, uc[u].y, t.y * uc[u].x);
                         uc[u] = C{ur, ui};
                         const R sr = fma(ur, ur, -ui * ui);
-                        const R si = R(2) * ur * ui;
-                        pr[u].x = fma(sr, gp.x, fma(-si, gp.y, pr[u].x));
-                        pr[u].y = fma(sr, gp.y, fma(si, gp.x, pr[u].y));
+                        const R q = ur * ui;
+                        pr[u].x = fma(sr, gp.x, fma(-q, g2.y, pr[u].x));
+                        pr[u].y = fma(sr, gp.y, fma(q, g2.x, pr[u].y));
                     }
                 }
                 // each chunk's sum is formed from zero and added to the row sums
