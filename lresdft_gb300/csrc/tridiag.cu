@@ -25,7 +25,9 @@
 //                      tridiagonalisation of the full symmetric window matrix held in an
 //                      L2-resident working copy; the rank-2 updates of each panel of nb
 //                      columns are delayed (the panel's v and w vectors in shared memory)
-//                      and applied once per panel.  Algorithmic work (4/3) n^3 flops.
+//                      and applied once per panel; three barriers per column (the norm, the
+//                      dots and A x taken over the unscaled column in one phase).
+//                      Algorithmic work (4/3) n^3 flops.
 //   tri_apply_res_kernel  (FP32) one CTA per (window, block of up to 128 rows) with the
 //                      rows resident in shared memory through all panels: Y = F^ Q by
 //                      panels in compact WY form, Y <- Y - ((Y V) T_p) V^T, 4 x 4 register
