@@ -24,6 +24,7 @@ public drop-in API with a host potential in and a host density out every step.  
 from __future__ import annotations
 
 import argparse
+import datetime
 import json
 import os
 import subprocess
@@ -56,21 +57,54 @@ def read_peaks():
 
 
 class Clocks:
-    """nvidia-smi sampler during the timed region."""
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
-         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-         "clocks_event_reasons.sw_power_cap")
+    """nvidia-smi sampler (every 50 ms, timestamped) started before the warm-up; the clocks
+    reported are those of the samples taken inside the timed region (begin() / end()), or the
+    sample nearest to its middle when the region is shorter than the sampling interval."""
+    Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    NAMES = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
 
     def __init__(self):
         self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
         self.p = None
+        self.t0 = self.t1 = None
 
     def start(self):
         try:
             self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+                                       "-lms", "50"], stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.p = None
+
+    def begin(self):
+        self.t0 = datetime.datetime.now()
+
+    def end(self):
+        self.t1 = datetime.datetime.now()
+
+    @classmethod
+    def summarise(cls, lines, t0, t1):
+        """Clock record of the CSV lines of the samples within [t0, t1]."""
+        rows = []
+        for line in lines:
+            r = [x.strip() for x in line.split(",")]
+            if len(r) < 10:
+                continue
+            try:
+                ts = datetime.datetime.strptime(r[0], "%Y/%m/%d %H:%M:%S.%f")
+                rows.append((ts, float(r[2]), float(r[3]), [r[6 + i] == "Active" for i in range(4)]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "samples": 0, "reasons": ["no nvidia-smi samples"]}
+        inside = [x for x in rows if t0 <= x[0] <= t1]
+        if not inside:
+            mid = t0 + (t1 - t0) / 2
+            inside = [min(rows, key=lambda x: abs((x[0] - mid).total_seconds()))]
+        reasons = sorted({cls.NAMES[i] for x in inside for i in range(4) if x[3][i]})
+        return {"sm_mhz": float(np.median([x[1] for x in inside])), "sm_max_mhz": max(x[2] for x in inside),
+                "samples": len(inside), "sampled_every_ms": 50, "reasons": reasons}
 
     def stop(self):
         if self.p is None:
@@ -78,14 +112,10 @@ class Clocks:
         self.p.terminate()
         self.p.wait()
         self.f.flush()
-        rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines() if r.strip()]
+        lines = open(self.f.name).read().strip().splitlines()
         os.unlink(self.f.name)
-        sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].strip().replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if len(r) >= 9 and r[2].strip().replace(".", "").isdigit()]
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in rows if len(r) >= 9 for i in range(4) if r[5 + i].strip() == "Active"})
-        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "samples": len(rows), "reasons": reasons}
+        t1 = self.t1 or datetime.datetime.now()
+        return self.summarise(lines, self.t0 or t1, t1)
 
 
 def algorithmic_flops(nW, npoles):
@@ -268,16 +298,17 @@ def run_ours(args):
         s.set_potential_device(v_dev.data_ptr())
         return s.pole_pass_device(mu, e_lo)
 
+    clocks = Clocks()
+    clocks.start()                        # running before the timed region begins
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
     names = ("pole_kernel", "pole_sums", "assemble_h", "gather", "transform", "tri_reduce", "tri_rows")
     per = {k: [] for k in names}
-    clocks = Clocks()
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    clocks.start()
+    clocks.begin()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(args.steps):
@@ -287,6 +318,7 @@ def run_ours(args):
             per[k].append(t[k])
     e1.record()
     torch.cuda.synchronize()
+    clocks.end()
     clk = clocks.stop()
     ms_total = e0.elapsed_time(e1)
     if dist:
@@ -571,7 +603,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")

@@ -59,11 +59,15 @@ def test_reference_arm_loads_no_product_library():
 
 
 def test_clock_samples_parsed():
+    """Only the samples inside the timed region count; with none inside, the nearest one."""
+    import datetime
     import bench
     c = bench.Clocks()
-    c.f.write("0, 1965, 2070, 900.50, 0x0000000000000004, Not Active, Not Active, Not Active, Active\n"
-              "0, 1980, 2070, 950.10, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active\n"
-              "0, 2010, 2070, 990.00, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active\n")
+    c.f.write("2026/12/04 10:00:00.050, 0, 1200, 2070, 400.00, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active\n"
+              "2026/12/04 10:00:00.100, 0, 1965, 2070, 900.50, 0x0000000000000004, Not Active, Not Active, Not Active, Active\n"
+              "2026/12/04 10:00:00.150, 0, 1980, 2070, 950.10, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active\n"
+              "2026/12/04 10:00:00.200, 0, 2010, 2070, 990.00, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active\n"
+              "2026/12/04 10:00:00.250, 0, 1100, 2070, 300.00, 0x0000000000000000, Active, Not Active, Not Active, Not Active\n")
 
     class Proc:
         def terminate(self):
@@ -73,9 +77,16 @@ def test_clock_samples_parsed():
             pass
 
     c.p = Proc()
+    c.t0 = datetime.datetime(2026, 12, 4, 10, 0, 0, 90000)
+    c.t1 = datetime.datetime(2026, 12, 4, 10, 0, 0, 210000)
     out = c.stop()
     assert out["sm_mhz"] == 1980.0 and out["sm_max_mhz"] == 2070.0 and out["samples"] == 3
     assert out["reasons"] == ["sw_power_cap"]
+    t = datetime.datetime(2026, 12, 4, 10, 0, 0, 160000)
+    lines = ["2026/12/04 10:00:00.100, 0, 1965, 2070, 900.50, 0x0, Not Active, Not Active, Not Active, Not Active",
+             "2026/12/04 10:00:00.150, 0, 1980, 2070, 950.10, 0x0, Not Active, Not Active, Not Active, Not Active"]
+    near = bench.Clocks.summarise(lines, t, t + datetime.timedelta(milliseconds=5))
+    assert near["samples"] == 1 and near["sm_mhz"] == 1980.0
 
 
 def test_algorithmic_flops():
