@@ -72,6 +72,49 @@ def test_single_pass_matches_reference_density(systems, name, hpath):
     s.close()
 
 
+def _nonlocal_term(b, natoms, seed=7, k=2):
+    """A separable nonlocal term of the GTH form, sum over atoms of B_a h_a B_a^T (projectors
+    B_a on the atom's own functions, positive strengths h_a), as a CSR matrix over the basis."""
+    from scipy import sparse
+    rng = np.random.default_rng(seed)
+    rows, cols, vals = [], [], []
+    for a in range(natoms):
+        f = np.flatnonzero(b.atom_of_fn == a)
+        B = 0.3 * rng.standard_normal((len(f), k))
+        V = B @ np.diag(rng.uniform(0.1, 0.5, k)) @ B.T
+        V = 0.5 * (V + V.T)                             # exactly symmetric
+        ii, jj = np.meshgrid(f, f, indexing="ij")
+        rows.append(ii.ravel())
+        cols.append(jj.ravel())
+        vals.append(V.ravel())
+    nb = len(b.atom_of_fn)
+    return sparse.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(nb, nb))
+
+
+@pytest.mark.parametrize("route", ["tridiag", "ldl"])
+def test_nonlocal_hamiltonian_through_csr(systems, route):
+    """A Hamiltonian that is not an LCAO H(v): H(v) plus a separable nonlocal term of the form
+    a GTH pseudopotential adds (lrft/gth.py:105-232 assembles its H so), given through the CSR
+    entry point (lres_set_hamiltonian_csr, the H argument of lrft_windows): one FP64 pass at the
+    reference's (mu, e_lo) against the oracle's pole route on the same matrix, 1e-10 in the
+    density and 1e-9 in the band energy."""
+    from oracle import lrft_oracle as orc
+    g, cr, b = systems["jit2"]
+    v = g["v"].reshape(cr.shape)
+    H = (b.H(v) + _nonlocal_term(b, len(cr.pos))).tocsr()
+    H.sort_indices()
+    mu, e_lo = float(g["cold_mu"]), float(g["cold_elo"])
+    s = _solver(b, cr, g, route=route)
+    s.set_hamiltonian(H)
+    dens, N, eb = s.pole_pass(mu, e_lo)
+    ref, Nr, Er = orc.pole_density(H, b.S, b.Xr, s.windows, s.own, cr.ng, cr.dV, mu, e_lo, s.M)
+    s.close()
+    own = np.concatenate(s.own)
+    assert np.max(np.abs(dens[own] - ref[own])) < 1e-10
+    assert abs(eb - Er) < 1e-9 and abs(N - Nr) < 1e-9
+    assert abs(Nr - cr.n_elec) > 1e-3               # the term moved the electron count: H was used
+
+
 @pytest.mark.parametrize("name", CASES)
 def test_routes_agree(systems, name):
     """The tridiagonal route (the default) and the LDL^T route evaluate the same resolvent
