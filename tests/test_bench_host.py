@@ -1,7 +1,8 @@
 """bench.py's host side on the CPU: the reference arm's JSON line carries every key of the
 benchmark contract (run on a 2x2x2 crystal instead of the 1024-electron workload), the
-nvidia-smi clock samples are parsed into the `clocks` object, and the algorithmic work of
-the roofline is (32/3) n^3 real flops per window-pole solve."""
+nvidia-smi clock samples are parsed into the `clocks` object, the algorithmic work of
+the roofline is (32/3) n^3 real flops per window-pole solve, and the timed legs take the
+slowest of two gloo ranks."""
 import json
 import types
 
@@ -102,3 +103,38 @@ def test_reference_arm_other_ranks_do_nothing(monkeypatch, capsys):
     monkeypatch.setattr(bench, "build_system", lambda *a, **k: (_ for _ in ()).throw(AssertionError("ran")))
     bench.run_reference(types.SimpleNamespace(steps=1, warmup=3))
     assert capsys.readouterr().out == ""
+
+
+def _rank_main(rank, world, port, out):
+    import os
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import bench
+    ms = bench.max_over_ranks(10.0 + 5.0 * rank, dist, "cpu")       # rank 1 is the slower one
+    dist.barrier()
+    out.put((rank, ms))
+    dist.destroy_process_group()
+
+
+def test_max_over_ranks_two_gloo_ranks():
+    """Under torchrun every timed leg of our arm reports the slowest rank's time: two gloo ranks
+    on the CPU (spawned processes) both get the larger of their two times; without a process
+    group the value is returned as it is."""
+    import socket
+    import torch.multiprocessing as mp
+    import bench
+    assert bench.max_over_ranks(3.25, None, "cpu") == 3.25
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    out = ctx.Queue()
+    procs = [ctx.Process(target=_rank_main, args=(r, 2, port, out)) for r in range(2)]
+    for p in procs:
+        p.start()
+    got = sorted(out.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+    assert got == [(0, 15.0), (1, 15.0)]
+    assert all(p.exitcode == 0 for p in procs)
