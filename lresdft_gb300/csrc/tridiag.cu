@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(NT, reduce_min_ctas(NT, sizeof(R))) tri_reduce
     R* const qx = pv + ldv;                              // [ldv] q = A x (unsplit)
     R* const acol = qx + ldv;                            // [2][ldv] panel-start columns j, j+1
     R* const psum = acol + 2 * ldv;                      // [4 NT] split sums of A x
-    R* const dots = psum + 4 * NT;                       // [64] W^T v, V^T v
+    R* const dots = psum + 4 * NT;                       // [64] W^T x, V^T x, x^T x
     R* const red = dots + 64;                            // [NW]
     __shared__ int item_sh;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
